@@ -1,0 +1,582 @@
+// ev_api.cu -- library state, storage and the statevector run loop.
+//
+// The run loop restates StateVectorBackend::run_seeded
+// (src/backend/statevector.rs:77-90) and drive/apply_op
+// (src/backend/mod.rs:43-72) with the state resident on the device:
+//   - every op is a kernel on the state's stream; the host never waits
+//     inside a run;
+//   - the classical register lives in device memory, Measure writes its
+//     outcome there and IfClassic turns into a device predicate that the
+//     gated kernel reads before doing any work;
+//   - measurement uniforms come from the reference's Rng stream, drawn on the
+//     host one per Measure record in op order and consumed on the device
+//     through a counter, so a conditional Measure that does not run does not
+//     consume one (matching rng.next_f64() being called only inside
+//     measure_qubit).
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "ev_device.cuh"
+#include "ev_internal.h"
+
+namespace ev {
+
+static thread_local char g_err[512] = "";
+
+int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+void clear_error() { g_err[0] = 0; }
+
+__global__ void k_set_basis0_c128(double2* a) { a[0] = make_double2(1.0, 0.0); }
+__global__ void k_set_basis0_c64(float2* a) { a[0] = make_float2(1.0f, 0.0f); }
+
+__global__ void k_f64_to_c64(const double2* __restrict__ in, float2* __restrict__ out, uint64_t n) {
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride)
+    out[j] = make_float2(float(in[j].x), float(in[j].y));
+}
+__global__ void k_c64_to_f64(const float2* __restrict__ in, double2* __restrict__ out, uint64_t n) {
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride)
+    out[j] = make_double2(double(in[j].x), double(in[j].y));
+}
+
+static cudaEvent_t take_event(ev_state* s) {
+  if (!s->event_pool.empty()) {
+    cudaEvent_t e = s->event_pool.back();
+    s->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return e;
+}
+
+ProfScope::ProfScope(ev_state* st, int c, double b) : s(st), cls(c), bytes(b) {
+  if (s->profiling) {
+    a = take_event(s);
+    if (a) cudaEventRecord(a, s->stream);
+  }
+}
+
+ProfScope::~ProfScope() {
+  if (!a) return;
+  cudaEvent_t b = take_event(s);
+  if (!b) return;
+  cudaEventRecord(b, s->stream);
+  s->pending.push_back({cls, a, b, bytes});
+}
+
+void profile_flush(ev_state* s) {
+  for (const ProfRec& r : s->pending) {
+    float ms = 0.f;
+    if (cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      s->stats[r.cls].launches += 1;
+      s->stats[r.cls].ms += ms;
+      s->stats[r.cls].bytes += r.bytes;
+    } else {
+      cudaGetLastError();
+    }
+    s->event_pool.push_back(r.a);
+    s->event_pool.push_back(r.b);
+  }
+  s->pending.clear();
+}
+
+int state_zero(ev_state* s) {
+  s->launches += 1;
+  EV_CUDA(cudaMemsetAsync(s->amps, 0, s->len() * s->amp_bytes(), s->stream));
+  if (s->dtype == EV_C128)
+    k_set_basis0_c128<<<1, 1, 0, s->stream>>>(static_cast<double2*>(s->amps));
+  else
+    k_set_basis0_c64<<<1, 1, 0, s->stream>>>(static_cast<float2*>(s->amps));
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
+// ---- validation (src/circuit.rs:245-306) --------------------------------
+
+static int qubit_err(uint64_t q, uint64_t n) {
+  return fail(EV_ERR_QUBIT_OUT_OF_RANGE, "qubit q%llu out of range for %llu-qubit register",
+              (unsigned long long)q, (unsigned long long)n);
+}
+static int check_qubit(const ev_circuit* c, uint64_t q) {
+  return q < c->num_qubits ? EV_OK : qubit_err(q, c->num_qubits);
+}
+static int check_classical(const ev_circuit* c, uint64_t b) {
+  if (b < c->num_classical) return EV_OK;
+  return fail(EV_ERR_CLASSICAL_BIT_OUT_OF_RANGE,
+              "classical bit c%llu out of range for %llu-bit register", (unsigned long long)b,
+              (unsigned long long)c->num_classical);
+}
+
+static int validate_op(const ev_circuit* c, uint64_t* pos) {
+  if (*pos >= c->nops)
+    return fail(EV_ERR_INVALID_ARGUMENT, "op list ends inside an IfClassic record");
+  const ev_op& op = c->ops[*pos];
+  *pos += 1;
+  switch (op.kind) {
+    case EV_OP_APPLY1:
+      return check_qubit(c, op.q0);
+    case EV_OP_APPLY2:
+      EV_TRY(check_qubit(c, op.q0));
+      EV_TRY(check_qubit(c, op.q1));
+      if (op.q0 == op.q1)
+        return fail(EV_ERR_DUPLICATE_QUBIT, "qubit q%llu used more than once in a single gate",
+                    (unsigned long long)op.q0);
+      return EV_OK;
+    case EV_OP_CONTROLLED:
+      EV_TRY(check_qubit(c, op.q0));
+      if (op.nctrl && (!c->ctrl_pool || op.ctrl_off + op.nctrl > c->pool_len))
+        return fail(EV_ERR_INVALID_ARGUMENT, "control list outside the control pool");
+      for (uint32_t j = 0; j < op.nctrl; ++j) {
+        const uint64_t q = c->ctrl_pool[op.ctrl_off + j];
+        EV_TRY(check_qubit(c, q));
+        if (q == op.q0)
+          return fail(EV_ERR_DUPLICATE_QUBIT, "qubit q%llu used more than once in a single gate",
+                      (unsigned long long)q);
+      }
+      return EV_OK;
+    case EV_OP_MEASURE:
+      EV_TRY(check_qubit(c, op.q0));
+      return check_classical(c, op.q1);
+    case EV_OP_IF:
+      EV_TRY(check_classical(c, op.q0));
+      return validate_op(c, pos);
+    default:
+      return fail(EV_ERR_INVALID_ARGUMENT, "unknown op kind %u", op.kind);
+  }
+}
+
+static int validate(const ev_circuit* c) {
+  if (!c) return fail(EV_ERR_INVALID_ARGUMENT, "null circuit");
+  if (c->nops && !c->ops) return fail(EV_ERR_INVALID_ARGUMENT, "null op list");
+  uint64_t pos = 0;
+  while (pos < c->nops) EV_TRY(validate_op(c, &pos));
+  return EV_OK;
+}
+
+// ---- run --------------------------------------------------------------
+
+// Device buffers of one run: classical register, uniforms, nested-IF bits.
+struct RunBuffers {
+  uint8_t* classical = nullptr;
+  double* uniforms = nullptr;
+  uint64_t* ifbits = nullptr;
+  ~RunBuffers() {
+    if (classical) cudaFree(classical);
+    if (uniforms) cudaFree(uniforms);
+    if (ifbits) cudaFree(ifbits);
+  }
+};
+
+int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int tile_bits,
+              const uint8_t* pred, uint64_t* consumed);
+
+static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run_options* o,
+                   uint8_t* classical_out) {
+  const int mode = o ? o->mode : EV_MODE_EXACT;
+  const int tile_bits = o ? o->tile_bits : 0;
+  RunBuffers rb;
+  // count Measure records and the nesting of IF chains
+  uint64_t nmeas = 0, nif = 0;
+  for (uint64_t j = 0; j < c->nops; ++j) {
+    if (c->ops[j].kind == EV_OP_MEASURE) ++nmeas;
+    if (c->ops[j].kind == EV_OP_IF) ++nif;
+  }
+  const uint64_t ncl = c->num_classical ? c->num_classical : 1;
+  EV_CUDA(cudaMalloc(&rb.classical, ncl));
+  EV_CUDA(cudaMemsetAsync(rb.classical, 0, ncl, s->stream));
+  std::vector<double> uni(nmeas ? nmeas : 1, 0.0);
+  Rng rng(seed);
+  for (uint64_t j = 0; j < nmeas; ++j) uni[j] = rng.next_f64();
+  EV_CUDA(cudaMalloc(&rb.uniforms, uni.size() * sizeof(double)));
+  EV_CUDA(cudaMemcpyAsync(rb.uniforms, uni.data(), uni.size() * sizeof(double),
+                          cudaMemcpyHostToDevice, s->stream));
+  EV_CUDA(cudaMemsetAsync(s->scratch.counter, 0, sizeof(uint32_t), s->stream));
+  if (nif) EV_CUDA(cudaMalloc(&rb.ifbits, nif * sizeof(uint64_t)));
+  // The host copy of the nested-IF bit lists must outlive the async copy.
+  std::vector<uint64_t> host_ifbits(nif ? nif : 1);
+  uint64_t if_used = 0;
+  uint64_t pos = 0;
+  while (pos < c->nops) {
+    // collect an IF prefix chain
+    uint64_t chain[64];
+    int nchain = 0;
+    while (c->ops[pos].kind == EV_OP_IF) {
+      if (nchain < 64) chain[nchain++] = c->ops[pos].q0;
+      ++pos;
+    }
+    const uint8_t* pred = nullptr;
+    if (nchain == 1) {
+      pred = rb.classical + chain[0];
+    } else if (nchain > 1) {
+      std::memcpy(&host_ifbits[if_used], chain, nchain * sizeof(uint64_t));
+      EV_CUDA(cudaMemcpyAsync(rb.ifbits + if_used, &host_ifbits[if_used], nchain * sizeof(uint64_t),
+                              cudaMemcpyHostToDevice, s->stream));
+      EV_TRY(launch_pred_and(s, rb.classical, rb.ifbits + if_used, nchain, s->scratch.pred));
+      if_used += nchain;
+      pred = s->scratch.pred;
+    }
+    // tiled mode: fuse a run of unconditional gate records
+    if (mode == EV_MODE_TILED && nchain == 0 && c->ops[pos].kind != EV_OP_MEASURE) {
+      uint64_t end = pos;
+      while (end < c->nops && c->ops[end].kind != EV_OP_MEASURE && c->ops[end].kind != EV_OP_IF)
+        ++end;
+      uint64_t consumed = 0;
+      EV_TRY(tiled_run(s, c, pos, end, tile_bits, nullptr, &consumed));
+      pos = end;
+      continue;
+    }
+    const ev_op& op = c->ops[pos];
+    switch (op.kind) {
+      case EV_OP_APPLY1:
+        EV_TRY(launch_apply1(s, op.q0, op.m, pred));
+        break;
+      case EV_OP_APPLY2:
+        EV_TRY(launch_apply2(s, op.q0, op.q1, op.m, pred));
+        break;
+      case EV_OP_CONTROLLED: {
+        uint64_t mask = 0;
+        for (uint32_t j = 0; j < op.nctrl; ++j) mask |= uint64_t(1) << c->ctrl_pool[op.ctrl_off + j];
+        EV_TRY(launch_controlled(s, mask, op.q0, op.m, pred));
+        break;
+      }
+      case EV_OP_MEASURE:
+        EV_TRY(launch_measure(s, op.q0, 0.0, rb.uniforms, rb.classical + op.q1, pred));
+        break;
+    }
+    ++pos;
+  }
+  // complex64 runs end with an FP64 renormalisation: FP32-rounded gate
+  // matrices are unitary only to ~1e-7, and the drift of the norm over a deep
+  // circuit would otherwise dominate the error against the f64 result.
+  if (s->dtype == EV_C64) EV_TRY(launch_normalize(s));
+  if (c->num_classical) {
+    EV_CUDA(cudaMemcpyAsync(classical_out, rb.classical, c->num_classical, cudaMemcpyDeviceToHost,
+                            s->stream));
+  }
+  EV_CUDA(cudaStreamSynchronize(s->stream));
+  return EV_OK;
+}
+
+static int create_state(uint64_t n, int32_t dtype, ev_state** out) {
+  if (!out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_state_create: null output");
+  if (dtype != EV_C128 && dtype != EV_C64)
+    return fail(EV_ERR_INVALID_ARGUMENT, "unknown amplitude type %d", dtype);
+  if (n > 40) return fail(EV_ERR_OOM, "2^%llu amplitudes cannot be stored", (unsigned long long)n);
+  std::unique_ptr<ev_state> s(new ev_state());
+  s->n = n;
+  s->dtype = dtype;
+  EV_CUDA(cudaGetDevice(&s->device));
+  EV_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device));
+  const size_t bytes = size_t(s->len()) * s->amp_bytes();
+  cudaError_t e = cudaMalloc(&s->amps, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    s->amps = nullptr;
+    return fail(EV_ERR_OOM, "cannot allocate %zu bytes for a %llu-qubit state", bytes,
+                (unsigned long long)n);
+  }
+  const size_t sb = kMaxRedBlocks * 4 * sizeof(double) + 8 * sizeof(double) + 4 * sizeof(double) +
+                    64 + 16;
+  e = cudaMalloc(&s->scratch_block, sb);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(s->amps);
+    return fail(EV_ERR_OOM, "cannot allocate state scratch");
+  }
+  char* p = static_cast<char*>(s->scratch_block);
+  s->scratch.partials = reinterpret_cast<double*>(p);
+  p += kMaxRedBlocks * 4 * sizeof(double);
+  s->scratch.result = reinterpret_cast<double*>(p);
+  p += 8 * sizeof(double);
+  s->scratch.meas = reinterpret_cast<double*>(p);
+  p += 4 * sizeof(double);
+  s->scratch.pred = reinterpret_cast<uint8_t*>(p);
+  p += 64;
+  s->scratch.counter = reinterpret_cast<uint32_t*>(p);
+  e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    cudaFree(s->amps);
+    cudaFree(s->scratch_block);
+    return fail(EV_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+  }
+  int rc = state_zero(s.get());
+  if (rc == EV_OK) {
+    e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) rc = fail(EV_ERR_CUDA, "state init: %s", cudaGetErrorString(e));
+  }
+  if (rc != EV_OK) {
+    cudaFree(s->amps);
+    cudaFree(s->scratch_block);
+    cudaStreamDestroy(s->stream);
+    return rc;
+  }
+  *out = s.release();
+  return EV_OK;
+}
+
+}  // namespace ev
+
+using namespace ev;
+
+extern "C" const char* ev_last_error(void) { return g_err; }
+extern "C" const char* ev_version(void) { return "everett-gb300 0.1.0 (sm_103a)"; }
+
+extern "C" int ev_device_count(int* out) {
+  clear_error();
+  if (!out) return fail(EV_ERR_INVALID_ARGUMENT, "null output");
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  *out = n;
+  return EV_OK;
+}
+
+extern "C" int ev_state_create(uint64_t n, int32_t dtype, ev_state** out) {
+  clear_error();
+  return create_state(n, dtype, out);
+}
+
+extern "C" int ev_state_destroy(ev_state* s) {
+  clear_error();
+  if (!s) return EV_OK;
+  cudaSetDevice(s->device);
+  cudaStreamSynchronize(s->stream);
+  if (s->amps) cudaFree(s->amps);
+  if (s->scratch_block) cudaFree(s->scratch_block);
+  if (s->mass) cudaFree(s->mass);
+  profile_flush(s);
+  for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
+  for (cudaEvent_t e : s->slots)
+    if (e) cudaEventDestroy(e);
+  cudaStreamDestroy(s->stream);
+  delete s;
+  return EV_OK;
+}
+
+extern "C" int ev_state_num_qubits(const ev_state* s, uint64_t* out) {
+  if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "null argument");
+  *out = s->n;
+  return EV_OK;
+}
+
+extern "C" int ev_state_dtype(const ev_state* s, int32_t* out) {
+  if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "null argument");
+  *out = s->dtype;
+  return EV_OK;
+}
+
+extern "C" int ev_state_set_zero(ev_state* s) {
+  clear_error();
+  if (!s) return fail(EV_ERR_INVALID_ARGUMENT, "null state");
+  EV_CUDA(cudaSetDevice(s->device));
+  return state_zero(s);
+}
+
+extern "C" int ev_state_synchronize(const ev_state* s) {
+  clear_error();
+  if (!s) return fail(EV_ERR_INVALID_ARGUMENT, "null state");
+  EV_CUDA(cudaSetDevice(s->device));
+  EV_CUDA(cudaStreamSynchronize(s->stream));
+  return EV_OK;
+}
+
+// Staging size for complex64 conversions (complex amplitudes per chunk).
+static const uint64_t kStage = uint64_t(1) << 24;
+
+extern "C" int ev_state_upload(ev_state* s, const double* amps, uint64_t len) {
+  clear_error();
+  if (!s || (len && !amps)) return fail(EV_ERR_INVALID_ARGUMENT, "ev_state_upload: null argument");
+  if (len != s->len())
+    return fail(EV_ERR_DIMENSION_MISMATCH, "amplitude buffer has length %llu, expected %llu",
+                (unsigned long long)len, (unsigned long long)s->len());
+  EV_CUDA(cudaSetDevice(s->device));
+  if (s->dtype == EV_C128) {
+    EV_CUDA(cudaMemcpyAsync(s->amps, amps, len * 16, cudaMemcpyHostToDevice, s->stream));
+    EV_CUDA(cudaStreamSynchronize(s->stream));
+    return EV_OK;
+  }
+  const uint64_t chunk = len < kStage ? len : kStage;
+  double2* stage = nullptr;
+  EV_CUDA(cudaMalloc(&stage, chunk * 16));
+  int rc = EV_OK;
+  for (uint64_t off = 0; off < len && rc == EV_OK; off += chunk) {
+    const uint64_t cnt = (len - off) < chunk ? (len - off) : chunk;
+    cudaError_t e = cudaMemcpyAsync(stage, amps + 2 * off, cnt * 16, cudaMemcpyHostToDevice, s->stream);
+    if (e == cudaSuccess) {
+      k_f64_to_c64<<<unsigned((cnt + 255) / 256 < 4096 ? (cnt + 255) / 256 : 4096), 256, 0, s->stream>>>(
+          stage, static_cast<float2*>(s->amps) + off, cnt);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) rc = fail(EV_ERR_CUDA, "ev_state_upload: %s", cudaGetErrorString(e));
+  }
+  cudaFree(stage);
+  return rc;
+}
+
+extern "C" int ev_state_download(const ev_state* s, double* amps, uint64_t len) {
+  clear_error();
+  if (!s || (len && !amps)) return fail(EV_ERR_INVALID_ARGUMENT, "ev_state_download: null argument");
+  if (len != s->len())
+    return fail(EV_ERR_DIMENSION_MISMATCH, "amplitude buffer has length %llu, expected %llu",
+                (unsigned long long)len, (unsigned long long)s->len());
+  EV_CUDA(cudaSetDevice(s->device));
+  if (s->dtype == EV_C128) {
+    EV_CUDA(cudaMemcpyAsync(amps, s->amps, len * 16, cudaMemcpyDeviceToHost, s->stream));
+    EV_CUDA(cudaStreamSynchronize(s->stream));
+    return EV_OK;
+  }
+  const uint64_t chunk = len < kStage ? len : kStage;
+  double2* stage = nullptr;
+  EV_CUDA(cudaMalloc(&stage, chunk * 16));
+  int rc = EV_OK;
+  for (uint64_t off = 0; off < len && rc == EV_OK; off += chunk) {
+    const uint64_t cnt = (len - off) < chunk ? (len - off) : chunk;
+    k_c64_to_f64<<<unsigned((cnt + 255) / 256 < 4096 ? (cnt + 255) / 256 : 4096), 256, 0, s->stream>>>(
+        static_cast<const float2*>(s->amps) + off, stage, cnt);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(amps + 2 * off, stage, cnt * 16, cudaMemcpyDeviceToHost, s->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) rc = fail(EV_ERR_CUDA, "ev_state_download: %s", cudaGetErrorString(e));
+  }
+  cudaFree(stage);
+  return rc;
+}
+
+extern "C" int ev_validate(const ev_circuit* c) {
+  clear_error();
+  return validate(c);
+}
+
+extern "C" int ev_run_seeded(const ev_circuit* c, uint64_t seed, const ev_run_options* opts,
+                             ev_state** state_out, uint8_t* classical_out) {
+  clear_error();
+  EV_TRY(validate(c));
+  if (!state_out || (c->num_classical && !classical_out))
+    return fail(EV_ERR_INVALID_ARGUMENT, "ev_run_seeded: null output");
+  const int32_t dtype = opts ? opts->dtype : EV_C128;
+  ev_state* s = nullptr;
+  EV_TRY(create_state(c->num_qubits, dtype, &s));
+  const int rc = run_ops(s, c, seed, opts, classical_out);
+  if (rc != EV_OK) {
+    ev_state_destroy(s);
+    return rc;
+  }
+  *state_out = s;
+  return EV_OK;
+}
+
+extern "C" int ev_state_run(ev_state* s, const ev_circuit* c, uint64_t seed,
+                            const ev_run_options* opts, uint8_t* classical_out) {
+  clear_error();
+  if (!s) return fail(EV_ERR_INVALID_ARGUMENT, "ev_state_run: null state");
+  EV_TRY(validate(c));
+  if (c->num_qubits != s->n)
+    return fail(EV_ERR_DIMENSION_MISMATCH, "circuit has %llu qubits, state has %llu",
+                (unsigned long long)c->num_qubits, (unsigned long long)s->n);
+  if (opts && opts->dtype != s->dtype)
+    return fail(EV_ERR_INVALID_ARGUMENT, "run options name a different amplitude type");
+  if (c->num_classical && !classical_out)
+    return fail(EV_ERR_INVALID_ARGUMENT, "ev_state_run: null classical output");
+  EV_CUDA(cudaSetDevice(s->device));
+  EV_TRY(state_zero(s));
+  return run_ops(s, c, seed, opts, classical_out);
+}
+
+// ---- measurement hooks ------------------------------------------------------
+
+extern "C" int ev_state_record_event(ev_state* s, int32_t slot) {
+  clear_error();
+  if (!s || slot < 0 || slot >= 16) return fail(EV_ERR_INVALID_ARGUMENT, "bad event slot");
+  EV_CUDA(cudaSetDevice(s->device));
+  if (!s->slots[slot]) EV_CUDA(cudaEventCreate(&s->slots[slot]));
+  EV_CUDA(cudaEventRecord(s->slots[slot], s->stream));
+  return EV_OK;
+}
+
+extern "C" int ev_state_elapsed_ms(ev_state* s, int32_t from_slot, int32_t to_slot, float* ms) {
+  clear_error();
+  if (!s || !ms || from_slot < 0 || from_slot >= 16 || to_slot < 0 || to_slot >= 16 ||
+      !s->slots[from_slot] || !s->slots[to_slot])
+    return fail(EV_ERR_INVALID_ARGUMENT, "bad event slot");
+  EV_CUDA(cudaSetDevice(s->device));
+  EV_CUDA(cudaEventSynchronize(s->slots[to_slot]));
+  EV_CUDA(cudaEventElapsedTime(ms, s->slots[from_slot], s->slots[to_slot]));
+  return EV_OK;
+}
+
+extern "C" int ev_state_launch_count(const ev_state* s, uint64_t* out) {
+  if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "null argument");
+  *out = s->launches;
+  return EV_OK;
+}
+
+extern "C" int ev_state_profile(ev_state* s, int32_t enable) {
+  clear_error();
+  if (!s) return fail(EV_ERR_INVALID_ARGUMENT, "null state");
+  EV_CUDA(cudaSetDevice(s->device));
+  profile_flush(s);
+  if (enable)
+    for (auto& st : s->stats) st = ProfStat{};
+  s->profiling = enable != 0;
+  return EV_OK;
+}
+
+extern "C" int ev_state_profile_read(ev_state* s, ev_kernel_stat* out, int32_t max, int32_t* count) {
+  clear_error();
+  if (!s || !count || (max > 0 && !out)) return fail(EV_ERR_INVALID_ARGUMENT, "null argument");
+  EV_CUDA(cudaSetDevice(s->device));
+  profile_flush(s);
+  static const char* names[P_COUNT] = {"tile_pass", "gate", "measure", "sample",
+                                       "fused_unitary", "permute", "other"};
+  int w = 0;
+  for (int c = 0; c < P_COUNT; ++c) {
+    if (s->stats[c].launches == 0) continue;
+    if (w < max) {
+      std::memset(out[w].name, 0, sizeof(out[w].name));
+      std::strncpy(out[w].name, names[c], sizeof(out[w].name) - 1);
+      out[w].launches = s->stats[c].launches;
+      out[w].ms = s->stats[c].ms;
+      out[w].bytes = s->stats[c].bytes;
+    }
+    ++w;
+  }
+  *count = w;
+  return EV_OK;
+}
+
+extern "C" int ev_host_alloc(uint64_t bytes, void** out) {
+  clear_error();
+  if (!out) return fail(EV_ERR_INVALID_ARGUMENT, "null output");
+  cudaError_t e = cudaMallocHost(out, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *out = nullptr;
+    return fail(EV_ERR_OOM, "cudaMallocHost(%llu): %s", (unsigned long long)bytes, cudaGetErrorString(e));
+  }
+  return EV_OK;
+}
+
+extern "C" int ev_host_free(void* p) {
+  clear_error();
+  if (p) EV_CUDA(cudaFreeHost(p));
+  return EV_OK;
+}

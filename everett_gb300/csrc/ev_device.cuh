@@ -1,0 +1,79 @@
+// ev_device.cuh -- device arithmetic that reproduces the reference's
+// rounding steps.
+//
+// The CPU crate multiplies complex numbers in FMA form
+//   re = fma(a.re, b.re, -(a.im*b.im)),  im = fma(a.re, b.im, a.im*b.re)
+// (src/complex.rs:115-124) and adds them component-wise.  Every helper here
+// spells each rounding step with an explicit round-to-nearest intrinsic so
+// that neither the compiler's contraction nor reassociation can change a
+// result: in complex128 the engine's gate arithmetic is bit-identical to the
+// reference's (signed zeros aside).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+namespace ev {
+
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(__fma_rn(a.x, b.x, -__dmul_rn(a.y, b.y)),
+                      __fma_rn(a.x, b.y, __dmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(__fmaf_rn(a.x, b.x, -__fmul_rn(a.y, b.y)),
+                     __fmaf_rn(a.x, b.y, __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) {
+  return make_double2(__dadd_rn(a.x, b.x), __dadd_rn(a.y, b.y));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  return make_float2(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y));
+}
+// (r + 0i) * b in FMA form collapses to a rounded product per component:
+// fma(r, x, -(0*y)) == r*x for finite x, y.
+__device__ __forceinline__ double2 rmul(double r, double2 b) {
+  return make_double2(__dmul_rn(r, b.x), __dmul_rn(r, b.y));
+}
+__device__ __forceinline__ float2 rmul(float r, float2 b) {
+  return make_float2(__fmul_rn(r, b.x), __fmul_rn(r, b.y));
+}
+__device__ __forceinline__ double2 cneg(double2 a) { return make_double2(-a.x, -a.y); }
+__device__ __forceinline__ float2 cneg(float2 a) { return make_float2(-a.x, -a.y); }
+
+// norm_sqr = re.mul_add(re, im*im) (src/complex.rs:80-82), always in f64.
+__device__ __forceinline__ double nsq(double2 a) { return __fma_rn(a.x, a.x, __dmul_rn(a.y, a.y)); }
+__device__ __forceinline__ double nsq(float2 a) {
+  const double x = a.x, y = a.y;
+  return __fma_rn(x, x, __dmul_rn(y, y));
+}
+
+template <typename V>
+struct Real;
+template <>
+struct Real<double2> {
+  using T = double;
+};
+template <>
+struct Real<float2> {
+  using T = float;
+};
+
+template <typename V>
+__device__ __forceinline__ V mkv(double re, double im);
+template <>
+__device__ __forceinline__ double2 mkv<double2>(double re, double im) {
+  return make_double2(re, im);
+}
+template <>
+__device__ __forceinline__ float2 mkv<float2>(double re, double im) {
+  return make_float2(float(re), float(im));
+}
+
+// Inserts a 0 bit at position k of i (src/kernel.rs:39-44).
+__device__ __forceinline__ uint64_t insert0(uint64_t i, int k) {
+  const uint64_t low = (uint64_t(1) << k) - 1;
+  return ((i >> k) << (k + 1)) | (i & low);
+}
+
+}  // namespace ev

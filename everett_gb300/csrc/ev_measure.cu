@@ -1,0 +1,490 @@
+// ev_measure.cu -- FP64 reductions, Born-rule measurement, collapse and
+// shot sampling.
+//
+// measure_qubit (src/measure.rs:15-51) makes two passes: p1 = sum of
+// |a_j|^2 over j with bit k set, then outcome = u < p1 and the surviving half
+// is scaled by 1/sqrt(surviving) while the other half is zeroed.  Here:
+//   pass 1  k_reduce<P1>  one HBM read of the bit-k half; fixed-order block
+//                         partials, so results are deterministic run to run
+//   decide  k_decide      one thread: the reference's outcome and scale
+//                         formulas, with IEEE sqrt and division
+//   pass 2  k_collapse    reads only the kept half, writes both halves
+// The sum order differs from the reference's left-to-right loop, so p1 (and
+// the scale) agree to rounding (~1e-16 relative), not bit for bit; outcomes
+// agree unless u lies within that rounding of p1.
+//
+// State observables (src/state.rs:94-185) use the same reduction with other
+// terms.  Every reduction accumulates in f64 for both storage types.
+#include <cmath>
+#include <cstring>
+
+#include "ev_device.cuh"
+#include "ev_internal.h"
+
+namespace ev {
+
+enum RedOp { R_NORM = 0, R_P1, R_BLOCH, R_OVERLAP };
+
+constexpr int kRedThreads = 256;
+
+template <int OP, typename V>
+__device__ __forceinline__ void red_term(const V* __restrict__ a, const V* __restrict__ b,
+                                         uint64_t i, int k, double acc[4]) {
+  if constexpr (OP == R_NORM) {
+    acc[0] += nsq(a[i]);
+  } else if constexpr (OP == R_P1) {
+    acc[0] += nsq(a[insert0(i, k) | (uint64_t(1) << k)]);
+  } else if constexpr (OP == R_BLOCH) {
+    const uint64_t j0 = insert0(i, k), j1 = j0 | (uint64_t(1) << k);
+    const V x = a[j0], y = a[j1];
+    const double2 x2 = make_double2(x.x, x.y), y2 = make_double2(y.x, -double(y.y));
+    acc[0] += nsq(x2);
+    acc[1] += nsq(y2);
+    const double2 r = cmul(x2, y2);  // amp * partner.conj()
+    acc[2] += r.x;
+    acc[3] += r.y;
+  } else {  // R_OVERLAP: conj(other_j) * self_j
+    const V x = a[i], y = b[i];
+    const double2 r = cmul(make_double2(y.x, -double(y.y)), make_double2(x.x, x.y));
+    acc[0] += r.x;
+    acc[1] += r.y;
+  }
+}
+
+// Block b reduces the contiguous counter range [b*chunk, (b+1)*chunk) and
+// writes 4 partials; the tree inside the block has a fixed shape.
+template <int OP, typename V>
+__global__ void __launch_bounds__(kRedThreads)
+    k_reduce(const V* __restrict__ a, const V* __restrict__ b, uint64_t count, uint64_t chunk,
+             int k, double* __restrict__ partials, const uint8_t* pred) {
+  if (pred != nullptr && *pred == 0) return;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
+  const uint64_t hi = lo + chunk < count ? lo + chunk : count;
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) red_term<OP>(a, b, i, k, acc);
+  __shared__ double sh[4][kRedThreads];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) sh[c][threadIdx.x] = acc[c];
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) partials[blockIdx.x * 4 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// Sums nblocks x 4 partials in a fixed order into result[0..4).
+__global__ void __launch_bounds__(kRedThreads)
+    k_finish(const double* __restrict__ partials, int nblocks, double* __restrict__ result,
+             const uint8_t* pred) {
+  if (pred != nullptr && *pred == 0) return;
+  __shared__ double sh[4][kRedThreads];
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (int b = threadIdx.x; b < nblocks; b += kRedThreads)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[c] += partials[b * 4 + c];
+#pragma unroll
+  for (int c = 0; c < 4; ++c) sh[c][threadIdx.x] = acc[c];
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) result[threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// outcome = u < p1; surviving = outcome ? p1 : 1 - p1;
+// scale = surviving > 0 ? 1/sqrt(surviving) : 0   (measure.rs:29-38).
+__global__ void k_decide(const double* __restrict__ result, double u_host,
+                         const double* __restrict__ u_dev, uint32_t* __restrict__ counter,
+                         double* __restrict__ meas, uint8_t* __restrict__ outcome_dev,
+                         const uint8_t* pred) {
+  if (pred != nullptr && *pred == 0) return;
+  const double p1 = result[0];
+  double u = u_host;
+  if (u_dev != nullptr) u = u_dev[counter[0]++];
+  const bool outcome = u < p1;
+  const double surviving = outcome ? p1 : __dadd_rn(1.0, -p1);
+  const double scale = surviving > 0.0 ? __ddiv_rn(1.0, __dsqrt_rn(surviving)) : 0.0;
+  meas[0] = p1;
+  meas[1] = scale;
+  meas[2] = outcome ? 1.0 : 0.0;
+  meas[3] = u;
+  if (outcome_dev != nullptr) *outcome_dev = outcome ? 1 : 0;
+}
+
+template <typename V>
+__device__ __forceinline__ V scale_amp(V a, double s) {
+  if constexpr (sizeof(V) == 16)
+    return make_double2(__dmul_rn(a.x, s), __dmul_rn(a.y, s));
+  else
+    return make_float2(float(__dmul_rn(double(a.x), s)), float(__dmul_rn(double(a.y), s)));
+}
+
+// Pass 2 of measure_qubit (measure.rs:40-48).
+template <typename V>
+__global__ void __launch_bounds__(256)
+    k_collapse(V* __restrict__ a, uint64_t npairs, int k, const double* __restrict__ meas,
+               const uint8_t* pred) {
+  if (pred != nullptr && *pred == 0) return;
+  const double scale = meas[1];
+  const bool one = meas[2] != 0.0;
+  const uint64_t bit = uint64_t(1) << k;
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  V zero;
+  zero.x = 0;
+  zero.y = 0;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < npairs; i += stride) {
+    const uint64_t j0 = insert0(i, k), j1 = j0 | bit;
+    const uint64_t keep = one ? j1 : j0, drop = one ? j0 : j1;
+    a[keep] = scale_amp(a[keep], scale);
+    a[drop] = zero;
+  }
+}
+
+// State::normalize (state.rs:103-111): norm = sqrt(norm_sqr); inv = 1/norm.
+template <typename V>
+__global__ void __launch_bounds__(256)
+    k_normalize(V* __restrict__ a, uint64_t len, const double* __restrict__ result) {
+  const double norm = __dsqrt_rn(result[0]);
+  if (!(norm > 0.0)) return;
+  const double inv = __ddiv_rn(1.0, norm);
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < len; j += stride)
+    a[j] = scale_amp(a[j], inv);
+}
+
+__global__ void k_pred_and(const uint8_t* __restrict__ classical, const uint64_t* bits, int nbits,
+                           uint8_t* out) {
+  uint8_t v = 1;
+  for (int i = 0; i < nbits; ++i) v = v && classical[bits[i]];
+  *out = v;
+}
+
+// ---- sampling tree --------------------------------------------------------
+// mass level q (2^q entries) lives at offset 2^q - 1.  mass[n-1][r] =
+// |a_r|^2 + |a_{r+2^(n-1)}|^2 and mass[q][r] = mass[q+1][r] + mass[q+1][r+2^q].
+
+template <typename V>
+__global__ void __launch_bounds__(256)
+    k_mass_leaf(const V* __restrict__ a, uint64_t half, double* __restrict__ out) {
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < half; r += stride)
+    out[r] = __dadd_rn(nsq(a[r]), nsq(a[r + half]));
+}
+
+__global__ void __launch_bounds__(256)
+    k_mass_level(const double* __restrict__ in, uint64_t w, double* __restrict__ out) {
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < w; r += stride)
+    out[r] = __dadd_rn(in[r], in[r + w]);
+}
+
+// Levels top..0 of the tree in one block (level top already built).
+__global__ void __launch_bounds__(1024) k_mass_top(double* __restrict__ mass, int top) {
+  for (int q = top - 1; q >= 0; --q) {
+    const uint64_t w = uint64_t(1) << q;
+    const double* in = mass + (2 * w - 1);
+    double* out = mass + (w - 1);
+    for (uint64_t r = threadIdx.x; r < w; r += blockDim.x) out[r] = __dadd_rn(in[r], in[r + w]);
+    __syncthreads();
+  }
+}
+
+// One thread per shot: descend the tree with n uniforms (qubits 0..n-1).
+template <typename V>
+__global__ void __launch_bounds__(256)
+    k_descend(const double* __restrict__ mass, const V* __restrict__ a, int n,
+              const double* __restrict__ uni, uint64_t shots, uint64_t* __restrict__ out) {
+  const uint64_t s = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= shots) return;
+  uint64_t r = 0;
+  for (int q = 0; q < n; ++q) {
+    const uint64_t w = uint64_t(1) << q;
+    const double m = mass[(w - 1) + r];
+    const double m1 = (q + 1 < n) ? mass[(2 * w - 1) + r + w] : nsq(a[r + w]);
+    const double p1 = __ddiv_rn(m1, m);
+    if (uni[s * uint64_t(n) + q] < p1) r |= w;
+  }
+  out[s] = r;
+}
+
+// ---- host ------------------------------------------------------------------
+
+template <int OP>
+static int reduce(const ev_state* s, const ev_state* other, uint64_t count, int k,
+                  const uint8_t* pred) {
+  const uint64_t want = (count + 4095) / 4096;
+  int nb = int(want < 1 ? 1 : want);
+  const int cap = s->num_sms * 4 < kMaxRedBlocks ? s->num_sms * 4 : kMaxRedBlocks;
+  if (nb > cap) nb = cap;
+  const uint64_t chunk = (count + nb - 1) / nb;
+  if (s->dtype == EV_C128)
+    k_reduce<OP, double2><<<nb, kRedThreads, 0, s->stream>>>(
+        static_cast<const double2*>(s->amps),
+        other ? static_cast<const double2*>(other->amps) : nullptr, count, chunk, k,
+        s->scratch.partials, pred);
+  else
+    k_reduce<OP, float2><<<nb, kRedThreads, 0, s->stream>>>(
+        static_cast<const float2*>(s->amps),
+        other ? static_cast<const float2*>(other->amps) : nullptr, count, chunk, k,
+        s->scratch.partials, pred);
+  k_finish<<<1, kRedThreads, 0, s->stream>>>(s->scratch.partials, nb, s->scratch.result, pred);
+  s->launches += 2;
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
+static unsigned grid_for(const ev_state* s, uint64_t work) {
+  const uint64_t want = (work + 255) / 256;
+  const uint64_t cap = uint64_t(s->num_sms) * 8;
+  return unsigned(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
+int launch_measure(ev_state* s, uint64_t k, double u_host, const double* u_dev,
+                   uint8_t* outcome_dev, const uint8_t* pred) {
+  // pass 1 reads the bit-k half; pass 2 reads the kept half and writes all
+  ProfScope prof(s, P_MEASURE, 2.0 * double(s->len()) * double(s->amp_bytes()));
+  s->launches += 2;
+  EV_TRY(reduce<R_P1>(s, nullptr, s->len() / 2, int(k), pred));
+  k_decide<<<1, 1, 0, s->stream>>>(s->scratch.result, u_host, u_dev, s->scratch.counter,
+                                   s->scratch.meas, outcome_dev, pred);
+  const uint64_t np = s->len() / 2;
+  if (s->dtype == EV_C128)
+    k_collapse<double2><<<grid_for(s, np), 256, 0, s->stream>>>(
+        static_cast<double2*>(s->amps), np, int(k), s->scratch.meas, pred);
+  else
+    k_collapse<float2><<<grid_for(s, np), 256, 0, s->stream>>>(
+        static_cast<float2*>(s->amps), np, int(k), s->scratch.meas, pred);
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
+int launch_pred_and(ev_state* s, const uint8_t* classical, const uint64_t* bits, int nbits,
+                    uint8_t* pred_out) {
+  k_pred_and<<<1, 1, 0, s->stream>>>(classical, bits, nbits, pred_out);
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
+static int fetch_result(const ev_state* s, double* out, int count) {
+  EV_CUDA(cudaMemcpyAsync(out, s->scratch.result, sizeof(double) * count, cudaMemcpyDeviceToHost,
+                          s->stream));
+  EV_CUDA(cudaStreamSynchronize(s->stream));
+  return EV_OK;
+}
+
+int reduce_norm(const ev_state* s, double* out_host) {
+  EV_TRY(reduce<R_NORM>(s, nullptr, s->len(), 0, nullptr));
+  return fetch_result(s, out_host, 1);
+}
+
+static int ensure_mass(ev_state* s) {
+  const uint64_t need = s->len() - 1;
+  if (s->mass && s->mass_len >= need) return EV_OK;
+  if (s->mass) cudaFree(s->mass);
+  s->mass = nullptr;
+  s->mass_len = 0;
+  void* p = nullptr;
+  EV_CUDA(cudaMalloc(&p, need * sizeof(double)));
+  s->mass = static_cast<double*>(p);
+  s->mass_len = need;
+  return EV_OK;
+}
+
+static int build_mass(ev_state* s) {
+  const int n = int(s->n);
+  ProfScope prof(s, P_SAMPLE, double(s->len()) * double(s->amp_bytes()) + 16.0 * double(s->len()));
+  s->launches += 1 + (n - 2 >= 12 ? n - 13 : 0) + 1;
+  double* mass = s->mass;
+  const uint64_t half = s->len() / 2;
+  double* top = mass + (half - 1);  // level n-1
+  if (s->dtype == EV_C128)
+    k_mass_leaf<double2><<<grid_for(s, half), 256, 0, s->stream>>>(
+        static_cast<const double2*>(s->amps), half, top);
+  else
+    k_mass_leaf<float2><<<grid_for(s, half), 256, 0, s->stream>>>(
+        static_cast<const float2*>(s->amps), half, top);
+  int q = n - 2;
+  for (; q >= 12; --q) {
+    const uint64_t w = uint64_t(1) << q;
+    k_mass_level<<<grid_for(s, w), 256, 0, s->stream>>>(mass + (2 * w - 1), w, mass + (w - 1));
+  }
+  if (q >= 0) k_mass_top<<<1, 1024, 0, s->stream>>>(mass, q + 1);
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
+}  // namespace ev
+
+using namespace ev;
+
+extern "C" int ev_measure_qubit(ev_state* s, uint64_t k, double u, int32_t* outcome) {
+  clear_error();
+  if (!s || !outcome) return fail(EV_ERR_INVALID_ARGUMENT, "ev_measure_qubit: null argument");
+  if (k >= s->n)
+    return fail(EV_ERR_QUBIT_OUT_OF_RANGE, "qubit q%llu out of range for %llu-qubit register",
+                (unsigned long long)k, (unsigned long long)s->n);
+  EV_CUDA(cudaSetDevice(s->device));
+  EV_TRY(launch_measure(s, k, u, nullptr, nullptr, nullptr));
+  double meas[4];
+  EV_CUDA(cudaMemcpyAsync(meas, s->scratch.meas, sizeof(meas), cudaMemcpyDeviceToHost, s->stream));
+  EV_CUDA(cudaStreamSynchronize(s->stream));
+  *outcome = meas[2] != 0.0 ? 1 : 0;
+  return EV_OK;
+}
+
+extern "C" int ev_norm_sqr(const ev_state* s, double* out) {
+  clear_error();
+  if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_norm_sqr: null argument");
+  EV_CUDA(cudaSetDevice(s->device));
+  return reduce_norm(s, out);
+}
+
+int ev::launch_normalize(ev_state* s) {
+  ProfScope prof(s, P_OTHER, 3.0 * double(s->len()) * double(s->amp_bytes()));
+  EV_TRY(reduce<R_NORM>(s, nullptr, s->len(), 0, nullptr));
+  s->launches += 1;
+  if (s->dtype == EV_C128)
+    k_normalize<double2><<<grid_for(s, s->len()), 256, 0, s->stream>>>(
+        static_cast<double2*>(s->amps), s->len(), s->scratch.result);
+  else
+    k_normalize<float2><<<grid_for(s, s->len()), 256, 0, s->stream>>>(
+        static_cast<float2*>(s->amps), s->len(), s->scratch.result);
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
+extern "C" int ev_normalize(ev_state* s) {
+  clear_error();
+  if (!s) return fail(EV_ERR_INVALID_ARGUMENT, "ev_normalize: null argument");
+  EV_CUDA(cudaSetDevice(s->device));
+  EV_TRY(launch_normalize(s));
+  EV_CUDA(cudaStreamSynchronize(s->stream));
+  return EV_OK;
+}
+
+// State::probability: one amplitude, norm_sqr on the host with std::fma
+// (state.rs:119-122).
+extern "C" int ev_probability(const ev_state* s, uint64_t basis, double* out) {
+  clear_error();
+  if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_probability: null argument");
+  if (basis >= s->len())
+    return fail(EV_ERR_INVALID_ARGUMENT, "basis state %llu out of range", (unsigned long long)basis);
+  EV_CUDA(cudaSetDevice(s->device));
+  double re, im;
+  if (s->dtype == EV_C128) {
+    double v[2];
+    EV_CUDA(cudaMemcpyAsync(v, static_cast<const double2*>(s->amps) + basis, 16,
+                            cudaMemcpyDeviceToHost, s->stream));
+    EV_CUDA(cudaStreamSynchronize(s->stream));
+    re = v[0];
+    im = v[1];
+  } else {
+    float v[2];
+    EV_CUDA(cudaMemcpyAsync(v, static_cast<const float2*>(s->amps) + basis, 8,
+                            cudaMemcpyDeviceToHost, s->stream));
+    EV_CUDA(cudaStreamSynchronize(s->stream));
+    re = v[0];
+    im = v[1];
+  }
+  *out = std::fma(re, re, im * im);
+  return EV_OK;
+}
+
+extern "C" int ev_overlap(const ev_state* self, const ev_state* other, double out[2]) {
+  clear_error();
+  if (!self || !other || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_overlap: null argument");
+  if (self->n != other->n)
+    return fail(EV_ERR_DIMENSION_MISMATCH, "states must have equal qubit counts (%llu vs %llu)",
+                (unsigned long long)self->n, (unsigned long long)other->n);
+  if (self->dtype != other->dtype)
+    return fail(EV_ERR_INVALID_ARGUMENT, "states must have the same amplitude type");
+  EV_CUDA(cudaSetDevice(self->device));
+  // other's pending work must be complete before self's stream reads it
+  EV_CUDA(cudaStreamSynchronize(other->stream));
+  EV_TRY(reduce<R_OVERLAP>(self, other, self->len(), 0, nullptr));
+  double r[2];
+  EV_TRY(fetch_result(self, r, 2));
+  out[0] = r[0];
+  out[1] = r[1];
+  return EV_OK;
+}
+
+// State::fidelity = |<other|self>|^2 with the FMA-form norm (state.rs:149-151).
+extern "C" int ev_fidelity(const ev_state* self, const ev_state* other, double* out) {
+  if (!out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_fidelity: null argument");
+  double ov[2];
+  EV_TRY(ev_overlap(self, other, ov));
+  *out = std::fma(ov[0], ov[0], ov[1] * ov[1]);
+  return EV_OK;
+}
+
+extern "C" int ev_bloch_vector(const ev_state* s, uint64_t qubit, double out[3]) {
+  clear_error();
+  if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_bloch_vector: null argument");
+  if (qubit >= s->n)
+    return fail(EV_ERR_QUBIT_OUT_OF_RANGE, "qubit q%llu out of range for %llu-qubit register",
+                (unsigned long long)qubit, (unsigned long long)s->n);
+  EV_CUDA(cudaSetDevice(s->device));
+  EV_TRY(reduce<R_BLOCH>(s, nullptr, s->len() / 2, int(qubit), nullptr));
+  double r[4];
+  EV_TRY(fetch_result(s, r, 4));
+  out[0] = 2.0 * r[2];
+  out[1] = 2.0 * r[3];
+  out[2] = r[0] - r[1];
+  return EV_OK;
+}
+
+extern "C" int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* out) {
+  clear_error();
+  if (!s || (shots && !out)) return fail(EV_ERR_INVALID_ARGUMENT, "ev_sample: null argument");
+  if (s->n > 63) return fail(EV_ERR_INVALID_ARGUMENT, "ev_sample: at most 63 qubits");
+  if (shots == 0) return EV_OK;
+  if (s->n == 0) {
+    std::memset(out, 0, shots * sizeof(uint64_t));
+    return EV_OK;
+  }
+  EV_CUDA(cudaSetDevice(s->device));
+  EV_TRY(ensure_mass(s));
+  EV_TRY(build_mass(s));
+  const uint64_t nu = shots * s->n;
+  std::vector<double> uni(nu);
+  Rng rng(seed);
+  for (uint64_t j = 0; j < nu; ++j) uni[j] = rng.next_f64();
+  void* du = nullptr;
+  void* dout = nullptr;
+  EV_CUDA(cudaMalloc(&du, nu * sizeof(double)));
+  int rc = EV_OK;
+  if (cudaMalloc(&dout, shots * sizeof(uint64_t)) != cudaSuccess) {
+    cudaGetLastError();
+    cudaFree(du);
+    return fail(EV_ERR_OOM, "ev_sample: cannot allocate %llu shots", (unsigned long long)shots);
+  }
+  cudaError_t e = cudaMemcpyAsync(du, uni.data(), nu * sizeof(double), cudaMemcpyHostToDevice,
+                                  s->stream);
+  if (e == cudaSuccess) {
+    const unsigned g = unsigned((shots + 255) / 256);
+    s->launches += 1;
+    if (s->dtype == EV_C128)
+      k_descend<double2><<<g, 256, 0, s->stream>>>(s->mass, static_cast<const double2*>(s->amps),
+                                                   int(s->n), static_cast<const double*>(du),
+                                                   shots, static_cast<uint64_t*>(dout));
+    else
+      k_descend<float2><<<g, 256, 0, s->stream>>>(s->mass, static_cast<const float2*>(s->amps),
+                                                  int(s->n), static_cast<const double*>(du), shots,
+                                                  static_cast<uint64_t*>(dout));
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, dout, shots * sizeof(uint64_t), cudaMemcpyDeviceToHost, s->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) rc = fail(EV_ERR_CUDA, "ev_sample: %s", cudaGetErrorString(e));
+  cudaFree(du);
+  cudaFree(dout);
+  return rc;
+}

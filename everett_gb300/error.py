@@ -1,0 +1,67 @@
+"""Errors of the engine, mirroring everett::Error (src/error.rs:10-53).
+
+The first four classes correspond one-to-one to the reference's variants that
+the statevector path can raise; the rest are device conditions the CPU crate
+has no counterpart for.
+"""
+from __future__ import annotations
+
+from . import _native as N
+
+
+class EverettError(Exception):
+    """Base class; ``code`` is the C ABI's EV_ERR_* value."""
+
+    code = -1
+
+
+class QubitOutOfRange(EverettError):
+    code = N.ERR_QUBIT_OUT_OF_RANGE
+
+
+class ClassicalBitOutOfRange(EverettError):
+    code = N.ERR_CLASSICAL_BIT_OUT_OF_RANGE
+
+
+class DuplicateQubit(EverettError):
+    code = N.ERR_DUPLICATE_QUBIT
+
+
+class DimensionMismatch(EverettError):
+    code = N.ERR_DIMENSION_MISMATCH
+
+
+class InvalidArgument(EverettError):
+    code = N.ERR_INVALID_ARGUMENT
+
+
+class DeviceOutOfMemory(EverettError):
+    code = N.ERR_OOM
+
+
+class CudaError(EverettError):
+    code = N.ERR_CUDA
+
+
+class DeviceTimeout(EverettError):
+    code = N.ERR_TIMEOUT
+
+
+class AdmissionRefused(EverettError):
+    code = N.ERR_ADMISSION
+
+
+class Cancelled(EverettError):
+    code = N.ERR_CANCELLED
+
+
+_BY_CODE = {cls.code: cls for cls in (
+    QubitOutOfRange, ClassicalBitOutOfRange, DuplicateQubit, DimensionMismatch, InvalidArgument,
+    DeviceOutOfMemory, CudaError, DeviceTimeout, AdmissionRefused, Cancelled)}
+
+
+def error_for_code(code: int, message: str) -> EverettError:
+    cls = _BY_CODE.get(code, EverettError)
+    err = cls(message or f"error code {code}")
+    err.code = code
+    return err

@@ -1,0 +1,212 @@
+/*
+ * everett_cuda.h -- C ABI of the GB300 statevector engine.
+ *
+ * This is the drop-in boundary for everett's dense statevector run path
+ * (`StateVectorBackend::run(&Circuit) -> Result<Execution>`,
+ * src/backend/statevector.rs:68-90).  Every entry point takes plain pointers
+ * and sizes, returns 0 (EV_OK) or an EV_ERR_* code, and records a message
+ * readable through ev_last_error() on the calling thread.
+ *
+ * Conventions
+ *   - Qubit 0 is the least-significant bit of a basis index
+ *     (src/qubit.rs:9-14).
+ *   - Complex numbers travel as interleaved f64 pairs [re, im], the layout of
+ *     the reference's #[repr(C)] Complex64 (src/complex.rs:22-29).
+ *   - A 1-qubit matrix is 4 complex entries row-major [m00, m01, m10, m11]
+ *     (src/gate.rs:21-25) = 8 doubles.  A 2-qubit matrix is 16 complex entries
+ *     row-major in the basis |q_a q_b> with a the more significant operand
+ *     (src/gate.rs:27-35) = 32 doubles.
+ *   - The library owns device memory; callers own every host buffer.
+ *   - A state handle is used from one host thread at a time.  Each state owns
+ *     its own CUDA stream, so work on different states may overlap.
+ */
+#ifndef EVERETT_CUDA_H
+#define EVERETT_CUDA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- error codes ---------------------------------------------------------
+ * The first four mirror the variants of everett::Error that the statevector
+ * path can raise (src/error.rs:10-53); the rest are device-side conditions
+ * the CPU crate cannot meet. */
+enum {
+  EV_OK = 0,
+  EV_ERR_QUBIT_OUT_OF_RANGE = 1,         /* Error::QubitOutOfRange        */
+  EV_ERR_CLASSICAL_BIT_OUT_OF_RANGE = 2, /* Error::ClassicalBitOutOfRange */
+  EV_ERR_DUPLICATE_QUBIT = 3,            /* Error::DuplicateQubit         */
+  EV_ERR_DIMENSION_MISMATCH = 4,         /* Error::DimensionMismatch      */
+  EV_ERR_INVALID_ARGUMENT = 16, /* null pointer, bad dtype, malformed op list */
+  EV_ERR_OOM = 17,              /* device allocation refused              */
+  EV_ERR_CUDA = 18,             /* a CUDA runtime call failed             */
+  EV_ERR_TIMEOUT = 19,          /* a bounded device wait gave up          */
+  EV_ERR_ADMISSION = 20,        /* serve: request can never fit in HBM    */
+  EV_ERR_CANCELLED = 21         /* serve: request cancelled before it ran */
+};
+
+/* amplitude storage types */
+enum { EV_C128 = 0, EV_C64 = 1 };
+
+/* ---- operations ----------------------------------------------------------
+ * One ev_op per everett::Op variant (src/op.rs:14-58).  IfClassic
+ * (`Op::IfClassic { bit, then: Box<Op> }`) is encoded in prefix form: an
+ * EV_OP_IF record with q0 = the classical bit is followed by the record(s)
+ * of its body, which may itself be another EV_OP_IF. */
+enum {
+  EV_OP_APPLY1 = 1,     /* gate m[0..8)  on target q0                      */
+  EV_OP_APPLY2 = 2,     /* gate m[0..32) on operands a = q0, b = q1        */
+  EV_OP_CONTROLLED = 3, /* gate m[0..8) on target q0, controls in the pool */
+  EV_OP_MEASURE = 4,    /* measure qubit q0 into classical bit q1          */
+  EV_OP_IF = 5          /* run the next op only if classical bit q0 is set */
+};
+
+typedef struct ev_op {
+  uint32_t kind;     /* EV_OP_*                                            */
+  uint32_t nctrl;    /* EV_OP_CONTROLLED: number of controls               */
+  uint64_t ctrl_off; /* EV_OP_CONTROLLED: index of first control in pool   */
+  uint64_t q0;
+  uint64_t q1;
+  double m[32];      /* interleaved re,im; 8 used by 1-qubit gates         */
+} ev_op;
+
+/* A circuit: register sizes, the op list and the pool of control indices
+ * (`Circuit { ops, num_qubits, num_classical }`, src/circuit.rs:26-30). */
+typedef struct ev_circuit {
+  uint64_t num_qubits;
+  uint64_t num_classical;
+  const ev_op* ops;
+  uint64_t nops;
+  const uint64_t* ctrl_pool;
+  uint64_t pool_len;
+} ev_circuit;
+
+/* Execution options of the run loop. */
+enum {
+  EV_MODE_EXACT = 0, /* one kernel per op, the reference's arithmetic order */
+  EV_MODE_TILED = 1  /* runs of low-qubit ops applied in one shared-memory
+                        pass; same per-amplitude arithmetic, fewer passes  */
+};
+typedef struct ev_run_options {
+  int32_t dtype;     /* EV_C128 or EV_C64                                  */
+  int32_t mode;      /* EV_MODE_*                                          */
+  int32_t tile_bits; /* tiled mode: qubits per shared-memory tile (0=auto) */
+  int32_t reserved;
+} ev_run_options;
+
+typedef struct ev_state ev_state;
+
+/* ---- library ---------------------------------------------------------- */
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* ev_last_error(void);
+/* Version string of the library. */
+const char* ev_version(void);
+/* Number of CUDA devices the library can see (0 on a host without a GPU). */
+int ev_device_count(int* out);
+
+/* ---- state storage (src/state.rs:24-90) ------------------------------- */
+
+/* |0...0> on n qubits (State::zero, src/state.rs:39-44).  EV_ERR_OOM if the
+ * 2^n x 16 (or 8) byte buffer does not fit. */
+int ev_state_create(uint64_t n, int32_t dtype, ev_state** out);
+int ev_state_destroy(ev_state* s);
+int ev_state_num_qubits(const ev_state* s, uint64_t* out);
+int ev_state_dtype(const ev_state* s, int32_t* out);
+/* Reset to |0...0>. */
+int ev_state_set_zero(ev_state* s);
+/* Copy 2^n complex amplitudes (interleaved f64) into / out of the state
+ * (State::from_amplitudes / amplitudes, src/state.rs:51-90).  len is the
+ * number of complex amplitudes; EV_ERR_DIMENSION_MISMATCH unless len == 2^n.
+ * complex64 states convert on the device. */
+int ev_state_upload(ev_state* s, const double* amps, uint64_t len);
+int ev_state_download(const ev_state* s, double* amps, uint64_t len);
+/* Wait until all work queued on the state's stream has finished. */
+int ev_state_synchronize(const ev_state* s);
+
+/* ---- gate kernels (src/kernel.rs:76, :192, :299) ------------------------ */
+
+/* Single-qubit gate on qubit k (kernel::apply_1q). */
+int ev_apply_1q(ev_state* s, uint64_t k, const double m[8]);
+/* Two-qubit gate on operands a (more significant) and b (kernel::apply_2q).
+ * CNOT, CZ and SWAP are recognised by exact matrix equality, as in
+ * src/kernel.rs:201-212. */
+int ev_apply_2q(ev_state* s, uint64_t a, uint64_t b, const double m[32]);
+/* Single-qubit gate on target, applied where every control is set
+ * (kernel::apply_controlled_1q). */
+int ev_apply_controlled_1q(ev_state* s, const uint64_t* controls,
+                           uint64_t ncontrols, uint64_t target,
+                           const double m[8]);
+
+/* ---- measurement (src/measure.rs:15-51) -------------------------------- */
+
+/* Measure qubit k with the caller's uniform u in [0,1): outcome = u < p1,
+ * then collapse and rescale by 1/sqrt(surviving). */
+int ev_measure_qubit(ev_state* s, uint64_t k, double u, int32_t* outcome);
+
+/* ---- observables (src/state.rs:94-185) --------------------------------- */
+
+int ev_norm_sqr(const ev_state* s, double* out);
+int ev_normalize(ev_state* s);
+int ev_probability(const ev_state* s, uint64_t basis, double* out);
+/* <other|self> as [re, im]. */
+int ev_overlap(const ev_state* self, const ev_state* other, double out[2]);
+int ev_fidelity(const ev_state* self, const ev_state* other, double* out);
+/* [<X>, <Y>, <Z>] of one qubit (State::bloch_vector). */
+int ev_bloch_vector(const ev_state* s, uint64_t qubit, double out[3]);
+
+/* ---- circuits (src/circuit.rs:245-306, src/backend/mod.rs:43-72) ------- */
+
+/* Circuit::validate: the first error in op order, with the reference's
+ * check order inside each op. */
+int ev_validate(const ev_circuit* c);
+/* StateVectorBackend::run_seeded: validate, start from |0...0>, seed the
+ * measurement Rng (xoshiro256++ via SplitMix64, src/rng.rs:18-58) and walk
+ * the ops.  On success *state_out is a new device-resident state owned by
+ * the caller and classical_out[0..num_classical) holds the register
+ * (0/1 bytes).  opts may be NULL (complex128, exact mode). */
+int ev_run_seeded(const ev_circuit* c, uint64_t seed, const ev_run_options* opts,
+                  ev_state** state_out, uint8_t* classical_out);
+
+/* The same run on an existing state of matching size and type: the state is
+ * reset to |0...0> first, so a caller can reuse one device buffer for many
+ * runs (the serving loop and the benchmark do). */
+int ev_state_run(ev_state* s, const ev_circuit* c, uint64_t seed,
+                 const ev_run_options* opts, uint8_t* classical_out);
+
+/* ---- shot sampling (no reference counterpart) ---------------------------
+ * Shot j measures qubits 0..n-1 in order, each exactly as measure_qubit
+ * would on the collapsed copy, with the uniforms of Rng::seed_from_u64(seed)
+ * taken n per shot, shots in order.  Bit q of out[j] is qubit q's outcome.
+ * The state is not modified.  n <= 63. */
+int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* out);
+
+/* ---- measurement hooks (no reference counterpart) ------------------------
+ * Used by benchmarks and profilers: events on the state's stream, the number
+ * of kernels the engine has launched for a state, per-kernel-class timing
+ * recorded with events around each launch while profiling is on, and pinned
+ * host buffers for end-to-end copies. */
+int ev_state_record_event(ev_state* s, int32_t slot); /* slot in [0, 16) */
+int ev_state_elapsed_ms(ev_state* s, int32_t from_slot, int32_t to_slot, float* ms);
+int ev_state_launch_count(const ev_state* s, uint64_t* out);
+
+typedef struct ev_kernel_stat {
+  char name[32];     /* kernel class, e.g. "tile_pass", "gate", "measure" */
+  uint64_t launches; /* timed launches                                    */
+  double ms;         /* summed event time                                 */
+  double bytes;      /* summed algorithmic HBM bytes                      */
+} ev_kernel_stat;
+int ev_state_profile(ev_state* s, int32_t enable); /* enabling clears stats */
+int ev_state_profile_read(ev_state* s, ev_kernel_stat* out, int32_t max, int32_t* count);
+
+int ev_host_alloc(uint64_t bytes, void** out); /* page-locked host memory */
+int ev_host_free(void* p);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EVERETT_CUDA_H */

@@ -1,0 +1,491 @@
+// ev_oracle.cpp -- CPU restatement of everett's dense statevector path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the parity oracle for the GB300
+// engine: it restates, in scalar C++, the arithmetic of the reference crate
+// (hz2/everett 0.1.2) that the engine must reproduce.  Only the test suite,
+// the smoke check and the CPU-baseline leg of the benchmark may load it; the
+// engine itself never calls it.
+//
+// Pinning.  The reference is Rust and no Rust toolchain exists where this is
+// built, so the oracle is pinned against the reference's own known-answer
+// tests (kernel.rs:515-770, measure.rs:59-106, state.rs:192-234,
+// tests/algorithms_*.rs, tests/properties.rs), re-expressed in
+// tests/test_oracle.py.  The xoshiro256++ stream has no golden values in the
+// reference (rng.rs:62-95 tests only determinism, range and mean): that part
+// of parity is unpinned.
+//
+// Build: -O2 -ffp-contract=off (no implicit FMA contraction), with std::fma
+// wherever the Rust source calls mul_add, so every rounding step matches the
+// reference's.  Loops that the reference runs sequentially stay sequential
+// unless noted; the OpenMP pragmas only split loops whose iterations are
+// independent (each amplitude pair / quad is written by exactly one
+// iteration), so the parallel build produces bit-identical results.
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "../include/everett_cuda.h"
+
+namespace {
+
+// ---- Complex64 (src/complex.rs:22-124) ------------------------------------
+struct C {
+  double re, im;
+};
+
+// (a + bi)(c + di): re = fma(a, c, -(b*d)), im = fma(a, d, b*c)
+// (complex.rs:115-124).
+inline C cmul(C a, C b) {
+  return C{std::fma(a.re, b.re, -(a.im * b.im)), std::fma(a.re, b.im, a.im * b.re)};
+}
+inline C cadd(C a, C b) { return C{a.re + b.re, a.im + b.im}; }
+inline C conj(C a) { return C{a.re, -a.im}; }
+// norm_sqr = re.mul_add(re, im*im) (complex.rs:80-82).
+inline double norm_sqr(C a) { return std::fma(a.re, a.re, a.im * a.im); }
+// Complex64 * f64 (complex.rs:127-133).
+inline C cscale(C a, double s) { return C{a.re * s, a.im * s}; }
+
+inline C ld(const double* m, int i) { return C{m[2 * i], m[2 * i + 1]}; }
+
+// ---- index math (src/kernel.rs:39-66) --------------------------------------
+inline void index_pair(uint64_t k, uint64_t i, uint64_t* i0, uint64_t* i1) {
+  const uint64_t low_mask = (uint64_t(1) << k) - 1;
+  *i0 = ((i >> k) << (k + 1)) | (i & low_mask);
+  *i1 = *i0 | (uint64_t(1) << k);
+}
+
+inline void index_quad(uint64_t a, uint64_t b, uint64_t i, uint64_t idx[4]) {
+  const uint64_t lo = a < b ? a : b, hi = a < b ? b : a;
+  const uint64_t low_mask = (uint64_t(1) << lo) - 1;
+  const uint64_t t = ((i >> lo) << (lo + 1)) | (i & low_mask);
+  const uint64_t mid_mask = (uint64_t(1) << hi) - 1;
+  const uint64_t base = ((t >> hi) << (hi + 1)) | (t & mid_mask);
+  const uint64_t bit_a = uint64_t(1) << a, bit_b = uint64_t(1) << b;
+  idx[0] = base;
+  idx[1] = base | bit_b;
+  idx[2] = base | bit_a;
+  idx[3] = base | bit_a | bit_b;
+}
+
+// ---- Gate2 constants used by the exact-match dispatch (gate.rs:189-232) ----
+bool is_perm2(const double* m, const int rows[4], double last_sign) {
+  // matrix with a single 1 per row at column rows[r] (times last_sign on row 3)
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      double want = (c == rows[r]) ? (r == 3 ? last_sign : 1.0) : 0.0;
+      if (!(m[2 * (4 * r + c)] == want && m[2 * (4 * r + c) + 1] == 0.0)) return false;
+    }
+  return true;
+}
+const int kCnotRows[4] = {0, 1, 3, 2};
+const int kIdRows[4] = {0, 1, 2, 3};
+const int kSwapRows[4] = {0, 2, 1, 3};
+
+// ---- Rng: xoshiro256++ seeded by SplitMix64 (src/rng.rs:18-58) -------------
+struct Rng {
+  uint64_t s[4];
+  explicit Rng(uint64_t seed) {
+    for (int w = 0; w < 4; ++w) {
+      seed += 0x9E3779B97F4A7C15ULL;
+      uint64_t z = seed;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+      s[w] = z ^ (z >> 31);
+    }
+  }
+  static uint64_t rotl(uint64_t x, int r) { return (x << r) | (x >> (64 - r)); }
+  uint64_t next_u64() {
+    const uint64_t result = rotl(s[0] + s[3], 23) + s[0];
+    const uint64_t t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl(s[3], 45);
+    return result;
+  }
+  // (u64 >> 11) * 2^-53 (rng.rs:52-56).
+  double next_f64() { return double(next_u64() >> 11) * (1.0 / double(uint64_t(1) << 53)); }
+};
+
+// ---- kernels ----------------------------------------------------------------
+
+// apply_1q_scalar (kernel.rs:100-119).  The reference's AVX2 branch is never
+// taken on the aarch64 host and is pinned equal to this one (kernel.rs:728).
+void apply_1q(C* amps, uint64_t len, uint64_t k, const double* mm) {
+  const C m0 = ld(mm, 0), m1 = ld(mm, 1), m2 = ld(mm, 2), m3 = ld(mm, 3);
+  const int64_t pairs = int64_t(len / 2);
+#pragma omp parallel for schedule(static) if (pairs >= (1 << 16))
+  for (int64_t i = 0; i < pairs; ++i) {
+    uint64_t i0, i1;
+    index_pair(k, uint64_t(i), &i0, &i1);
+    const C a0 = amps[i0], a1 = amps[i1];
+    amps[i0] = cadd(cmul(m0, a0), cmul(m1, a1));
+    amps[i1] = cadd(cmul(m2, a0), cmul(m3, a1));
+  }
+}
+
+// dense 4x4 quad loop (kernel.rs:214-243): rows in index_quad order, each row
+// summed left to right.
+void apply_2q_dense(C* amps, uint64_t len, uint64_t a, uint64_t b, const double* mm) {
+  const int64_t groups = int64_t(len / 4);
+#pragma omp parallel for schedule(static) if (groups >= (1 << 15))
+  for (int64_t i = 0; i < groups; ++i) {
+    uint64_t idx[4];
+    index_quad(a, b, uint64_t(i), idx);
+    const C amp[4] = {amps[idx[0]], amps[idx[1]], amps[idx[2]], amps[idx[3]]};
+    for (int row = 0; row < 4; ++row) {
+      C acc = cmul(ld(mm, row * 4 + 0), amp[0]);
+      acc = cadd(acc, cmul(ld(mm, row * 4 + 1), amp[1]));
+      acc = cadd(acc, cmul(ld(mm, row * 4 + 2), amp[2]));
+      acc = cadd(acc, cmul(ld(mm, row * 4 + 3), amp[3]));
+      amps[idx[row]] = acc;
+    }
+  }
+}
+
+// apply_2q with the exact-match dispatch (kernel.rs:192-289).
+void apply_2q(C* amps, uint64_t len, uint64_t a, uint64_t b, const double* mm) {
+  const int64_t groups = int64_t(len / 4);
+  if (is_perm2(mm, kCnotRows, 1.0)) {  // swap i10 <-> i11 (kernel.rs:248-260)
+#pragma omp parallel for schedule(static) if (groups >= (1 << 15))
+    for (int64_t i = 0; i < groups; ++i) {
+      uint64_t idx[4];
+      index_quad(a, b, uint64_t(i), idx);
+      const C tmp = amps[idx[2]];
+      amps[idx[2]] = amps[idx[3]];
+      amps[idx[3]] = tmp;
+    }
+    return;
+  }
+  if (is_perm2(mm, kIdRows, -1.0)) {  // CZ: negate i11 (kernel.rs:263-274)
+#pragma omp parallel for schedule(static) if (groups >= (1 << 15))
+    for (int64_t i = 0; i < groups; ++i) {
+      uint64_t idx[4];
+      index_quad(a, b, uint64_t(i), idx);
+      amps[idx[3]] = C{-amps[idx[3]].re, -amps[idx[3]].im};
+    }
+    return;
+  }
+  if (is_perm2(mm, kSwapRows, 1.0)) {  // swap i01 <-> i10 (kernel.rs:277-289)
+#pragma omp parallel for schedule(static) if (groups >= (1 << 15))
+    for (int64_t i = 0; i < groups; ++i) {
+      uint64_t idx[4];
+      index_quad(a, b, uint64_t(i), idx);
+      const C tmp = amps[idx[1]];
+      amps[idx[1]] = amps[idx[2]];
+      amps[idx[2]] = tmp;
+    }
+    return;
+  }
+  apply_2q_dense(amps, len, a, b, mm);
+}
+
+// apply_controlled_1q_scalar (kernel.rs:332-358): full sweep over pairs with
+// a mask test on i0.
+void apply_controlled(C* amps, uint64_t len, uint64_t mask, uint64_t target,
+                      const double* mm) {
+  const C m0 = ld(mm, 0), m1 = ld(mm, 1), m2 = ld(mm, 2), m3 = ld(mm, 3);
+  const int64_t pairs = int64_t(len / 2);
+#pragma omp parallel for schedule(static) if (pairs >= (1 << 16))
+  for (int64_t i = 0; i < pairs; ++i) {
+    uint64_t i0, i1;
+    index_pair(target, uint64_t(i), &i0, &i1);
+    if ((i0 & mask) == mask) {
+      const C a0 = amps[i0], a1 = amps[i1];
+      amps[i0] = cadd(cmul(m0, a0), cmul(m1, a1));
+      amps[i1] = cadd(cmul(m2, a0), cmul(m3, a1));
+    }
+  }
+}
+
+// measure_qubit (measure.rs:15-51): sequential p1 sum from 0.0, outcome =
+// u < p1, scale = 1/sqrt(surviving) or 0, zero the other half.
+int measure_qubit(C* amps, uint64_t len, uint64_t k, double u) {
+  const uint64_t bit = uint64_t(1) << k;
+  double p1 = 0.0;
+  for (uint64_t j = 0; j < len; ++j)
+    if (j & bit) p1 += norm_sqr(amps[j]);
+  const bool outcome = u < p1;
+  const double surviving = outcome ? p1 : 1.0 - p1;
+  const double scale = surviving > 0.0 ? 1.0 / std::sqrt(surviving) : 0.0;
+  const int64_t n = int64_t(len);
+#pragma omp parallel for schedule(static) if (n >= (1 << 16))
+  for (int64_t j = 0; j < n; ++j) {
+    const bool keep = ((uint64_t(j) & bit) != 0) == outcome;
+    amps[j] = keep ? cscale(amps[j], scale) : C{0.0, 0.0};
+  }
+  return outcome ? 1 : 0;
+}
+
+// State::norm_sqr: iterator sum, folded left to right from -0.0 (Rust's
+// neutral element for f64 Sum) (state.rs:94-96).
+double state_norm_sqr(const C* amps, uint64_t len) {
+  double acc = -0.0;
+  for (uint64_t j = 0; j < len; ++j) acc += norm_sqr(amps[j]);
+  return acc;
+}
+
+// ---- op walk (src/backend/mod.rs:43-72, src/circuit.rs:245-306) ------------
+
+int check_qubit(const ev_circuit* c, uint64_t q) {
+  return q < c->num_qubits ? EV_OK : EV_ERR_QUBIT_OUT_OF_RANGE;
+}
+int check_classical(const ev_circuit* c, uint64_t b) {
+  return b < c->num_classical ? EV_OK : EV_ERR_CLASSICAL_BIT_OUT_OF_RANGE;
+}
+
+// Validates the op starting at *pos (prefix-encoded IfClassic) and advances
+// *pos past it.  Mirrors Circuit::validate_op (circuit.rs:252-284).
+int validate_op(const ev_circuit* c, uint64_t* pos) {
+  if (*pos >= c->nops) return EV_ERR_INVALID_ARGUMENT;
+  const ev_op& op = c->ops[*pos];
+  *pos += 1;
+  int rc;
+  switch (op.kind) {
+    case EV_OP_APPLY1:
+      return check_qubit(c, op.q0);
+    case EV_OP_APPLY2:
+      if ((rc = check_qubit(c, op.q0))) return rc;
+      if ((rc = check_qubit(c, op.q1))) return rc;
+      return op.q0 == op.q1 ? EV_ERR_DUPLICATE_QUBIT : EV_OK;
+    case EV_OP_CONTROLLED:
+      if ((rc = check_qubit(c, op.q0))) return rc;
+      if (op.ctrl_off + op.nctrl > c->pool_len) return EV_ERR_INVALID_ARGUMENT;
+      for (uint32_t j = 0; j < op.nctrl; ++j) {
+        const uint64_t q = c->ctrl_pool[op.ctrl_off + j];
+        if ((rc = check_qubit(c, q))) return rc;
+        if (q == op.q0) return EV_ERR_DUPLICATE_QUBIT;
+      }
+      return EV_OK;
+    case EV_OP_MEASURE:
+      if ((rc = check_qubit(c, op.q0))) return rc;
+      return check_classical(c, op.q1);
+    case EV_OP_IF:
+      if ((rc = check_classical(c, op.q0))) return rc;
+      return validate_op(c, pos);
+    default:
+      return EV_ERR_INVALID_ARGUMENT;
+  }
+}
+
+// apply_op (backend/mod.rs:51-72).  Returns the index after the op.
+uint64_t run_op(const ev_circuit* c, uint64_t pos, C* amps, uint64_t len, Rng* rng,
+                uint8_t* classical, bool active) {
+  const ev_op& op = c->ops[pos];
+  if (op.kind == EV_OP_IF) {
+    const bool take = active && classical[op.q0] != 0;
+    return run_op(c, pos + 1, amps, len, rng, classical, take);
+  }
+  if (active) {
+    switch (op.kind) {
+      case EV_OP_APPLY1:
+        apply_1q(amps, len, op.q0, op.m);
+        break;
+      case EV_OP_APPLY2:
+        apply_2q(amps, len, op.q0, op.q1, op.m);
+        break;
+      case EV_OP_CONTROLLED: {
+        uint64_t mask = 0;
+        for (uint32_t j = 0; j < op.nctrl; ++j) mask |= uint64_t(1) << c->ctrl_pool[op.ctrl_off + j];
+        apply_controlled(amps, len, mask, op.q0, op.m);
+        break;
+      }
+      case EV_OP_MEASURE:
+        classical[op.q1] = uint8_t(measure_qubit(amps, len, op.q0, rng->next_f64()));
+        break;
+    }
+  }
+  return pos + 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+// ---- gate constructors (src/gate.rs:54-136) ---------------------------------
+// Matrices are built on the host with libm sin/cos, exactly as the reference
+// builds them; the engine receives matrices, never angles.
+static void put(double* m, int i, double re, double im) {
+  m[2 * i] = re;
+  m[2 * i + 1] = im;
+}
+void oracle_gate_h(double* m) {
+  const double s = 0.70710678118654752440;  // FRAC_1_SQRT_2
+  put(m, 0, s, 0); put(m, 1, s, 0); put(m, 2, s, 0); put(m, 3, -s, 0);
+}
+void oracle_gate_rx(double t, double* m) {  // gate.rs:106-110
+  const double s = std::sin(t / 2.0), co = std::cos(t / 2.0);
+  put(m, 0, co, 0); put(m, 1, 0, -s); put(m, 2, 0, -s); put(m, 3, co, 0);
+}
+void oracle_gate_ry(double t, double* m) {  // gate.rs:114-118
+  const double s = std::sin(t / 2.0), co = std::cos(t / 2.0);
+  put(m, 0, co, 0); put(m, 1, -s, 0); put(m, 2, s, 0); put(m, 3, co, 0);
+}
+void oracle_gate_rz(double t, double* m) {  // gate.rs:122-130: expi(-t/2), expi(t/2)
+  put(m, 0, std::cos(-t / 2.0), std::sin(-t / 2.0)); put(m, 1, 0, 0); put(m, 2, 0, 0);
+  put(m, 3, std::cos(t / 2.0), std::sin(t / 2.0));
+}
+void oracle_gate_phase(double l, double* m) {  // gate.rs:134-136
+  put(m, 0, 1, 0); put(m, 1, 0, 0); put(m, 2, 0, 0); put(m, 3, std::cos(l), std::sin(l));
+}
+
+// ---- kernels on a caller-owned interleaved buffer ----------------------------
+void oracle_apply_1q(double* amps, uint64_t len, uint64_t k, const double* m) {
+  apply_1q(reinterpret_cast<C*>(amps), len, k, m);
+}
+void oracle_apply_2q(double* amps, uint64_t len, uint64_t a, uint64_t b, const double* m) {
+  apply_2q(reinterpret_cast<C*>(amps), len, a, b, m);
+}
+void oracle_apply_2q_dense(double* amps, uint64_t len, uint64_t a, uint64_t b,
+                           const double* m) {
+  apply_2q_dense(reinterpret_cast<C*>(amps), len, a, b, m);
+}
+void oracle_apply_controlled_1q(double* amps, uint64_t len, const uint64_t* controls,
+                                uint64_t nctrl, uint64_t target, const double* m) {
+  uint64_t mask = 0;
+  for (uint64_t j = 0; j < nctrl; ++j) mask |= uint64_t(1) << controls[j];
+  apply_controlled(reinterpret_cast<C*>(amps), len, mask, target, m);
+}
+int oracle_measure_qubit(double* amps, uint64_t len, uint64_t k, double u) {
+  return measure_qubit(reinterpret_cast<C*>(amps), len, k, u);
+}
+
+// ---- State observables (src/state.rs:94-185) ---------------------------------
+double oracle_norm_sqr(const double* amps, uint64_t len) {
+  return state_norm_sqr(reinterpret_cast<const C*>(amps), len);
+}
+void oracle_normalize(double* amps, uint64_t len) {  // state.rs:103-111
+  C* a = reinterpret_cast<C*>(amps);
+  const double norm = std::sqrt(state_norm_sqr(a, len));
+  if (norm > 0.0) {
+    const double inv = 1.0 / norm;
+    for (uint64_t j = 0; j < len; ++j) a[j] = cscale(a[j], inv);
+  }
+}
+// <other|self> = sum conj(other_j) * self_j, accumulated from ZERO (state.rs:130-138).
+void oracle_overlap(const double* self, const double* other, uint64_t len, double* out) {
+  const C* a = reinterpret_cast<const C*>(self);
+  const C* b = reinterpret_cast<const C*>(other);
+  C acc{0.0, 0.0};
+  for (uint64_t j = 0; j < len; ++j) acc = cadd(acc, cmul(conj(b[j]), a[j]));
+  out[0] = acc.re;
+  out[1] = acc.im;
+}
+void oracle_bloch_vector(const double* amps, uint64_t len, uint64_t qubit, double* out) {
+  const C* a = reinterpret_cast<const C*>(amps);
+  const uint64_t bit = uint64_t(1) << qubit;
+  double r00 = 0.0, r11 = 0.0;
+  C r01{0.0, 0.0};
+  for (uint64_t j = 0; j < len; ++j) {
+    if ((j & bit) == 0) {
+      r00 += norm_sqr(a[j]);
+      r01 = cadd(r01, cmul(a[j], conj(a[j | bit])));
+    } else {
+      r11 += norm_sqr(a[j]);
+    }
+  }
+  out[0] = 2.0 * r01.re;
+  out[1] = 2.0 * r01.im;
+  out[2] = r00 - r11;
+}
+
+// ---- Rng -------------------------------------------------------------------
+void oracle_rng_u64(uint64_t seed, uint64_t count, uint64_t* out) {
+  Rng r(seed);
+  for (uint64_t j = 0; j < count; ++j) out[j] = r.next_u64();
+}
+void oracle_rng_f64(uint64_t seed, uint64_t count, double* out) {
+  Rng r(seed);
+  for (uint64_t j = 0; j < count; ++j) out[j] = r.next_f64();
+}
+
+// ---- circuits ----------------------------------------------------------------
+int oracle_validate(const ev_circuit* c) {
+  uint64_t pos = 0;
+  while (pos < c->nops) {
+    const int rc = validate_op(c, &pos);
+    if (rc) return rc;
+  }
+  return EV_OK;
+}
+
+// StateVectorBackend::run_seeded (statevector.rs:77-90): validate, |0..0>,
+// Rng::seed_from_u64(seed), drive.  amps_out holds 2^n complex.
+int oracle_run_seeded(const ev_circuit* c, uint64_t seed, double* amps_out,
+                      uint8_t* classical_out) {
+  const int rc = oracle_validate(c);
+  if (rc) return rc;
+  const uint64_t len = uint64_t(1) << c->num_qubits;
+  C* amps = reinterpret_cast<C*>(amps_out);
+  for (uint64_t j = 0; j < len; ++j) amps[j] = C{0.0, 0.0};
+  amps[0] = C{1.0, 0.0};
+  Rng rng(seed);
+  for (uint64_t j = 0; j < c->num_classical; ++j) classical_out[j] = 0;
+  uint64_t pos = 0;
+  while (pos < c->nops) pos = run_op(c, pos, amps, len, &rng, classical_out, true);
+  return EV_OK;
+}
+
+// Runs ops [first, last) of a circuit on an existing buffer with no
+// measurement (used to time a bounded sample of a circuit).
+void oracle_apply_ops(const ev_circuit* c, uint64_t first, uint64_t last, double* amps_io) {
+  const uint64_t len = uint64_t(1) << c->num_qubits;
+  Rng rng(0);
+  std::vector<uint8_t> classical(c->num_classical + 1, 0);
+  uint64_t pos = first;
+  while (pos < last) pos = run_op(c, pos, reinterpret_cast<C*>(amps_io), len, &rng, classical.data(), true);
+}
+
+// ---- shot sampling -----------------------------------------------------------
+// Literal form of the shot contract: for each shot, copy the state and call
+// measure_qubit for qubits 0..n-1 with consecutive uniforms of one Rng.
+// O(shots * n * 2^n); for small registers only.
+void oracle_sample_literal(const double* amps, uint64_t n, uint64_t seed, uint64_t shots,
+                           uint64_t* out) {
+  const uint64_t len = uint64_t(1) << n;
+  std::vector<C> work(len);
+  Rng rng(seed);
+  for (uint64_t s = 0; s < shots; ++s) {
+    std::memcpy(work.data(), amps, len * sizeof(C));
+    uint64_t bits = 0;
+    for (uint64_t q = 0; q < n; ++q)
+      if (measure_qubit(work.data(), len, q, rng.next_f64())) bits |= uint64_t(1) << q;
+    out[s] = bits;
+  }
+}
+
+// Conditional-mass form of the same contract.  mass[q][r] is the total
+// probability of basis states whose low q bits equal r, built by pairwise
+// sums: mass[n][j] = |a_j|^2 and mass[q][r] = mass[q+1][r] + mass[q+1][r+2^q].
+// Qubit q of a shot whose earlier outcomes are r is 1 iff
+// u < mass[q+1][r + 2^q] / mass[q][r]; a zero mass gives NaN and outcome 0,
+// as measure_qubit's zero scale does.  Mathematically equal to the literal
+// form; outcomes differ only where u lies within rounding of the boundary.
+void oracle_sample_tree(const double* amps, uint64_t n, uint64_t seed, uint64_t shots,
+                        uint64_t* out) {
+  const uint64_t len = uint64_t(1) << n;
+  const C* a = reinterpret_cast<const C*>(amps);
+  std::vector<std::vector<double>> mass(n + 1);
+  mass[n].resize(len);
+  for (uint64_t j = 0; j < len; ++j) mass[n][j] = norm_sqr(a[j]);
+  for (int64_t q = int64_t(n) - 1; q >= 0; --q) {
+    const uint64_t w = uint64_t(1) << q;
+    mass[q].resize(w);
+    for (uint64_t r = 0; r < w; ++r) mass[q][r] = mass[q + 1][r] + mass[q + 1][r + w];
+  }
+  Rng rng(seed);
+  for (uint64_t s = 0; s < shots; ++s) {
+    uint64_t r = 0;
+    for (uint64_t q = 0; q < n; ++q) {
+      const double u = rng.next_f64();
+      const double p1 = mass[q + 1][r + (uint64_t(1) << q)] / mass[q][r];
+      if (u < p1) r |= uint64_t(1) << q;
+    }
+    out[s] = r;
+  }
+}
+
+}  // extern "C"
