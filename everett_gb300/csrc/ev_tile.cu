@@ -33,7 +33,7 @@ enum TileKind : uint8_t {
   T_DENSE2
 };
 
-struct TileOp {
+struct __align__(16) TileOp {
   uint8_t kind;
   uint8_t k1;      // Kind1 for T_1Q
   uint8_t p0, p1;  // local positions: target / (a, b)
@@ -43,9 +43,13 @@ struct TileOp {
   uint32_t lmask;  // local control mask
   uint32_t pad2;
   uint64_t emask;  // controls outside the tile (global bit mask)
-  uint8_t ins[24]; // T_1Q: sorted local positions of (local controls + target)
+  uint64_t ins;    // T_1Q: sorted local positions of (local controls + target),
+                   // 4 bits each, lowest position in the low nibble
+  uint64_t pad3[2];
   double m[32];
 };
+
+static_assert(sizeof(TileOp) % 16 == 0, "op records are staged with 16-byte copies");
 
 struct TilePlan {
   int k, L;
@@ -60,42 +64,80 @@ __device__ __forceinline__ V ldm(const double* m, int i) {
   return mkv<V>(m[2 * i], m[2 * i + 1]);
 }
 
-template <typename V>
-__device__ __forceinline__ void tile_pair(V* t, uint32_t i0, uint32_t i1, int k1, const double* m) {
-  switch (k1) {
-    case K1_DENSE: {
+__device__ __forceinline__ uint32_t ins0(uint32_t i, int p) {
+  return ((i >> p) << (p + 1)) | (i & ((1u << p) - 1));
+}
+
+// One (possibly controlled) 1-qubit record over the tile: the pair loop is
+// specialised per matrix kind, with the matrix held in registers.
+template <int K1, typename V>
+__device__ __forceinline__ void tile_1q(V* t, uint32_t count, const TileOp& op) {
+  const V m0 = ldm<V>(op.m, 0), m1 = ldm<V>(op.m, 1), m2 = ldm<V>(op.m, 2), m3 = ldm<V>(op.m, 3);
+  using R = typename Real<V>::T;
+  const uint32_t tbit = 1u << op.p0, lmask = op.lmask;
+  const int nins = op.nins;
+  const uint64_t ins = op.ins;
+  const int ins_first = int(ins & 15);
+  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
+    uint32_t j = ins0(i, ins_first);
+    for (int q = 1; q < nins; ++q) j = ins0(j, int((ins >> (4 * q)) & 15));
+    const uint32_t i0 = j | lmask, i1 = i0 | tbit;
+    if constexpr (K1 == K1_DENSE) {
       const V a0 = t[i0], a1 = t[i1];
-      t[i0] = cadd(cmul(ldm<V>(m, 0), a0), cmul(ldm<V>(m, 1), a1));
-      t[i1] = cadd(cmul(ldm<V>(m, 2), a0), cmul(ldm<V>(m, 3), a1));
-      break;
-    }
-    case K1_REAL: {
-      using R = typename Real<V>::T;
+      t[i0] = cadd(cmul(m0, a0), cmul(m1, a1));
+      t[i1] = cadd(cmul(m2, a0), cmul(m3, a1));
+    } else if constexpr (K1 == K1_REAL) {
       const V a0 = t[i0], a1 = t[i1];
-      t[i0] = cadd(rmul(R(m[0]), a0), rmul(R(m[2]), a1));
-      t[i1] = cadd(rmul(R(m[4]), a0), rmul(R(m[6]), a1));
-      break;
-    }
-    case K1_DIAG:
-      t[i0] = cmul(ldm<V>(m, 0), t[i0]);
-      t[i1] = cmul(ldm<V>(m, 3), t[i1]);
-      break;
-    case K1_PHASE:
-      t[i1] = cmul(ldm<V>(m, 3), t[i1]);
-      break;
-    case K1_ANTI: {
+      t[i0] = cadd(rmul(R(m0.x), a0), rmul(R(m1.x), a1));
+      t[i1] = cadd(rmul(R(m2.x), a0), rmul(R(m3.x), a1));
+    } else if constexpr (K1 == K1_DIAG) {
+      t[i0] = cmul(m0, t[i0]);
+      t[i1] = cmul(m3, t[i1]);
+    } else if constexpr (K1 == K1_PHASE) {
+      t[i1] = cmul(m3, t[i1]);
+    } else if constexpr (K1 == K1_ANTI) {
       const V a0 = t[i0], a1 = t[i1];
-      t[i0] = cmul(ldm<V>(m, 1), a1);
-      t[i1] = cmul(ldm<V>(m, 2), a0);
-      break;
+      t[i0] = cmul(m1, a1);
+      t[i1] = cmul(m2, a0);
     }
-    default:
-      break;
   }
 }
 
-__device__ __forceinline__ uint32_t ins0(uint32_t i, int p) {
-  return ((i >> p) << (p + 1)) | (i & ((1u << p) - 1));
+template <int KIND, typename V>
+__device__ __forceinline__ void tile_2q(V* t, uint32_t count, const TileOp& op) {
+  const uint32_t ba = 1u << op.p0, bb = 1u << op.p1;
+  const int lo = op.lo, hi = op.hi;
+  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
+    const uint32_t base = ins0(ins0(i, lo), hi);
+    const uint32_t i1 = base | bb, i2 = base | ba, i3 = base | ba | bb;
+    if constexpr (KIND == T_CNOT) {
+      const V x = t[i2];
+      t[i2] = t[i3];
+      t[i3] = x;
+    } else if constexpr (KIND == T_CZ) {
+      t[i3] = cneg(t[i3]);
+    } else if constexpr (KIND == T_SWAP) {
+      const V x = t[i1];
+      t[i1] = t[i2];
+      t[i2] = x;
+    } else if constexpr (KIND == T_DIAG2) {
+      t[base] = cmul(ldm<V>(op.m, 0), t[base]);
+      t[i1] = cmul(ldm<V>(op.m, 5), t[i1]);
+      t[i2] = cmul(ldm<V>(op.m, 10), t[i2]);
+      t[i3] = cmul(ldm<V>(op.m, 15), t[i3]);
+    } else {  // dense 4x4, rows summed left to right
+      const V a[4] = {t[base], t[i1], t[i2], t[i3]};
+      const uint32_t out[4] = {base, i1, i2, i3};
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        V acc = cmul(ldm<V>(op.m, 4 * r + 0), a[0]);
+        acc = cadd(acc, cmul(ldm<V>(op.m, 4 * r + 1), a[1]));
+        acc = cadd(acc, cmul(ldm<V>(op.m, 4 * r + 2), a[2]));
+        acc = cadd(acc, cmul(ldm<V>(op.m, 4 * r + 3), a[3]));
+        t[out[r]] = acc;
+      }
+    }
+  }
 }
 
 template <typename V>
@@ -103,82 +145,68 @@ __device__ void apply_tile_op(V* t, int k, const TileOp& op) {
   const uint32_t size = 1u << k;
   if (op.kind == T_1Q) {
     const uint32_t count = size >> op.nins;
-    const uint32_t tbit = 1u << op.p0;
-    for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
-      uint32_t j = i;
-      for (int q = 0; q < op.nins; ++q) j = ins0(j, op.ins[q]);
-      const uint32_t i0 = j | op.lmask;
-      tile_pair(t, i0, i0 | tbit, op.k1, op.m);
+    switch (op.k1) {
+      case K1_DENSE: tile_1q<K1_DENSE>(t, count, op); break;
+      case K1_REAL: tile_1q<K1_REAL>(t, count, op); break;
+      case K1_DIAG: tile_1q<K1_DIAG>(t, count, op); break;
+      case K1_PHASE: tile_1q<K1_PHASE>(t, count, op); break;
+      case K1_ANTI: tile_1q<K1_ANTI>(t, count, op); break;
+      default: break;
     }
     return;
   }
   const uint32_t count = size >> 2;
-  const uint32_t ba = 1u << op.p0, bb = 1u << op.p1;
-  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
-    const uint32_t base = ins0(ins0(i, op.lo), op.hi);
-    const uint32_t i1 = base | bb, i2 = base | ba, i3 = base | ba | bb;
-    switch (op.kind) {
-      case T_CNOT: {
-        const V x = t[i2];
-        t[i2] = t[i3];
-        t[i3] = x;
-        break;
-      }
-      case T_CZ:
-        t[i3] = cneg(t[i3]);
-        break;
-      case T_SWAP: {
-        const V x = t[i1];
-        t[i1] = t[i2];
-        t[i2] = x;
-        break;
-      }
-      case T_DIAG2:
-        t[base] = cmul(ldm<V>(op.m, 0), t[base]);
-        t[i1] = cmul(ldm<V>(op.m, 5), t[i1]);
-        t[i2] = cmul(ldm<V>(op.m, 10), t[i2]);
-        t[i3] = cmul(ldm<V>(op.m, 15), t[i3]);
-        break;
-      default: {  // dense 4x4, rows summed left to right
-        const V a[4] = {t[base], t[i1], t[i2], t[i3]};
-        const uint32_t out[4] = {base, i1, i2, i3};
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          V acc = cmul(ldm<V>(op.m, 4 * r + 0), a[0]);
-          acc = cadd(acc, cmul(ldm<V>(op.m, 4 * r + 1), a[1]));
-          acc = cadd(acc, cmul(ldm<V>(op.m, 4 * r + 2), a[2]));
-          acc = cadd(acc, cmul(ldm<V>(op.m, 4 * r + 3), a[3]));
-          t[out[r]] = acc;
-        }
-      }
-    }
+  switch (op.kind) {
+    case T_CNOT: tile_2q<T_CNOT>(t, count, op); break;
+    case T_CZ: tile_2q<T_CZ>(t, count, op); break;
+    case T_SWAP: tile_2q<T_SWAP>(t, count, op); break;
+    case T_DIAG2: tile_2q<T_DIAG2>(t, count, op); break;
+    default: tile_2q<T_DENSE2>(t, count, op); break;
   }
 }
 
-// One persistent block per resident slot; tiles strided over the grid.
+constexpr int kTileThreads = 512;
+constexpr int kMaxPassOps = 48;  // op records per pass (staged in shared memory)
+
+// One persistent block per resident slot; tiles strided over the grid.  The
+// pass's op records and index tables are staged in shared memory once per
+// block: [tile 2^k amplitudes][row offsets 2^(k-L)][op records][comp qubits].
 template <typename V>
-__global__ void __launch_bounds__(512)
-    k_tile(V* __restrict__ s, uint64_t ntiles, TilePlan plan, const TileOp* __restrict__ ops,
-           int nops, const uint8_t* pred) {
+__global__ void __launch_bounds__(kTileThreads, 2)
+    k_tile(V* __restrict__ s, uint64_t ntiles, const TilePlan* __restrict__ gplan,
+           const TileOp* __restrict__ gops, int nops, const uint8_t* pred) {
   if (pred != nullptr && *pred == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  V* tile = reinterpret_cast<V*>(smem_raw);
-  const int k = plan.k, L = plan.L;
+  const int k = gplan->k, L = gplan->L, nH = gplan->nH, ncomp = gplan->ncomp;
   const uint32_t size = 1u << k;
   const uint32_t nrows = 1u << (k - L);
+  V* tile = reinterpret_cast<V*>(smem_raw);
   uint64_t* offs = reinterpret_cast<uint64_t*>(smem_raw + sizeof(V) * size);
+  // op records start on a 16-byte boundary (they are staged with 16-byte
+  // stores); tile + offsets is not a multiple of 16 bytes for tiny tiles
+  const size_t ops_at = (sizeof(V) * size + sizeof(uint64_t) * nrows + 15) & ~size_t(15);
+  TileOp* ops = reinterpret_cast<TileOp*>(smem_raw + ops_at);
+  uint8_t* comp = reinterpret_cast<uint8_t*>(ops + nops);
+  {
+    const uint4* src = reinterpret_cast<const uint4*>(gops);
+    uint4* dst = reinterpret_cast<uint4*>(ops);
+    const int words = nops * int(sizeof(TileOp) / sizeof(uint4));
+    for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+    if (threadIdx.x < 64) comp[threadIdx.x] = gplan->comp[threadIdx.x];
+  }
   for (uint32_t h = threadIdx.x; h < nrows; h += blockDim.x) {
     uint64_t o = 0;
-    for (int b = 0; b < plan.nH; ++b)
-      if ((h >> b) & 1) o |= uint64_t(1) << plan.H[b];
+    for (int b = 0; b < nH; ++b)
+      if ((h >> b) & 1) o |= uint64_t(1) << gplan->H[b];
     offs[h] = o;
   }
   const uint32_t lowmask = (1u << L) - 1;
   __syncthreads();
   for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     uint64_t base = 0;
-    for (int b = 0; b < plan.ncomp; ++b)
-      if ((t >> b) & 1) base |= uint64_t(1) << plan.comp[b];
+    for (int b = 0; b < ncomp; ++b)
+      if ((t >> b) & 1) base |= uint64_t(1) << comp[b];
+#pragma unroll 4
     for (uint32_t l = threadIdx.x; l < size; l += blockDim.x)
       tile[l] = s[base | offs[l >> L] | (l & lowmask)];
     __syncthreads();
@@ -188,6 +216,7 @@ __global__ void __launch_bounds__(512)
       apply_tile_op(tile, k, op);
       __syncthreads();
     }
+#pragma unroll 4
     for (uint32_t l = threadIdx.x; l < size; l += blockDim.x)
       s[base | offs[l >> L] | (l & lowmask)] = tile[l];
     __syncthreads();
@@ -225,7 +254,7 @@ static std::vector<Pass> plan_passes(const ev_circuit* c, uint64_t first, uint64
   while (pos < last) {
     uint64_t set = low;
     uint64_t end = pos;
-    while (end < last) {
+    while (end < last && end - pos < uint64_t(kMaxPassOps)) {
       const uint64_t want = set | data_qubits(c->ops[end]);
       if (popc(want) > k) break;
       set = want;
@@ -273,25 +302,29 @@ static void encode_op(const ev_circuit* c, const ev_op& op, uint64_t tset, const
   out->emask = emask;
   const uint32_t all = lmask | (1u << out->p0);
   int ni = 0;
-  for (int p = 0; p < 32; ++p)
-    if ((all >> p) & 1) out->ins[ni++] = uint8_t(p);
+  uint64_t packed = 0;
+  for (int p = 0; p < 16; ++p)
+    if ((all >> p) & 1) packed |= uint64_t(p) << (4 * ni++);
+  out->ins = packed;
   out->nins = uint8_t(ni);
 }
 
 template <typename V>
-static int launch_tile(ev_state* s, uint64_t ntiles, const TilePlan& plan, const TileOp* dops,
-                       int nops, const uint8_t* pred) {
-  const size_t smem = sizeof(V) * (size_t(1) << plan.k) + sizeof(uint64_t) * (size_t(1) << (plan.k - plan.L));
+static int launch_tile(ev_state* s, uint64_t ntiles, const TilePlan& plan, const TilePlan* dplan,
+                       const TileOp* dops, int nops, const uint8_t* pred) {
+  const size_t ops_at = (sizeof(V) * (size_t(1) << plan.k) +
+                         sizeof(uint64_t) * (size_t(1) << (plan.k - plan.L)) + 15) & ~size_t(15);
+  const size_t smem = ops_at + sizeof(TileOp) * size_t(nops) + 64;
   EV_CUDA(cudaFuncSetAttribute(k_tile<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
   int per_sm = 0;
-  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<V>, 512, smem));
+  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<V>, kTileThreads, smem));
   if (per_sm < 1) per_sm = 1;
   uint64_t grid = uint64_t(s->num_sms) * per_sm;
   if (grid > ntiles) grid = ntiles;
   ProfScope prof(s, P_TILE, 2.0 * double(s->len()) * double(sizeof(V)));
   s->launches += 1;
-  k_tile<V><<<unsigned(grid), 512, smem, s->stream>>>(static_cast<V*>(s->amps), ntiles, plan, dops,
-                                                      nops, pred);
+  k_tile<V><<<unsigned(grid), kTileThreads, smem, s->stream>>>(static_cast<V*>(s->amps), ntiles,
+                                                               dplan, dops, nops, pred);
   EV_CUDA(cudaGetLastError());
   return EV_OK;
 }
@@ -333,18 +366,28 @@ int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, i
     plans.push_back(plan);
     w += p.last - p.first;
   }
-  TileOp* dops = nullptr;
-  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dops), std::max<size_t>(1, ops.size()) * sizeof(TileOp), s->stream));
-  EV_CUDA(cudaMemcpyAsync(dops, ops.data(), ops.size() * sizeof(TileOp), cudaMemcpyHostToDevice, s->stream));
+  // one device buffer: plans, then op records
+  const size_t plan_bytes = (passes.size() * sizeof(TilePlan) + 255) / 256 * 256;
+  const size_t total = plan_bytes + std::max<size_t>(1, ops.size()) * sizeof(TileOp);
+  std::vector<unsigned char> host(total, 0);
+  std::memcpy(host.data(), plans.data(), passes.size() * sizeof(TilePlan));
+  std::memcpy(host.data() + plan_bytes, ops.data(), ops.size() * sizeof(TileOp));
+  unsigned char* dbuf = nullptr;
+  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dbuf), total, s->stream));
+  EV_CUDA(cudaMemcpyAsync(dbuf, host.data(), total, cudaMemcpyHostToDevice, s->stream));
+  const TilePlan* dplans = reinterpret_cast<const TilePlan*>(dbuf);
+  const TileOp* dops = reinterpret_cast<const TileOp*>(dbuf + plan_bytes);
   int rc = EV_OK;
   const uint64_t ntiles = uint64_t(1) << (n - k);
   for (size_t i = 0; i < passes.size() && rc == EV_OK; ++i) {
     if (s->dtype == EV_C128)
-      rc = launch_tile<double2>(s, ntiles, plans[i], dops + ranges[i].first, ranges[i].second, pred);
+      rc = launch_tile<double2>(s, ntiles, plans[i], dplans + i, dops + ranges[i].first,
+                                ranges[i].second, pred);
     else
-      rc = launch_tile<float2>(s, ntiles, plans[i], dops + ranges[i].first, ranges[i].second, pred);
+      rc = launch_tile<float2>(s, ntiles, plans[i], dplans + i, dops + ranges[i].first,
+                               ranges[i].second, pred);
   }
-  cudaFreeAsync(dops, s->stream);
+  cudaFreeAsync(dbuf, s->stream);
   if (passes_out) *passes_out = passes.size();
   return rc;
 }
