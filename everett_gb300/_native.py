@@ -71,6 +71,7 @@ _SIGS = {
     "ev_apply_2q": [_P, _U64, _U64, _P],
     "ev_apply_controlled_1q": [_P, _P, _U64, _U64, _P],
     "ev_measure_qubit": [_P, _U64, C.c_double, C.POINTER(_I32)],
+    "ev_measure_qubit_noalloc": [_P, _U64, _U64, C.c_double, _P, C.POINTER(_I32)],
     "ev_norm_sqr": [_P, _DP],
     "ev_normalize": [_P],
     "ev_probability": [_P, _U64, _DP],

@@ -17,6 +17,7 @@
 // terms.  Every reduction accumulates in f64 for both storage types.
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "ev_device.cuh"
 #include "ev_internal.h"
@@ -487,4 +488,88 @@ extern "C" int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* o
   cudaFree(du);
   cudaFree(dout);
   return rc;
+}
+
+// ---- measurement without allocation ----------------------------------------
+//
+// ev_measure_qubit_noalloc measures a complex128 statevector that lives in a
+// device buffer the caller owns, and allocates nothing: its reduction
+// partials and measurement words live in one file-scope __device__ array.
+// It is for callers that cannot call cudaMalloc: a serving process that hands
+// all of HBM to its own allocator up front, or a host framework (a Rust or
+// C++ runtime with its own device pool) that must not see a foreign
+// allocation or the device-wide synchronisation cudaMalloc/cudaFree imply.
+//
+// The array is 1024 reduction blocks x 4 partials plus 12 words
+// (4108 doubles, ~32 KiB); every GPU that loads the library holds it until
+// the process exits.  Host code must not pass the array's name to a kernel
+// (on the host it is only a stand-in, not a device address), so on the first
+// call on each device, with that device current, the entry point resolves the
+// address with cudaGetSymbolAddress and caches it; make that first call
+// before any stream capture.  All calls share the array and each overwrites
+// what the previous one left, so calls that overlap on the GPU (different
+// streams, no ordering between them) race; calls on one stream, or otherwise
+// ordered, are safe.
+namespace {
+constexpr int kNoAllocBlocks = 1024;
+constexpr uint64_t kNoAllocMaxQubits = 40;
+__device__ __align__(256) double g_noalloc_scratch[kNoAllocBlocks * 4 + 12];
+std::mutex g_noalloc_mu;
+double* g_noalloc_addr[256] = {};
+
+int noalloc_scratch(int device, double** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (device < 0 || device >= 256) return fail(EV_ERR_INVALID_ARGUMENT, "device %d out of range", device);
+  if (!g_noalloc_addr[device]) {
+    void* p = nullptr;
+    EV_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_addr[device] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_addr[device];
+  return EV_OK;
+}
+}  // namespace
+
+extern "C" int ev_measure_qubit_noalloc(double* amps, uint64_t n, uint64_t k, double u,
+                                        void* stream, int32_t* outcome) {
+  clear_error();
+  if (!amps || !outcome) return fail(EV_ERR_INVALID_ARGUMENT, "ev_measure_qubit_noalloc: null argument");
+  if (n > kNoAllocMaxQubits)
+    return fail(EV_ERR_INVALID_ARGUMENT,
+                "ev_measure_qubit_noalloc: %llu qubits exceeds the maximum of %llu",
+                (unsigned long long)n, (unsigned long long)kNoAllocMaxQubits);
+  if (k >= n)
+    return fail(EV_ERR_QUBIT_OUT_OF_RANGE, "qubit q%llu out of range for %llu-qubit register",
+                (unsigned long long)k, (unsigned long long)n);
+  int device = 0, sms = 0;
+  EV_CUDA(cudaGetDevice(&device));
+  EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  double* scratch = nullptr;
+  EV_TRY(noalloc_scratch(device, &scratch));
+  double* partials = scratch;
+  double* result = scratch + kNoAllocBlocks * 4;
+  double* meas = result + 8;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  double2* a = reinterpret_cast<double2*>(amps);
+  // same grid as the state-owned path, so the sums (and results) agree
+  const uint64_t count = (uint64_t(1) << n) / 2;
+  const uint64_t want = (count + 4095) / 4096;
+  int nb = int(want < 1 ? 1 : want);
+  int cap = sms * 4 < kMaxRedBlocks ? sms * 4 : kMaxRedBlocks;
+  if (cap > kNoAllocBlocks) cap = kNoAllocBlocks;
+  if (nb > cap) nb = cap;
+  const uint64_t chunk = (count + nb - 1) / nb;
+  k_reduce<R_P1, double2><<<nb, kRedThreads, 0, st>>>(a, nullptr, count, chunk, int(k), partials,
+                                                      nullptr);
+  k_finish<<<1, kRedThreads, 0, st>>>(partials, nb, result, nullptr);
+  k_decide<<<1, 1, 0, st>>>(result, u, nullptr, nullptr, meas, nullptr, nullptr);
+  const uint64_t gw = (count + 255) / 256, gcap = uint64_t(sms) * 8;
+  k_collapse<double2><<<unsigned(gw < 1 ? 1 : (gw < gcap ? gw : gcap)), 256, 0, st>>>(
+      a, count, int(k), meas, nullptr);
+  EV_CUDA(cudaGetLastError());
+  double words[4];
+  EV_CUDA(cudaMemcpyAsync(words, meas, sizeof(words), cudaMemcpyDeviceToHost, st));
+  EV_CUDA(cudaStreamSynchronize(st));
+  *outcome = words[2] != 0.0 ? 1 : 0;
+  return EV_OK;
 }

@@ -147,6 +147,21 @@ int ev_apply_controlled_1q(ev_state* s, const uint64_t* controls,
  * then collapse and rescale by 1/sqrt(surviving). */
 int ev_measure_qubit(ev_state* s, uint64_t k, double u, int32_t* outcome);
 
+/* No counterpart in the reference.  The same measurement on a complex128
+ * statevector in a device buffer the caller owns (2^n interleaved re,im
+ * doubles), for callers that cannot call cudaMalloc: one whose device memory
+ * is all handed out by its own allocator, or one that cannot accept the
+ * device-wide synchronisation of an allocation.  It allocates nothing: its
+ * scratch is a fixed ~32 KiB array in the library's device memory, held on
+ * every GPU that loads the library until the process exits.  n <= 40
+ * (EV_ERR_INVALID_ARGUMENT beyond).  stream may be NULL (legacy default
+ * stream); the call returns after the measurement has completed.  The first
+ * call on a device resolves the array's device address, so make it before
+ * any stream capture.  Calls share the array: calls that overlap on the GPU
+ * race, ordered calls do not. */
+int ev_measure_qubit_noalloc(double* amps, uint64_t n, uint64_t k, double u,
+                             void* stream, int32_t* outcome);
+
 /* ---- observables (src/state.rs:94-185) --------------------------------- */
 
 int ev_norm_sqr(const ev_state* s, double* out);
