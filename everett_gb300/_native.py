@@ -24,7 +24,8 @@ assert OP_DTYPE.itemsize == 288
 
 OP_APPLY1, OP_APPLY2, OP_CONTROLLED, OP_MEASURE, OP_IF = 1, 2, 3, 4, 5
 C128, C64 = 0, 1
-MODE_EXACT, MODE_TILED = 0, 1
+MODE_EXACT, MODE_TILED, MODE_FUSED = 0, 1, 2
+FUSED_TF32X3, FUSED_BF16X3, FUSED_FP32 = 0, 1, 2
 
 OK = 0
 ERR_QUBIT_OUT_OF_RANGE = 1
@@ -46,7 +47,7 @@ class EvCircuit(C.Structure):
 
 class EvRunOptions(C.Structure):
     _fields_ = [("dtype", C.c_int32), ("mode", C.c_int32), ("tile_bits", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("variant", C.c_int32)]
 
 
 _P = C.c_void_p

@@ -20,8 +20,11 @@ from .rng import Rng
 
 _DTYPES = {"complex128": N.C128, "c128": N.C128, "complex64": N.C64, "c64": N.C64,
            N.C128: N.C128, N.C64: N.C64}
-_MODES = {"exact": N.MODE_EXACT, "tiled": N.MODE_TILED, N.MODE_EXACT: N.MODE_EXACT,
-          N.MODE_TILED: N.MODE_TILED}
+_MODES = {"exact": N.MODE_EXACT, "tiled": N.MODE_TILED, "fused": N.MODE_FUSED,
+          N.MODE_EXACT: N.MODE_EXACT, N.MODE_TILED: N.MODE_TILED, N.MODE_FUSED: N.MODE_FUSED}
+_VARIANTS = {"tf32x3": N.FUSED_TF32X3, "bf16x3": N.FUSED_BF16X3, "fp32": N.FUSED_FP32,
+             N.FUSED_TF32X3: N.FUSED_TF32X3, N.FUSED_BF16X3: N.FUSED_BF16X3,
+             N.FUSED_FP32: N.FUSED_FP32}
 
 
 class State:
@@ -165,11 +168,12 @@ class Execution:
         return self._state
 
 
-def _options(dtype, mode, tile_bits) -> N.EvRunOptions:
+def _options(dtype, mode, tile_bits, variant="tf32x3") -> N.EvRunOptions:
     o = N.EvRunOptions()
     o.dtype = _DTYPES[dtype]
     o.mode = _MODES[mode]
     o.tile_bits = int(tile_bits)
+    o.variant = _VARIANTS[variant]
     return o
 
 
@@ -186,14 +190,19 @@ class CudaStateVectorBackend:
         self._rng = Rng.seed_from_u64(seed)
 
     @classmethod
-    def run(cls, circuit: Circuit, dtype="complex128", mode="exact", tile_bits=0) -> Execution:
-        return cls.run_seeded(circuit, 0, dtype=dtype, mode=mode, tile_bits=tile_bits)
+    def run(cls, circuit: Circuit, dtype="complex128", mode="exact", tile_bits=0,
+            variant="tf32x3") -> Execution:
+        """mode: "exact" (one kernel per op), "tiled" (runs of ops per
+        shared-memory pass) or "fused" (complex64: dense k-qubit unitaries,
+        k = tile_bits, arithmetic = variant "tf32x3" | "bf16x3" | "fp32")."""
+        return cls.run_seeded(circuit, 0, dtype=dtype, mode=mode, tile_bits=tile_bits,
+                              variant=variant)
 
     @classmethod
     def run_seeded(cls, circuit: Circuit, seed: int, dtype="complex128", mode="exact",
-                   tile_bits=0) -> Execution:
+                   tile_bits=0, variant="tf32x3") -> Execution:
         c = circuit.ev_struct()
-        opts = _options(dtype, mode, tile_bits)
+        opts = _options(dtype, mode, tile_bits, variant)
         h = C.c_void_p()
         ncl = circuit.num_classical()
         classical = np.zeros(max(1, ncl), dtype=np.uint8)
@@ -203,10 +212,10 @@ class CudaStateVectorBackend:
 
     @staticmethod
     def run_into(state: State, circuit: Circuit, seed: int = 0, mode="exact",
-                 tile_bits=0) -> list:
+                 tile_bits=0, variant="tf32x3") -> list:
         """Runs a circuit on an existing state (reset to |0...0> first)."""
         c = circuit.ev_struct()
-        opts = _options(state.dtype(), mode, tile_bits)
+        opts = _options(state.dtype(), mode, tile_bits, variant)
         ncl = circuit.num_classical()
         classical = np.zeros(max(1, ncl), dtype=np.uint8)
         N.check(N.lib().ev_state_run(state.handle, C.byref(c), seed, C.byref(opts),

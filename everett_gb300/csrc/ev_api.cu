@@ -182,12 +182,19 @@ struct RunBuffers {
 };
 
 int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int tile_bits,
-              const uint8_t* pred, uint64_t* consumed);
+              const uint8_t* pred, uint64_t* passes_out);
+int fused_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int kbits,
+              int variant, uint64_t* blocks_out);
 
 static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run_options* o,
                    uint8_t* classical_out) {
   const int mode = o ? o->mode : EV_MODE_EXACT;
   const int tile_bits = o ? o->tile_bits : 0;
+  const int variant = o ? o->variant : 0;
+  if (mode == EV_MODE_FUSED && s->dtype != EV_C64)
+    return fail(EV_ERR_INVALID_ARGUMENT, "fused mode needs complex64 amplitudes");
+  if (mode < EV_MODE_EXACT || mode > EV_MODE_FUSED)
+    return fail(EV_ERR_INVALID_ARGUMENT, "unknown run mode %d", mode);
   RunBuffers rb;
   // count Measure records and the nesting of IF chains
   uint64_t nmeas = 0, nif = 0;
@@ -204,7 +211,8 @@ static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run
   EV_CUDA(cudaMalloc(&rb.uniforms, uni.size() * sizeof(double)));
   EV_CUDA(cudaMemcpyAsync(rb.uniforms, uni.data(), uni.size() * sizeof(double),
                           cudaMemcpyHostToDevice, s->stream));
-  EV_CUDA(cudaMemsetAsync(s->scratch.counter, 0, sizeof(uint32_t), s->stream));
+  // counter[0]: uniforms consumed; counter[1]: device timeout flag
+  EV_CUDA(cudaMemsetAsync(s->scratch.counter, 0, 2 * sizeof(uint32_t), s->stream));
   if (nif) EV_CUDA(cudaMalloc(&rb.ifbits, nif * sizeof(uint64_t)));
   // The host copy of the nested-IF bit lists must outlive the async copy.
   std::vector<uint64_t> host_ifbits(nif ? nif : 1);
@@ -230,12 +238,15 @@ static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run
       pred = s->scratch.pred;
     }
     // tiled mode: fuse a run of unconditional gate records
-    if (mode == EV_MODE_TILED && nchain == 0 && c->ops[pos].kind != EV_OP_MEASURE) {
+    if (mode != EV_MODE_EXACT && nchain == 0 && c->ops[pos].kind != EV_OP_MEASURE) {
       uint64_t end = pos;
       while (end < c->nops && c->ops[end].kind != EV_OP_MEASURE && c->ops[end].kind != EV_OP_IF)
         ++end;
-      uint64_t consumed = 0;
-      EV_TRY(tiled_run(s, c, pos, end, tile_bits, nullptr, &consumed));
+      uint64_t passes = 0;
+      if (mode == EV_MODE_TILED)
+        EV_TRY(tiled_run(s, c, pos, end, tile_bits, nullptr, &passes));
+      else
+        EV_TRY(fused_run(s, c, pos, end, tile_bits, variant, &passes));
       pos = end;
       continue;
     }
@@ -267,7 +278,12 @@ static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run
     EV_CUDA(cudaMemcpyAsync(classical_out, rb.classical, c->num_classical, cudaMemcpyDeviceToHost,
                             s->stream));
   }
+  uint32_t flags[2] = {0, 0};
+  EV_CUDA(cudaMemcpyAsync(flags, s->scratch.counter, sizeof(flags), cudaMemcpyDeviceToHost,
+                          s->stream));
   EV_CUDA(cudaStreamSynchronize(s->stream));
+  if (flags[1] != 0)
+    return fail(EV_ERR_TIMEOUT, "a bounded device wait gave up during the run");
   return EV_OK;
 }
 

@@ -1,0 +1,689 @@
+// ev_fused.cu -- complex64 gate runs fused into dense k-qubit unitaries.
+//
+// The host groups consecutive gate records into blocks that act on at most
+// k qubits (a record may move ahead of earlier records that share none of
+// its qubits), multiplies each block's gates into one 2^k x 2^k unitary in
+// f64, and applies each block to the state in one HBM pass.  A block on the
+// qubit set F maps every group of 2^k amplitudes that agree outside F to
+// U times that group: with rows = groups, the state is a (2^(n-k) x 2^k)
+// complex matrix S and the pass computes S U^T.  In the real embedding each
+// row is 2^(k+1) interleaved floats [re_0, im_0, re_1, ...] and
+//     y = x W,  W[2f][2a] = Re U[a][f],  W[2f+1][2a] = -Im U[a][f],
+//               W[2f][2a+1] = Im U[a][f], W[2f+1][2a+1] = Re U[a][f],
+// a real GEMM with K = N = 2^(k+1).
+//
+// Three arithmetics:
+//   EV_FUSED_TF32X3  tcgen05.mma kind::tf32, x = x_hi + x_lo and
+//                    W = W_hi + W_lo split into TF32 parts, D accumulates
+//                    x_hi W_hi + x_hi W_lo + x_lo W_hi in f32 (TMEM)
+//   EV_FUSED_BF16X3  the same with BF16 parts (kind::f16)
+//   EV_FUSED_FP32    CUDA cores, f32 complex multiply-add
+// The tensor-core kernel stages 128 rows per step: loads gather the rows
+// (addresses contiguous for at least 128 amplitudes because the row qubits
+// are the lowest qubits outside F), split into hi/lo and write the A operand
+// in the 128-byte-swizzled K-major layout; one thread issues the MMAs and
+// commits them to an mbarrier; the four warps read their 32 TMEM lanes back
+// and scatter the rows to HBM.  Every mbarrier wait is bounded: on timeout
+// the kernel records an error, frees its TMEM and returns.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <complex>
+#include <cstring>
+#include <vector>
+
+#include "ev_device.cuh"
+#include "ev_internal.h"
+
+namespace ev {
+
+using cd = std::complex<double>;
+
+constexpr int kRows = 128;  // rows per MMA step (UMMA M)
+
+// Per-block index tables, built on the host.
+struct FusedDesc {
+  uint64_t ftab[64];   // global offset of local group index f (bits of F)
+  uint64_t rtab[128];  // global offset of row r within a 128-row step (bits of R)
+  uint64_t hitab[64];  // global offset of the T bits above the contiguous low run
+  uint8_t rlo[128], flo[128];  // local index l: low 7 bits -> (r part, f part)
+  uint8_t rhi[64], fhi[64];    // high bits of l -> (r part, f part)
+  uint8_t comp_hi[64];         // qubits outside T, ascending (row-step index bits)
+  int32_t ncomp_hi;
+  int32_t k;
+  int32_t lowbits;  // T holds qubits 0..lowbits-1
+  int32_t pad;
+  uint64_t nsteps;  // 2^(n-k-7) row steps
+};
+
+// ---- host: fusion ----------------------------------------------------------
+
+struct Block {
+  std::vector<int> F;           // sorted qubits, |F| == k after padding
+  std::vector<uint64_t> ops;    // op indices in application order
+  std::vector<cd> U;            // 2^k x 2^k row-major
+};
+
+static void op_qubits(const ev_circuit* c, const ev_op& op, std::vector<int>* q) {
+  q->clear();
+  if (op.kind == EV_OP_APPLY2) {
+    q->push_back(int(op.q0));
+    q->push_back(int(op.q1));
+    return;
+  }
+  q->push_back(int(op.q0));
+  if (op.kind == EV_OP_CONTROLLED)
+    for (uint32_t j = 0; j < op.nctrl; ++j) {
+      const int cq = int(c->ctrl_pool[op.ctrl_off + j]);
+      if (std::find(q->begin(), q->end(), cq) == q->end()) q->push_back(cq);
+    }
+}
+
+// Left-multiplies U (d x d, local bit i <-> F[i]) by one gate record.
+static void apply_to_unitary(const ev_circuit* c, const ev_op& op, const std::vector<int>& F,
+                             std::vector<cd>* U) {
+  const int d = int(1u << F.size());
+  auto loc = [&](int q) { return int(std::find(F.begin(), F.end(), q) - F.begin()); };
+  auto m = [&](int i) { return cd(op.m[2 * i], op.m[2 * i + 1]); };
+  if (op.kind == EV_OP_APPLY2) {
+    const int ba = 1 << loc(int(op.q0)), bb = 1 << loc(int(op.q1));
+    for (int col = 0; col < d; ++col)
+      for (int base = 0; base < d; ++base) {
+        if (base & (ba | bb)) continue;
+        const int idx[4] = {base, base | bb, base | ba, base | ba | bb};
+        cd in[4], out[4];
+        for (int r = 0; r < 4; ++r) in[r] = (*U)[idx[r] * d + col];
+        for (int r = 0; r < 4; ++r) {
+          out[r] = 0;
+          for (int cc = 0; cc < 4; ++cc) out[r] += m(4 * r + cc) * in[cc];
+        }
+        for (int r = 0; r < 4; ++r) (*U)[idx[r] * d + col] = out[r];
+      }
+    return;
+  }
+  const int tb = 1 << loc(int(op.q0));
+  int cmask = 0;
+  if (op.kind == EV_OP_CONTROLLED)
+    for (uint32_t j = 0; j < op.nctrl; ++j) cmask |= 1 << loc(int(c->ctrl_pool[op.ctrl_off + j]));
+  for (int col = 0; col < d; ++col)
+    for (int i0 = 0; i0 < d; ++i0) {
+      if ((i0 & tb) || (i0 & cmask) != cmask) continue;
+      const int i1 = i0 | tb;
+      const cd a0 = (*U)[i0 * d + col], a1 = (*U)[i1 * d + col];
+      (*U)[i0 * d + col] = m(0) * a0 + m(1) * a1;
+      (*U)[i1 * d + col] = m(2) * a0 + m(3) * a1;
+    }
+}
+
+// Greedy fusion: each block starts at the first pending record and takes
+// every later pending record whose qubits fit (|F| <= k) and which does not
+// touch a qubit of a record skipped before it.
+std::vector<Block> fuse_ops(const ev_circuit* c, uint64_t first, uint64_t last, int n, int k) {
+  std::vector<Block> blocks;
+  std::vector<uint64_t> pending;
+  for (uint64_t j = first; j < last; ++j) pending.push_back(j);
+  std::vector<int> q;
+  const size_t window = 4096;
+  while (!pending.empty()) {
+    Block b;
+    uint64_t fset = 0, blocked = 0;
+    std::vector<uint64_t> rest;
+    size_t scanned = 0;
+    for (size_t i = 0; i < pending.size(); ++i) {
+      const ev_op& op = c->ops[pending[i]];
+      op_qubits(c, op, &q);
+      uint64_t qm = 0;
+      for (int x : q) qm |= uint64_t(1) << x;
+      const bool fits = __builtin_popcountll(fset | qm) <= k && (qm & blocked) == 0;
+      if (fits && scanned < window) {
+        fset |= qm;
+        b.ops.push_back(pending[i]);
+      } else {
+        blocked |= qm;
+        rest.push_back(pending[i]);
+      }
+      ++scanned;
+    }
+    // pad F to exactly k qubits with the lowest unused ones
+    for (int x = 0; x < n && __builtin_popcountll(fset) < k; ++x) fset |= uint64_t(1) << x;
+    for (int x = 0; x < n; ++x)
+      if ((fset >> x) & 1) b.F.push_back(x);
+    const int d = 1 << b.F.size();
+    b.U.assign(size_t(d) * d, cd(0, 0));
+    for (int i = 0; i < d; ++i) b.U[size_t(i) * d + i] = 1;
+    for (uint64_t j : b.ops) apply_to_unitary(c, c->ops[j], b.F, &b.U);
+    blocks.push_back(std::move(b));
+    pending.swap(rest);
+  }
+  return blocks;
+}
+
+static uint64_t pdep(uint64_t x, const std::vector<int>& pos) {
+  uint64_t r = 0;
+  for (size_t i = 0; i < pos.size(); ++i)
+    if ((x >> i) & 1) r |= uint64_t(1) << pos[i];
+  return r;
+}
+
+static void build_desc(const Block& b, int n, FusedDesc* d) {
+  std::memset(d, 0, sizeof(*d));
+  const int k = int(b.F.size());
+  uint64_t fmask = 0;
+  for (int x : b.F) fmask |= uint64_t(1) << x;
+  std::vector<int> R, comp;
+  for (int x = 0; x < n; ++x)
+    if (!((fmask >> x) & 1)) (R.size() < 7 ? R : comp).push_back(x);
+  std::vector<int> T;  // sorted union of F and R
+  for (int x = 0; x < n; ++x)
+    if (((fmask >> x) & 1) || std::find(R.begin(), R.end(), x) != R.end()) T.push_back(x);
+  int low = 0;
+  while (low < int(T.size()) && T[low] == low) ++low;
+  d->k = k;
+  d->lowbits = low;
+  for (int f = 0; f < (1 << k); ++f) d->ftab[f] = pdep(uint64_t(f), b.F);
+  for (int r = 0; r < kRows; ++r) d->rtab[r] = pdep(uint64_t(r), R);
+  std::vector<int> Thi(T.begin() + low, T.end());
+  for (int h = 0; h < (1 << Thi.size()) && h < 64; ++h) d->hitab[h] = pdep(uint64_t(h), Thi);
+  // local index l (bit i <-> T[i]) to (r, f)
+  auto split = [&](uint64_t l, int* r, int* f) {
+    *r = 0;
+    *f = 0;
+    int ri = 0, fi = 0;
+    for (size_t i = 0; i < T.size(); ++i) {
+      const bool inF = (fmask >> T[i]) & 1;
+      if ((l >> i) & 1) {
+        if (inF)
+          *f |= 1 << fi;
+        else
+          *r |= 1 << ri;
+      }
+      inF ? ++fi : ++ri;
+    }
+  };
+  for (int j = 0; j < 128; ++j) {
+    int r, f;
+    split(uint64_t(j), &r, &f);
+    d->rlo[j] = uint8_t(r);
+    d->flo[j] = uint8_t(f);
+  }
+  for (int j = 0; j < (1 << (int(T.size()) - 7)) && j < 64; ++j) {
+    int r, f;
+    split(uint64_t(j) << 7, &r, &f);
+    d->rhi[j] = uint8_t(r);
+    d->fhi[j] = uint8_t(f);
+  }
+  d->ncomp_hi = int(comp.size());
+  for (size_t i = 0; i < comp.size(); ++i) d->comp_hi[i] = uint8_t(comp[i]);
+  d->nsteps = uint64_t(1) << comp.size();
+}
+
+// ---- device: shared helpers --------------------------------------------------
+
+__device__ __forceinline__ uint64_t step_base(const FusedDesc& d, uint64_t step) {
+  uint64_t base = 0;
+  for (int b = 0; b < d.ncomp_hi; ++b)
+    if ((step >> b) & 1) base |= uint64_t(1) << d.comp_hi[b];
+  return base;
+}
+
+// global address of local index l of a step
+__device__ __forceinline__ uint64_t local_addr(const FusedDesc& d, uint64_t base, uint32_t l) {
+  return base | (l & ((1u << d.lowbits) - 1)) | d.hitab[l >> d.lowbits];
+}
+
+// ---- CUDA-core f32 kernel ---------------------------------------------------
+
+template <int KB>
+__global__ void __launch_bounds__(256)
+    k_fused_fp32(float2* __restrict__ s, const FusedDesc* __restrict__ gd,
+                 const float2* __restrict__ U) {
+  constexpr int D = 1 << KB;
+  extern __shared__ __align__(16) unsigned char fp_raw[];
+  float2* tile = reinterpret_cast<float2*>(fp_raw);  // kRows x D
+  float2* um = tile + kRows * D;                     // D x D
+  __shared__ FusedDesc d;
+  for (int i = threadIdx.x; i < int(sizeof(FusedDesc) / 8); i += blockDim.x)
+    reinterpret_cast<uint64_t*>(&d)[i] = reinterpret_cast<const uint64_t*>(gd)[i];
+  for (int i = threadIdx.x; i < D * D; i += blockDim.x) um[i] = U[i];
+  __syncthreads();
+  for (uint64_t step = blockIdx.x; step < d.nsteps; step += gridDim.x) {
+    const uint64_t base = step_base(d, step);
+    for (uint32_t l = threadIdx.x; l < uint32_t(kRows * D); l += blockDim.x) {
+      const int r = d.rlo[l & 127] | d.rhi[l >> 7];
+      const int f = d.flo[l & 127] | d.fhi[l >> 7];
+      tile[r * D + f] = s[local_addr(d, base, l)];
+    }
+    __syncthreads();
+    for (uint32_t o = threadIdx.x; o < uint32_t(kRows * D); o += blockDim.x) {
+      const int r = o % kRows, a = o / kRows;  // consecutive threads: consecutive rows
+      float2 acc = make_float2(0.f, 0.f);
+#pragma unroll 8
+      for (int f = 0; f < D; ++f) {
+        const float2 u = um[a * D + f], x = tile[r * D + f];
+        acc.x = __fmaf_rn(u.x, x.x, __fmaf_rn(-u.y, x.y, acc.x));
+        acc.y = __fmaf_rn(u.x, x.y, __fmaf_rn(u.y, x.x, acc.y));
+      }
+      s[base | d.rtab[r] | d.ftab[a]] = acc;
+    }
+    __syncthreads();
+  }
+}
+
+// ---- tcgen05 kernel ------------------------------------------------------------
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
+// 1024 bytes apart.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
+  uint64_t desc = 0;
+  desc |= uint64_t((addr & 0x3FFFF) >> 4);        // start address
+  desc |= uint64_t(1) << 16;                      // leading byte offset (unused for SW128 K-major)
+  desc |= uint64_t(1024 >> 4) << 32;              // stride byte offset
+  desc |= uint64_t(1) << 46;                      // descriptor version
+  desc |= uint64_t(2) << 61;                      // 128-byte swizzle
+  return desc;
+}
+
+// Byte offset of element (row, kk) in a K-major SW128 operand of `rows` rows
+// whose element size is esz bytes.
+__device__ __forceinline__ uint32_t sw128_off(int row, int kk, int rows, int esz) {
+  const int per_row = 128 / esz;  // elements per 128-byte swizzle row
+  const int kb = kk / per_row, kin = kk % per_row;
+  const int byte = kin * esz;
+  return uint32_t(kb * rows * 128 + (row >> 3) * 1024 + (row & 7) * 128 +
+                  ((((byte >> 4) ^ (row & 7))) << 4) + (byte & 15));
+}
+
+template <int VAR>
+__device__ __forceinline__ void mma_issue(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                          uint32_t acc) {
+  if constexpr (VAR == EV_FUSED_TF32X3) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+  } else {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+  }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit) {
+  const uint32_t a = smem_addr(bar);
+  for (uint32_t it = 0; it < limit; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(a), "r"(phase)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t v[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+}
+
+template <int VAR>
+struct Elem;
+template <>
+struct Elem<EV_FUSED_TF32X3> {
+  static constexpr int size = 4;
+  static constexpr int kstep = 8;  // UMMA K per instruction
+  static constexpr uint32_t fmt = 2;  // TF32
+};
+template <>
+struct Elem<EV_FUSED_BF16X3> {
+  static constexpr int size = 2;
+  static constexpr int kstep = 16;
+  static constexpr uint32_t fmt = 1;  // BF16
+};
+
+// Splits x into hi + lo parts of the operand type and stores both.
+template <int VAR>
+__device__ __forceinline__ void put_split(unsigned char* hi, unsigned char* lo, uint32_t off,
+                                          float re, float im) {
+  if constexpr (VAR == EV_FUSED_TF32X3) {
+    const float hr = __uint_as_float(__float_as_uint(re) & 0xFFFFE000u);
+    const float hm = __uint_as_float(__float_as_uint(im) & 0xFFFFE000u);
+    *reinterpret_cast<float2*>(hi + off) = make_float2(hr, hm);
+    *reinterpret_cast<float2*>(lo + off) = make_float2(re - hr, im - hm);
+  } else {
+    const __nv_bfloat16 hr = __float2bfloat16_rn(re), hm = __float2bfloat16_rn(im);
+    const __nv_bfloat16 lr = __float2bfloat16_rn(re - __bfloat162float(hr));
+    const __nv_bfloat16 lm = __float2bfloat16_rn(im - __bfloat162float(hm));
+    __nv_bfloat162 h2, l2;
+    h2.x = hr;
+    h2.y = hm;
+    l2.x = lr;
+    l2.y = lm;
+    *reinterpret_cast<__nv_bfloat162*>(hi + off) = h2;
+    *reinterpret_cast<__nv_bfloat162*>(lo + off) = l2;
+  }
+}
+
+template <int KB, int VAR>
+struct TcShape {
+  static constexpr int D = 1 << KB;
+  static constexpr int K = 2 * D;  // = N
+  static constexpr int ESZ = Elem<VAR>::size;
+  static constexpr int A_BYTES = kRows * K * ESZ;
+  static constexpr int B_BYTES = K * K * ESZ;
+  static constexpr int SMEM = 2 * A_BYTES + 2 * B_BYTES + 1024 /* align */ + 64;
+  static constexpr int TMEM_COLS = K < 32 ? 32 : K;
+};
+
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+template <int KB, int VAR>
+__global__ void __launch_bounds__(128)
+    k_fused_tc(float2* __restrict__ s, const FusedDesc* __restrict__ gd,
+               const unsigned char* __restrict__ bmat, int* __restrict__ err) {
+  using Sh = TcShape<KB, VAR>;
+  constexpr int D = Sh::D, K = Sh::K, ESZ = Sh::ESZ;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ FusedDesc d;
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_slot;
+  unsigned char* sm = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* a_hi = sm;
+  unsigned char* a_lo = sm + Sh::A_BYTES;
+  unsigned char* b_hi = sm + 2 * Sh::A_BYTES;
+  unsigned char* b_lo = b_hi + Sh::B_BYTES;
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  for (int i = tid; i < int(sizeof(FusedDesc) / 8); i += blockDim.x)
+    reinterpret_cast<uint64_t*>(&d)[i] = reinterpret_cast<const uint64_t*>(gd)[i];
+  // B operands (hi then lo, each [N][K] row-major in the element type) into
+  // the swizzled layout
+  for (int e = tid; e < K * K; e += blockDim.x) {
+    const int nrow = e / K, kk = e % K;
+    const uint32_t off = sw128_off(nrow, kk, K, ESZ);
+    if constexpr (ESZ == 4) {
+      *reinterpret_cast<uint32_t*>(b_hi + off) = reinterpret_cast<const uint32_t*>(bmat)[e];
+      *reinterpret_cast<uint32_t*>(b_lo + off) = reinterpret_cast<const uint32_t*>(bmat)[K * K + e];
+    } else {
+      *reinterpret_cast<uint16_t*>(b_hi + off) = reinterpret_cast<const uint16_t*>(bmat)[e];
+      *reinterpret_cast<uint16_t*>(b_lo + off) = reinterpret_cast<const uint16_t*>(bmat)[K * K + e];
+    }
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(&tmem_slot)),
+                 "r"(uint32_t(Sh::TMEM_COLS)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  // instruction descriptor: f32 accumulate, A/B format, K-major, N, M
+  const uint32_t idesc = (1u << 4) | (Elem<VAR>::fmt << 7) | (Elem<VAR>::fmt << 10) |
+                         (uint32_t(K >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
+  uint32_t phase = 0;
+  bool ok = true;
+  const int row = warp * 32 + (tid & 31);
+  for (uint64_t step = blockIdx.x; step < d.nsteps && ok; step += gridDim.x) {
+    const uint64_t base = step_base(d, step);
+    // load, split, swizzle: two consecutive local indices per 16-byte load
+    for (uint32_t l = 2 * tid; l < uint32_t(kRows * D); l += 2 * blockDim.x) {
+      const float4 v = *reinterpret_cast<const float4*>(s + local_addr(d, base, l));
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const uint32_t li = l + h;
+        const int r = d.rlo[li & 127] | d.rhi[li >> 7];
+        const int f = d.flo[li & 127] | d.fhi[li >> 7];
+        const uint32_t off = sw128_off(r, 2 * f, kRows, ESZ);
+        put_split<VAR>(a_hi, a_lo, off, h ? v.z : v.x, h ? v.w : v.y);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t ah = smem_addr(a_hi), al = smem_addr(a_lo);
+      const uint32_t bh = smem_addr(b_hi), bl = smem_addr(b_lo);
+      constexpr int per_row = 128 / ESZ;
+      uint32_t acc = 0;
+#pragma unroll
+      for (int kk = 0; kk < K; kk += Elem<VAR>::kstep) {
+        const int kb = kk / per_row;
+        const uint32_t kin = uint32_t((kk % per_row) * ESZ);
+        const uint32_t ao = uint32_t(kb * kRows * 128) + kin;
+        const uint32_t bo = uint32_t(kb * K * 128) + kin;
+        mma_issue<VAR>(tmem, sw128_desc(ah + ao), sw128_desc(bh + bo), idesc, acc);
+        acc = 1;
+        mma_issue<VAR>(tmem, sw128_desc(ah + ao), sw128_desc(bl + bo), idesc, 1);
+        mma_issue<VAR>(tmem, sw128_desc(al + ao), sw128_desc(bh + bo), idesc, 1);
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+              smem_addr(&bar))
+          : "memory");
+    }
+    if (!mbar_wait(&bar, phase, kWaitLimit)) {
+      ok = false;
+      atomicExch(err, 1);
+      break;
+    }
+    phase ^= 1;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
+    const uint64_t rbase = base | d.rtab[row];
+#pragma unroll
+    for (int c0 = 0; c0 < K; c0 += 16) {
+      uint32_t v[16];
+      tmem_ld16(lane_base + uint32_t(c0), v);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int a = c0 / 2 + j;
+        s[rbase | d.ftab[a]] = make_float2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+  }
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(uint32_t(Sh::TMEM_COLS)));
+  }
+}
+
+// ---- host: launch ---------------------------------------------------------------
+
+static uint32_t tf32_hi_bits(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  return u & 0xFFFFE000u;
+}
+static float bits_f(uint32_t u) {
+  float x;
+  std::memcpy(&x, &u, 4);
+  return x;
+}
+static uint16_t bf16_rn(float x) {  // round to nearest even
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  const uint32_t lsb = (u >> 16) & 1;
+  u += 0x7FFFu + lsb;
+  return uint16_t(u >> 16);
+}
+static float bf16_f(uint16_t h) { return bits_f(uint32_t(h) << 16); }
+
+// Row-major [N][K] operand images (hi then lo) of W^T for one block.
+static void build_bmat(const Block& b, int variant, std::vector<unsigned char>* out) {
+  const int D = 1 << b.F.size(), K = 2 * D;
+  std::vector<double> Wt(size_t(K) * K);  // Wt[n][k] = W[k][n]
+  for (int a = 0; a < D; ++a)
+    for (int f = 0; f < D; ++f) {
+      const cd u = b.U[size_t(a) * D + f];
+      Wt[size_t(2 * a) * K + 2 * f] = u.real();
+      Wt[size_t(2 * a) * K + 2 * f + 1] = -u.imag();
+      Wt[size_t(2 * a + 1) * K + 2 * f] = u.imag();
+      Wt[size_t(2 * a + 1) * K + 2 * f + 1] = u.real();
+    }
+  if (variant == EV_FUSED_TF32X3) {
+    out->assign(size_t(2) * K * K * 4, 0);
+    uint32_t* hi = reinterpret_cast<uint32_t*>(out->data());
+    uint32_t* lo = hi + size_t(K) * K;
+    for (size_t e = 0; e < Wt.size(); ++e) {
+      const float w = float(Wt[e]);
+      const uint32_t h = tf32_hi_bits(w);
+      const float l = float(Wt[e] - double(bits_f(h)));
+      hi[e] = h;
+      std::memcpy(&lo[e], &l, 4);
+    }
+  } else {
+    out->assign(size_t(2) * K * K * 2, 0);
+    uint16_t* hi = reinterpret_cast<uint16_t*>(out->data());
+    uint16_t* lo = hi + size_t(K) * K;
+    for (size_t e = 0; e < Wt.size(); ++e) {
+      const uint16_t h = bf16_rn(float(Wt[e]));
+      hi[e] = h;
+      lo[e] = bf16_rn(float(Wt[e] - double(bf16_f(h))));
+    }
+  }
+}
+
+template <int KB, int VAR>
+static int launch_tc(ev_state* s, const FusedDesc* dd, const unsigned char* db, uint64_t nsteps,
+                     int* derr) {
+  using Sh = TcShape<KB, VAR>;
+  EV_CUDA(cudaFuncSetAttribute(k_fused_tc<KB, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               Sh::SMEM));
+  int per_sm = 0;
+  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tc<KB, VAR>, 128, Sh::SMEM));
+  if (per_sm < 1) per_sm = 1;
+  // keep every CTA's TMEM allocation satisfiable at once
+  const int tmem_cap = 512 / Sh::TMEM_COLS;
+  if (per_sm > tmem_cap) per_sm = tmem_cap;
+  uint64_t grid = uint64_t(s->num_sms) * per_sm;
+  if (grid > nsteps) grid = nsteps;
+  k_fused_tc<KB, VAR><<<unsigned(grid), 128, Sh::SMEM, s->stream>>>(static_cast<float2*>(s->amps),
+                                                                    dd, db, derr);
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
+template <int KB>
+static int launch_fp32(ev_state* s, const FusedDesc* dd, const float2* du, uint64_t nsteps) {
+  constexpr int D = 1 << KB;
+  const int smem = int(sizeof(float2)) * (kRows * D + D * D);
+  EV_CUDA(cudaFuncSetAttribute(k_fused_fp32<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  uint64_t grid = uint64_t(s->num_sms) * 2;
+  if (grid > nsteps) grid = nsteps;
+  k_fused_fp32<KB><<<unsigned(grid), 256, smem, s->stream>>>(static_cast<float2*>(s->amps), dd, du);
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
+int default_fused_bits() { return 5; }
+
+int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int tile_bits,
+              const uint8_t* pred, uint64_t* passes_out);
+
+// Fusion width actually used for a variant and a request (0 = default).
+int fused_width(int variant, int kbits) {
+  int k = kbits > 0 ? kbits : default_fused_bits();
+  if (k > 6) k = 6;
+  if (k < 1) k = 1;
+  if (variant == EV_FUSED_TF32X3) return 5;
+  if (variant == EV_FUSED_BF16X3) return k >= 6 ? 6 : 5;
+  return k;
+}
+
+int fused_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int kbits,
+              int variant, uint64_t* blocks_out) {
+  if (s->dtype != EV_C64) return fail(EV_ERR_INVALID_ARGUMENT, "fused mode needs a complex64 state");
+  if (variant < EV_FUSED_TF32X3 || variant > EV_FUSED_FP32)
+    return fail(EV_ERR_INVALID_ARGUMENT, "unknown fused variant %d", variant);
+  const int n = int(s->n);
+  const int k = fused_width(variant, kbits);
+  // registers too small for 128-row steps run through the tile pass
+  if (n < k + 7) return tiled_run(s, c, first, last, 0, nullptr, blocks_out);
+  const bool tc = variant != EV_FUSED_FP32;
+  std::vector<Block> blocks = fuse_ops(c, first, last, n, k);
+  if (blocks_out) *blocks_out = blocks.size();
+  if (blocks.empty()) return EV_OK;
+  // one device buffer: descriptors, then per-block matrices
+  std::vector<std::vector<unsigned char>> mats(blocks.size());
+  for (size_t i = 0; i < blocks.size(); ++i) {
+    if (tc) {
+      build_bmat(blocks[i], variant, &mats[i]);
+    } else {
+      const int D = 1 << blocks[i].F.size();
+      mats[i].resize(size_t(D) * D * sizeof(float2));
+      float2* u = reinterpret_cast<float2*>(mats[i].data());
+      for (int e = 0; e < D * D; ++e)
+        u[e] = make_float2(float(blocks[i].U[e].real()), float(blocks[i].U[e].imag()));
+    }
+  }
+  const size_t desc_bytes = (blocks.size() * sizeof(FusedDesc) + 255) / 256 * 256;
+  std::vector<size_t> mat_off(blocks.size());
+  size_t total = desc_bytes;
+  for (size_t i = 0; i < blocks.size(); ++i) {
+    mat_off[i] = total;
+    total += (mats[i].size() + 255) / 256 * 256;
+  }
+  std::vector<unsigned char> host(total, 0);
+  for (size_t i = 0; i < blocks.size(); ++i) {
+    build_desc(blocks[i], n, reinterpret_cast<FusedDesc*>(host.data()) + i);
+    std::memcpy(host.data() + mat_off[i], mats[i].data(), mats[i].size());
+  }
+  unsigned char* dbuf = nullptr;
+  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dbuf), total, s->stream));
+  EV_CUDA(cudaMemcpyAsync(dbuf, host.data(), total, cudaMemcpyHostToDevice, s->stream));
+  int* derr = reinterpret_cast<int*>(s->scratch.counter + 1);
+  int rc = EV_OK;
+  for (size_t i = 0; i < blocks.size() && rc == EV_OK; ++i) {
+    const FusedDesc* dd = reinterpret_cast<const FusedDesc*>(dbuf) + i;
+    const unsigned char* dm = dbuf + mat_off[i];
+    const uint64_t nsteps = reinterpret_cast<const FusedDesc*>(host.data())[i].nsteps;
+    ProfScope prof(s, P_FUSED, 2.0 * double(s->len()) * 8.0);
+    s->launches += 1;
+    const int kb = int(blocks[i].F.size());
+    if (tc) {
+      if (variant == EV_FUSED_TF32X3)
+        rc = launch_tc<5, EV_FUSED_TF32X3>(s, dd, dm, nsteps, derr);
+      else if (kb == 5)
+        rc = launch_tc<5, EV_FUSED_BF16X3>(s, dd, dm, nsteps, derr);
+      else
+        rc = launch_tc<6, EV_FUSED_BF16X3>(s, dd, dm, nsteps, derr);
+    } else {
+      const float2* du = reinterpret_cast<const float2*>(dm);
+      switch (kb) {
+        case 1: rc = launch_fp32<1>(s, dd, du, nsteps); break;
+        case 2: rc = launch_fp32<2>(s, dd, du, nsteps); break;
+        case 3: rc = launch_fp32<3>(s, dd, du, nsteps); break;
+        case 4: rc = launch_fp32<4>(s, dd, du, nsteps); break;
+        case 5: rc = launch_fp32<5>(s, dd, du, nsteps); break;
+        default: rc = launch_fp32<6>(s, dd, du, nsteps); break;
+      }
+    }
+  }
+  cudaFreeAsync(dbuf, s->stream);
+  return rc;
+}
+
+}  // namespace ev

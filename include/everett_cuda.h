@@ -87,14 +87,23 @@ typedef struct ev_circuit {
 /* Execution options of the run loop. */
 enum {
   EV_MODE_EXACT = 0, /* one kernel per op, the reference's arithmetic order */
-  EV_MODE_TILED = 1  /* runs of low-qubit ops applied in one shared-memory
-                        pass; same per-amplitude arithmetic, fewer passes  */
+  EV_MODE_TILED = 1, /* runs of ops applied to shared-memory tiles, one HBM
+                        pass per run; same per-amplitude arithmetic        */
+  EV_MODE_FUSED = 2  /* complex64 only: runs of ops fused on the host (f64)
+                        into dense k-qubit unitaries, one HBM pass each    */
+};
+/* Arithmetic of a fused k-qubit unitary (EV_MODE_FUSED). */
+enum {
+  EV_FUSED_TF32X3 = 0, /* tensor cores, split TF32 products, f32 accumulate */
+  EV_FUSED_BF16X3 = 1, /* tensor cores, split BF16 products, f32 accumulate */
+  EV_FUSED_FP32 = 2    /* CUDA cores, f32 complex multiply-add              */
 };
 typedef struct ev_run_options {
   int32_t dtype;     /* EV_C128 or EV_C64                                  */
   int32_t mode;      /* EV_MODE_*                                          */
-  int32_t tile_bits; /* tiled mode: qubits per shared-memory tile (0=auto) */
-  int32_t reserved;
+  int32_t tile_bits; /* tiled: qubits per tile; fused: qubits per unitary
+                        (0 = default)                                      */
+  int32_t variant;   /* fused: EV_FUSED_*                                  */
 } ev_run_options;
 
 typedef struct ev_state ev_state;
