@@ -14,6 +14,7 @@
 //     consume one (matching rng.next_f64() being called only inside
 //     measure_qubit).
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -34,6 +35,14 @@ int fail(int code, const char* fmt, ...) {
   return code;
 }
 void clear_error() { g_err[0] = 0; }
+
+bool debug_enabled() {
+  static const bool on = [] {
+    const char* v = getenv("EV_DEBUG");
+    return v != nullptr && v[0] != 0 && v[0] != '0';
+  }();
+  return on;
+}
 
 __global__ void k_set_basis0_c128(double2* a) { a[0] = make_double2(1.0, 0.0); }
 __global__ void k_set_basis0_c64(float2* a) { a[0] = make_float2(1.0f, 0.0f); }

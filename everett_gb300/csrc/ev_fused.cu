@@ -27,6 +27,8 @@
 // the kernel records an error, frees its TMEM and returns.
 #include <cuda_bf16.h>
 
+#include <cstdio>
+
 #include <algorithm>
 #include <complex>
 #include <cstring>
@@ -388,8 +390,10 @@ struct TcShape {
 
 constexpr uint32_t kWaitLimit = 1u << 24;
 
+constexpr int kTcThreads = 256;  // 8 warps: warps w and w+4 share TMEM lane quarter w
+
 template <int KB, int VAR>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kTcThreads)
     k_fused_tc(float2* __restrict__ s, const FusedDesc* __restrict__ gd,
                const unsigned char* __restrict__ bmat, int* __restrict__ err) {
   using Sh = TcShape<KB, VAR>;
@@ -441,19 +445,64 @@ __global__ void __launch_bounds__(128)
                          (uint32_t(K >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
   uint32_t phase = 0;
   bool ok = true;
-  const int row = warp * 32 + (tid & 31);
+  // Thread t owns row r = t mod 128 (its TMEM lane) and the groups of four
+  // consecutive complex values g = t/128, t/128 + 2, ...  A group is 8
+  // reals: one 16-byte swizzle chunk in BF16, two in TF32, so the A operand
+  // is written with whole-chunk stores; the 8 rows of a swizzle atom land in
+  // 8 different bank groups.  A warp holds 32 consecutive rows, i.e. the
+  // lowest qubits outside F, so its loads of one f are contiguous in HBM.
+  const int quarter = warp & 3, half = warp >> 2;
+  const int row = quarter * 32 + (tid & 31);
+  constexpr int G = D / 4;                         // groups per row
+  constexpr int GPT = G / (kTcThreads / kRows);    // groups per thread
+  const uint32_t rsw = uint32_t((row >> 3) * 1024 + (row & 7) * 128);
+  const uint32_t rx = uint32_t(row & 7);
+  const uint64_t roff = d.rtab[row];
   for (uint64_t step = blockIdx.x; step < d.nsteps && ok; step += gridDim.x) {
-    const uint64_t base = step_base(d, step);
-    // load, split, swizzle: two consecutive local indices per 16-byte load
-    for (uint32_t l = 2 * tid; l < uint32_t(kRows * D); l += 2 * blockDim.x) {
-      const float4 v = *reinterpret_cast<const float4*>(s + local_addr(d, base, l));
+    const uint64_t rbase = step_base(d, step) | roff;
+    float2 x[GPT][4];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const uint32_t li = l + h;
-        const int r = d.rlo[li & 127] | d.rhi[li >> 7];
-        const int f = d.flo[li & 127] | d.fhi[li >> 7];
-        const uint32_t off = sw128_off(r, 2 * f, kRows, ESZ);
-        put_split<VAR>(a_hi, a_lo, off, h ? v.z : v.x, h ? v.w : v.y);
+    for (int gi = 0; gi < GPT; ++gi) {
+      const int g = half + 2 * gi;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) x[gi][i] = __ldcs(s + (rbase | d.ftab[4 * g + i]));
+    }
+#pragma unroll
+    for (int gi = 0; gi < GPT; ++gi) {
+      const int g = half + 2 * gi;
+      if constexpr (VAR == EV_FUSED_TF32X3) {
+        // reals 8g..8g+7: K-block g/4, chunks 2(g%4) and 2(g%4)+1
+        const uint32_t kb = uint32_t(g / 4) * kRows * 128 + rsw;
+        const uint32_t c0 = uint32_t(2 * (g % 4));
+        float hi[8], lo[8];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float re = x[gi][i].x, im = x[gi][i].y;
+          hi[2 * i] = __uint_as_float(__float_as_uint(re) & 0xFFFFE000u);
+          hi[2 * i + 1] = __uint_as_float(__float_as_uint(im) & 0xFFFFE000u);
+          lo[2 * i] = re - hi[2 * i];
+          lo[2 * i + 1] = im - hi[2 * i + 1];
+        }
+        const uint32_t o0 = kb + (((c0) ^ rx) << 4), o1 = kb + (((c0 + 1) ^ rx) << 4);
+        *reinterpret_cast<float4*>(a_hi + o0) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<float4*>(a_hi + o1) = make_float4(hi[4], hi[5], hi[6], hi[7]);
+        *reinterpret_cast<float4*>(a_lo + o0) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+        *reinterpret_cast<float4*>(a_lo + o1) = make_float4(lo[4], lo[5], lo[6], lo[7]);
+      } else {
+        // reals 8g..8g+7: K-block g/8, chunk g%8
+        const uint32_t o = uint32_t(g / 8) * kRows * 128 + rsw + ((uint32_t(g % 8) ^ rx) << 4);
+        uint32_t hw[4], lw[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float re = x[gi][i].x, im = x[gi][i].y;
+          const __nv_bfloat16 hr = __float2bfloat16_rn(re), hm = __float2bfloat16_rn(im);
+          const __nv_bfloat16 lr = __float2bfloat16_rn(re - __bfloat162float(hr));
+          const __nv_bfloat16 lm = __float2bfloat16_rn(im - __bfloat162float(hm));
+          hw[i] = uint32_t(__bfloat16_as_ushort(hr)) | (uint32_t(__bfloat16_as_ushort(hm)) << 16);
+          lw[i] = uint32_t(__bfloat16_as_ushort(lr)) | (uint32_t(__bfloat16_as_ushort(lm)) << 16);
+        }
+        *reinterpret_cast<uint4*>(a_hi + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *reinterpret_cast<uint4*>(a_lo + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
       }
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -487,17 +536,28 @@ __global__ void __launch_bounds__(128)
     }
     phase ^= 1;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const uint32_t lane_base = tmem + (uint32_t(warp * 32) << 16);
-    const uint64_t rbase = base | d.rtab[row];
+    const uint32_t lane_base = tmem + (uint32_t(quarter * 32) << 16);
+    const bool pair_store = d.ftab[1] == 1;  // f bit 0 is qubit 0: outputs a, a+1 adjacent
 #pragma unroll
-    for (int c0 = 0; c0 < K; c0 += 16) {
-      uint32_t v[16];
-      tmem_ld16(lane_base + uint32_t(c0), v);
+    for (int c0 = half * (K / 2); c0 < (half + 1) * (K / 2); c0 += 16) {
+      uint32_t w[16];
+      tmem_ld16(lane_base + uint32_t(c0), w);
       asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (pair_store) {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int a = c0 / 2 + j;
-        s[rbase | d.ftab[a]] = make_float2(__uint_as_float(v[2 * j]), __uint_as_float(v[2 * j + 1]));
+        for (int j = 0; j < 8; j += 2) {
+          const int a = c0 / 2 + j;
+          __stcs(reinterpret_cast<float4*>(s + (rbase | d.ftab[a])),
+                 make_float4(__uint_as_float(w[2 * j]), __uint_as_float(w[2 * j + 1]),
+                             __uint_as_float(w[2 * j + 2]), __uint_as_float(w[2 * j + 3])));
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+          const int a = c0 / 2 + j;
+          __stcs(s + (rbase | d.ftab[a]),
+                 make_float2(__uint_as_float(w[2 * j]), __uint_as_float(w[2 * j + 1])));
+        }
       }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -572,16 +632,31 @@ static int launch_tc(ev_state* s, const FusedDesc* dd, const unsigned char* db, 
   using Sh = TcShape<KB, VAR>;
   EV_CUDA(cudaFuncSetAttribute(k_fused_tc<KB, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                Sh::SMEM));
-  int per_sm = 0;
-  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fused_tc<KB, VAR>, 128, Sh::SMEM));
+  EV_CUDA(cudaFuncSetAttribute(k_fused_tc<KB, VAR>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               int(cudaSharedmemCarveoutMaxShared)));
+  // resident CTAs from the SM's shared-memory budget (dynamic + static +
+  // the 1 KiB the runtime reserves per CTA)
+  cudaFuncAttributes fa{};
+  EV_CUDA(cudaFuncGetAttributes(&fa, k_fused_tc<KB, VAR>));
+  int smem_sm = 0;
+  EV_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->device));
+  int per_sm = smem_sm / int(Sh::SMEM + fa.sharedSizeBytes + 1024);
+  int regs_sm = 0;
+  EV_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, s->device));
+  const int by_regs = regs_sm / ((fa.numRegs + 7) / 8 * 8 * kTcThreads);
+  if (per_sm > by_regs) per_sm = by_regs;
   if (per_sm < 1) per_sm = 1;
-  // keep every CTA's TMEM allocation satisfiable at once
+  // keep every resident CTA's TMEM allocation satisfiable at once
   const int tmem_cap = 512 / Sh::TMEM_COLS;
   if (per_sm > tmem_cap) per_sm = tmem_cap;
+  s->tc_ctas_per_sm = per_sm;
   uint64_t grid = uint64_t(s->num_sms) * per_sm;
   if (grid > nsteps) grid = nsteps;
-  k_fused_tc<KB, VAR><<<unsigned(grid), 128, Sh::SMEM, s->stream>>>(static_cast<float2*>(s->amps),
-                                                                    dd, db, derr);
+  if (debug_enabled())
+    fprintf(stderr, "[ev] k_fused_tc<%d,%d> smem %d+%zu per CTA, %d CTAs/SM, grid %llu\n", KB, VAR,
+            Sh::SMEM, size_t(fa.sharedSizeBytes), per_sm, (unsigned long long)grid);
+  k_fused_tc<KB, VAR><<<unsigned(grid), kTcThreads, Sh::SMEM, s->stream>>>(
+      static_cast<float2*>(s->amps), dd, db, derr);
   EV_CUDA(cudaGetLastError());
   return EV_OK;
 }
@@ -591,6 +666,8 @@ static int launch_fp32(ev_state* s, const FusedDesc* dd, const float2* du, uint6
   constexpr int D = 1 << KB;
   const int smem = int(sizeof(float2)) * (kRows * D + D * D);
   EV_CUDA(cudaFuncSetAttribute(k_fused_fp32<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  EV_CUDA(cudaFuncSetAttribute(k_fused_fp32<KB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               int(cudaSharedmemCarveoutMaxShared)));
   uint64_t grid = uint64_t(s->num_sms) * 2;
   if (grid > nsteps) grid = nsteps;
   k_fused_fp32<KB><<<unsigned(grid), 256, smem, s->stream>>>(static_cast<float2*>(s->amps), dd, du);

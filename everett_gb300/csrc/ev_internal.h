@@ -14,6 +14,9 @@ namespace ev {
 int fail(int code, const char* fmt, ...);
 // Clears the thread's last error.
 void clear_error();
+// True when EV_DEBUG is set in the environment (launch configurations are
+// then printed to stderr).
+bool debug_enabled();
 
 #define EV_CUDA(call)                                                                \
   do {                                                                               \
@@ -72,6 +75,7 @@ struct ev_state {
   double* mass = nullptr;  // sampling tree, 2^n - 1 doubles, allocated on demand
   uint64_t mass_len = 0;
   mutable uint64_t launches = 0;  // kernels launched for this state
+  int tc_ctas_per_sm = 0;         // last tensor-core launch: resident CTAs per SM
   cudaEvent_t slots[16] = {};
   bool profiling = false;
   std::vector<ev::ProfRec> pending;

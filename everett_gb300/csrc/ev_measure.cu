@@ -54,6 +54,26 @@ __device__ __forceinline__ void red_term(const V* __restrict__ a, const V* __res
 
 // Block b reduces the contiguous counter range [b*chunk, (b+1)*chunk) and
 // writes 4 partials; the tree inside the block has a fixed shape.
+// Compensated f32 accumulation of |x|^2 for complex64 norms: each square is
+// split exactly into p + e (p = x*x, e = fma(x, x, -p)), the p terms are
+// summed with Neumaier's compensated sum and the (tiny) e terms plainly;
+// every 64 elements the partial joins the f64 accumulator.  Keeps the f64
+// pipe out of the per-element path while the result agrees with an f64 sum
+// to ~1e-14 relative.
+struct CompSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x;
+    c += fabsf(s) >= fabsf(x) ? (s - t) + x : (x - t) + s;
+    s = t;
+  }
+  __device__ __forceinline__ void add_sq(float x) {
+    const float p = x * x;
+    c += __fmaf_rn(x, x, -p);
+    add(p);
+  }
+};
+
 template <int OP, typename V>
 __global__ void __launch_bounds__(kRedThreads)
     k_reduce(const V* __restrict__ a, const V* __restrict__ b, uint64_t count, uint64_t chunk,
@@ -62,7 +82,23 @@ __global__ void __launch_bounds__(kRedThreads)
   double acc[4] = {0.0, 0.0, 0.0, 0.0};
   const uint64_t lo = uint64_t(blockIdx.x) * chunk;
   const uint64_t hi = lo + chunk < count ? lo + chunk : count;
-  for (uint64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) red_term<OP>(a, b, i, k, acc);
+  if constexpr (sizeof(V) == 8 && (OP == R_NORM || OP == R_P1)) {
+    CompSum cs;
+    int n = 0;
+    for (uint64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) {
+      const V x = OP == R_NORM ? a[i] : a[insert0(i, k) | (uint64_t(1) << k)];
+      cs.add_sq(x.x);
+      cs.add_sq(x.y);
+      if (++n == 64) {
+        acc[0] += double(cs.s) + double(cs.c);
+        cs = CompSum();
+        n = 0;
+      }
+    }
+    acc[0] += double(cs.s) + double(cs.c);
+  } else {
+    for (uint64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) red_term<OP>(a, b, i, k, acc);
+  }
   __shared__ double sh[4][kRedThreads];
 #pragma unroll
   for (int c = 0; c < 4; ++c) sh[c][threadIdx.x] = acc[c];
@@ -118,12 +154,17 @@ __global__ void k_decide(const double* __restrict__ result, double u_host,
   if (outcome_dev != nullptr) *outcome_dev = outcome ? 1 : 0;
 }
 
+// Rescaling by an f64 factor: complex128 multiplies in f64 (Complex64 * f64,
+// complex.rs:127-133); complex64 applies the f64-computed factor rounded to
+// f32, which changes a result by at most one f32 rounding.
 template <typename V>
 __device__ __forceinline__ V scale_amp(V a, double s) {
-  if constexpr (sizeof(V) == 16)
+  if constexpr (sizeof(V) == 16) {
     return make_double2(__dmul_rn(a.x, s), __dmul_rn(a.y, s));
-  else
-    return make_float2(float(__dmul_rn(double(a.x), s)), float(__dmul_rn(double(a.y), s)));
+  } else {
+    const float f = float(s);
+    return make_float2(__fmul_rn(a.x, f), __fmul_rn(a.y, f));
+  }
 }
 
 // Pass 2 of measure_qubit (measure.rs:40-48).

@@ -316,6 +316,8 @@ static int launch_tile(ev_state* s, uint64_t ntiles, const TilePlan& plan, const
                          sizeof(uint64_t) * (size_t(1) << (plan.k - plan.L)) + 15) & ~size_t(15);
   const size_t smem = ops_at + sizeof(TileOp) * size_t(nops) + 64;
   EV_CUDA(cudaFuncSetAttribute(k_tile<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+  EV_CUDA(cudaFuncSetAttribute(k_tile<V>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               int(cudaSharedmemCarveoutMaxShared)));
   int per_sm = 0;
   EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<V>, kTileThreads, smem));
   if (per_sm < 1) per_sm = 1;
