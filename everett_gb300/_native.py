@@ -88,6 +88,7 @@ _SIGS = {
     "ev_state_launch_count": [_P, C.POINTER(_U64)],
     "ev_state_profile": [_P, _I32],
     "ev_state_profile_read": [_P, _P, _I32, C.POINTER(_I32)],
+    "ev_batch_run": [_P, _U64, _P, _P],
     "ev_host_alloc": [_U64, C.POINTER(_P)],
     "ev_host_free": [_P],
 }

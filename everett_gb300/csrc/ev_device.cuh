@@ -77,3 +77,34 @@ __device__ __forceinline__ uint64_t insert0(uint64_t i, int k) {
 }
 
 }  // namespace ev
+
+namespace ev {
+// xoshiro256++ seeded through SplitMix64 (the reference's Rng,
+// src/rng.rs:18-58), for uniforms drawn on the device.
+struct DevRng {
+  uint64_t s[4];
+  __device__ explicit DevRng(uint64_t seed) {
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+      seed += 0x9E3779B97F4A7C15ULL;
+      uint64_t z = seed;
+      z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+      z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+      s[w] = z ^ (z >> 31);
+    }
+  }
+  __device__ static uint64_t rotl(uint64_t x, int r) { return (x << r) | (x >> (64 - r)); }
+  __device__ uint64_t next_u64() {
+    const uint64_t result = rotl(s[0] + s[3], 23) + s[0];
+    const uint64_t t = s[1] << 17;
+    s[2] ^= s[0];
+    s[3] ^= s[1];
+    s[1] ^= s[2];
+    s[0] ^= s[3];
+    s[2] ^= t;
+    s[3] = rotl(s[3], 45);
+    return result;
+  }
+  __device__ double next_f64() { return double(next_u64() >> 11) * (1.0 / 9007199254740992.0); }
+};
+}  // namespace ev

@@ -167,3 +167,71 @@ def gate_bytes(circuit: Circuit, amp_bytes: int = 16) -> int:
     op_bytes)."""
     n = circuit.num_qubits()
     return sum(op_bytes(op, n, amp_bytes) for op in circuit.ops())
+
+
+class RawCircuit:
+    """A gate-only circuit held directly as C ABI op records (for large
+    generated workloads where building Python op objects would dominate)."""
+
+    def __init__(self, n: int, ops: np.ndarray):
+        from . import _native as N
+        self._n = n
+        self._ops = np.ascontiguousarray(ops, dtype=N.OP_DTYPE)
+        self._ctrl = np.zeros(1, dtype=np.uint64)
+
+    def num_qubits(self) -> int:
+        return self._n
+
+    def num_classical(self) -> int:
+        return 0
+
+    def __len__(self) -> int:
+        return len(self._ops)
+
+    def to_ev(self):
+        return self._ops, self._ctrl, 0
+
+    def ev_struct(self):
+        from . import _native as N
+        c = N.EvCircuit()
+        c.num_qubits = self._n
+        c.num_classical = 0
+        c.ops = self._ops.ctypes.data if len(self._ops) else None
+        c.nops = len(self._ops)
+        c.ctrl_pool = self._ctrl.ctypes.data
+        c.pool_len = 0
+        return c
+
+    def to_circuit(self) -> Circuit:
+        """The same ops as a builder Circuit (for the oracle and small cases)."""
+        from .gate import Gate1, Gate2
+        c = Circuit(self._n)
+        for r in self._ops:
+            m = r["m"].view(np.complex128)
+            if r["kind"] == 1:
+                c.gate1(Gate1(*m[:4]), int(r["q0"]))
+            else:
+                c.gate2(Gate2(m), int(r["q0"]), int(r["q1"]))
+        return c
+
+
+def tfim_raw(rng: Rng, nmin: int = 8, nmax: int = 20, smin: int = 10, smax: int = 50,
+             dt: float = 0.05) -> RawCircuit:
+    """tfim_instance with the same draws, emitted as op records: steps of
+    RZZ(2 J_i dt) on every bond, then RX(2 h_i dt) on every qubit."""
+    from . import _native as N
+    n = nmin + int(rng.next_u64() % (nmax - nmin + 1))
+    steps = smin + int(rng.next_u64() % (smax - smin + 1))
+    J = [0.5 + rng.next_f64() for _ in range(n - 1)]
+    h = [0.5 + rng.next_f64() for _ in range(n)]
+    step = np.zeros(2 * n - 1, dtype=N.OP_DTYPE)
+    for i in range(n - 1):
+        step[i]["kind"] = N.OP_APPLY2
+        step[i]["q0"], step[i]["q1"] = i, i + 1
+        step[i]["m"][:] = Gate2.rzz(2.0 * J[i] * dt).as_f64()
+    for i in range(n):
+        r = step[n - 1 + i]
+        r["kind"] = N.OP_APPLY1
+        r["q0"] = i
+        r["m"][:8] = Gate1.rx(2.0 * h[i] * dt).as_f64()
+    return RawCircuit(n, np.tile(step, steps))

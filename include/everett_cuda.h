@@ -208,6 +208,43 @@ int ev_state_run(ev_state* s, const ev_circuit* c, uint64_t seed,
  * The state is not modified.  n <= 63. */
 int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* out);
 
+/* ---- batched runs (no reference counterpart) ------------------------------
+ * Many independent circuits of uneven qubit counts in one persistent launch
+ * over a device work queue.  Each circuit holds gate records only
+ * (EV_OP_APPLY1/APPLY2/CONTROLLED); it runs from |0...0> and reports
+ * <Z_0> (bloch_vector(0)[2] of the final state, normalised) and `shots`
+ * full-register shots drawn exactly as ev_sample draws them with its own
+ * seed.  Output pointers may be NULL. */
+typedef struct ev_batch_circuit {
+  ev_circuit circuit;
+  uint64_t seed;       /* Rng seed of the shot stream                      */
+  uint64_t shots;
+  uint64_t* shots_out; /* [shots]                                          */
+  double* expz_out;    /* <Z_0>                                            */
+  double* amps_out;    /* final state, 2^n interleaved f64 (test hook)     */
+} ev_batch_circuit;
+
+typedef struct ev_batch_options {
+  int32_t dtype;     /* EV_C64 (default) or EV_C128                        */
+  int32_t tile_bits; /* qubits per shared-memory tile; 0 = autotuned       */
+  int32_t threads;   /* threads per resident CTA (256 / 512); 0 = autotuned */
+  int32_t autotune;  /* 1: time candidates when no cached choice exists   */
+} ev_batch_options;
+
+typedef struct ev_batch_stats {
+  double device_ms;  /* persistent launch + uniform generation            */
+  double host_ms;    /* planning, copies, result scatter                  */
+  uint64_t items;    /* work-queue items                                   */
+  uint64_t launches; /* kernels launched                                   */
+  int32_t tile_bits; /* configuration used                                 */
+  int32_t threads;
+  int32_t from_cache; /* 1 if the configuration came from the tuning cache */
+  int32_t reserved;
+} ev_batch_stats;
+
+int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const ev_batch_options* opts,
+                 ev_batch_stats* stats);
+
 /* ---- measurement hooks (no reference counterpart) ------------------------
  * Used by benchmarks and profilers: events on the state's stream, the number
  * of kernels the engine has launched for a state, per-kernel-class timing

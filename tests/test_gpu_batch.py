@@ -1,0 +1,85 @@
+"""GPU parity of the batched runner against the oracle.
+
+complex128 batches: every final state bit-identical to the oracle's run,
+<Z_0> within 1e-12, shots identical to the oracle's conditional-mass tree.
+complex64 batches: fidelity >= 1 - 1e-6 against the oracle, shots identical
+to the tree of the batch's own final state.  Small tiles force the larger
+circuits through the multi-pass (tile, dependency-counter) queue items."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from everett_gb300 import Circuit, Gate1, Rng, batch, workloads
+from everett_gb300.error import InvalidArgument
+
+pytestmark = pytest.mark.gpu
+
+
+def tfim_mix(count, nmin, nmax, seed, smin=2, smax=6):
+    rng = Rng.seed_from_u64(seed)
+    return [workloads.tfim_instance(rng, nmin, nmax, smin, smax) for _ in range(count)]
+
+
+def oracle_expz(amps):
+    b = O.bloch_vector(amps, 0)
+    return b[2] / O.norm_sqr(amps)
+
+
+@pytest.mark.parametrize("tile_bits", [6, 8, 12])
+def test_batch_c128_bit_exact(gpu, tile_bits):
+    circs = tfim_mix(24, 2, 13, seed=tile_bits)
+    circs.append(workloads.random_layers(11, 4, seed=9))
+    circs.append(workloads.qft_on_basis(9, 300))
+    circs += [Circuit(3), Circuit(14)]  # no ops: the state stays |0...0>
+    res, stats = batch.run_batch(circs, seeds=range(100, 100 + len(circs)), shots=300,
+                                 dtype="complex128", tile_bits=tile_bits, threads=256,
+                                 return_states=True)
+    assert stats["tile_bits"] == tile_bits
+    for c, r, seed in zip(circs, res, range(100, 100 + len(circs))):
+        want, _, _ = O.run_seeded(c, 0)
+        assert np.array_equal(r.amplitudes, want), c.num_qubits()
+        assert abs(r.expz - oracle_expz(want)) < 1e-12
+        assert np.array_equal(r.shots, O.sample_tree(want, seed, 300))
+
+
+@pytest.mark.parametrize("threads", [256, 512])
+def test_batch_c64_fidelity_and_shots(gpu, threads):
+    circs = tfim_mix(40, 3, 16, seed=7, smin=3, smax=8)
+    res, stats = batch.run_batch(circs, seeds=range(len(circs)), shots=200, dtype="complex64",
+                                 tile_bits=10, threads=threads, return_states=True)
+    for i, (c, r) in enumerate(zip(circs, res)):
+        want, _, _ = O.run_seeded(c, 0)
+        got = r.amplitudes
+        fid = abs(np.vdot(want, got)) ** 2 / (np.vdot(got, got).real * np.vdot(want, want).real)
+        assert fid >= 1 - 1e-6
+        assert abs(r.expz - oracle_expz(want)) < 1e-5
+        assert np.array_equal(r.shots, O.sample_tree(np.ascontiguousarray(got), i, 200))
+
+
+def test_batch_matches_single_runs(gpu):
+    """A circuit gives the same final state alone and inside a batch."""
+    circs = tfim_mix(12, 4, 14, seed=3)
+    alone = [batch.run_batch([c], shots=50, dtype="complex128", tile_bits=9, threads=256,
+                             return_states=True)[0][0] for c in circs]
+    mixed, _ = batch.run_batch(circs, shots=50, dtype="complex128", tile_bits=9, threads=256,
+                               return_states=True)
+    for a, m in zip(alone, mixed):
+        assert np.array_equal(a.amplitudes, m.amplitudes)
+
+
+def test_batch_rejects_measurement_and_autotunes(gpu, tmp_path):
+    c = Circuit.with_classical(3, 1)
+    c.h(0).measure(0, 0)
+    with pytest.raises(InvalidArgument):
+        batch.run_batch([c])
+    os.environ["EV_AUTOTUNE_CACHE"] = str(tmp_path / "tune.txt")
+    try:
+        circs = tfim_mix(30, 8, 16, seed=5)
+        _, s1 = batch.run_batch(circs, shots=10, autotune=True)
+        assert not s1["from_cache"] and s1["tile_bits"] in (12, 13, 14)
+        _, s2 = batch.run_batch(circs, shots=10, autotune=True)
+        assert s2["from_cache"] and (s2["tile_bits"], s2["threads"]) == (s1["tile_bits"], s1["threads"])
+    finally:
+        del os.environ["EV_AUTOTUNE_CACHE"]
