@@ -5,7 +5,7 @@ The compute path is hand-written CUDA for sm_103a behind the C ABI in
 include/everett_cuda.h; this package is the host-side mirror of the
 reference's public surface (Circuit, Gate1/Gate2, Op, State, Execution, Rng).
 """
-from . import algorithms, batch, workloads
+from . import algorithms, batch, serve, workloads
 from ._native import device_count
 from .backend import CudaStateVectorBackend, Execution, State
 from .circuit import Apply1, Apply2, Circuit, Controlled, IfClassic, Measure
@@ -15,7 +15,7 @@ from .gate import Gate1, Gate2
 from .rng import Rng
 
 __all__ = [
-    "algorithms", "batch", "workloads", "device_count", "CudaStateVectorBackend", "Execution", "State",
+    "algorithms", "batch", "serve", "workloads", "device_count", "CudaStateVectorBackend", "Execution", "State",
     "Apply1", "Apply2", "Circuit", "Controlled", "IfClassic", "Measure", "ClassicalBitOutOfRange",
     "DimensionMismatch", "DuplicateQubit", "EverettError", "QubitOutOfRange", "Gate1", "Gate2",
     "Rng",

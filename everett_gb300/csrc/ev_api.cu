@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "ev_device.cuh"
@@ -35,6 +36,25 @@ int fail(int code, const char* fmt, ...) {
   return code;
 }
 void clear_error() { g_err[0] = 0; }
+
+int prepare_smem_kernel(const void* func) {
+  static std::mutex mu;
+  static std::vector<const void*> done;
+  std::lock_guard<std::mutex> lock(mu);
+  for (const void* f : done)
+    if (f == func) return EV_OK;
+  int dev = 0, optin = 0;
+  EV_CUDA(cudaGetDevice(&dev));
+  EV_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa{};
+  EV_CUDA(cudaFuncGetAttributes(&fa, func));
+  EV_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               optin - int(fa.sharedSizeBytes)));
+  EV_CUDA(cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               int(cudaSharedmemCarveoutMaxShared)));
+  done.push_back(func);
+  return EV_OK;
+}
 
 bool debug_enabled() {
   static const bool on = [] {
@@ -179,16 +199,33 @@ static int validate(const ev_circuit* c) {
 // ---- run --------------------------------------------------------------
 
 // Device buffers of one run: classical register, uniforms, nested-IF bits.
+// Stream-ordered allocations: no device-wide synchronisation, so runs on
+// different states overlap.
 struct RunBuffers {
+  cudaStream_t stream = nullptr;
   uint8_t* classical = nullptr;
   double* uniforms = nullptr;
   uint64_t* ifbits = nullptr;
   ~RunBuffers() {
-    if (classical) cudaFree(classical);
-    if (uniforms) cudaFree(uniforms);
-    if (ifbits) cudaFree(ifbits);
+    if (classical) cudaFreeAsync(classical, stream);
+    if (uniforms) cudaFreeAsync(uniforms, stream);
+    if (ifbits) cudaFreeAsync(ifbits, stream);
   }
 };
+
+// Keeps freed stream-ordered memory in the device pool instead of returning
+// it to the driver at every synchronisation.
+void keep_pool_warm(int device) {
+  static bool done[256] = {};
+  if (device < 0 || device >= 256 || done[device]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    uint64_t threshold = ~uint64_t(0);
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+  }
+  cudaGetLastError();
+  done[device] = true;
+}
 
 int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int tile_bits,
               const uint8_t* pred, uint64_t* passes_out);
@@ -205,6 +242,7 @@ static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run
   if (mode < EV_MODE_EXACT || mode > EV_MODE_FUSED)
     return fail(EV_ERR_INVALID_ARGUMENT, "unknown run mode %d", mode);
   RunBuffers rb;
+  rb.stream = s->stream;
   // count Measure records and the nesting of IF chains
   uint64_t nmeas = 0, nif = 0;
   for (uint64_t j = 0; j < c->nops; ++j) {
@@ -212,17 +250,18 @@ static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run
     if (c->ops[j].kind == EV_OP_IF) ++nif;
   }
   const uint64_t ncl = c->num_classical ? c->num_classical : 1;
-  EV_CUDA(cudaMalloc(&rb.classical, ncl));
+  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&rb.classical), ncl, s->stream));
   EV_CUDA(cudaMemsetAsync(rb.classical, 0, ncl, s->stream));
   std::vector<double> uni(nmeas ? nmeas : 1, 0.0);
   Rng rng(seed);
   for (uint64_t j = 0; j < nmeas; ++j) uni[j] = rng.next_f64();
-  EV_CUDA(cudaMalloc(&rb.uniforms, uni.size() * sizeof(double)));
+  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&rb.uniforms), uni.size() * sizeof(double), s->stream));
   EV_CUDA(cudaMemcpyAsync(rb.uniforms, uni.data(), uni.size() * sizeof(double),
                           cudaMemcpyHostToDevice, s->stream));
   // counter[0]: uniforms consumed; counter[1]: device timeout flag
   EV_CUDA(cudaMemsetAsync(s->scratch.counter, 0, 2 * sizeof(uint32_t), s->stream));
-  if (nif) EV_CUDA(cudaMalloc(&rb.ifbits, nif * sizeof(uint64_t)));
+  if (nif)
+    EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&rb.ifbits), nif * sizeof(uint64_t), s->stream));
   // The host copy of the nested-IF bit lists must outlive the async copy.
   std::vector<uint64_t> host_ifbits(nif ? nif : 1);
   uint64_t if_used = 0;
@@ -306,6 +345,7 @@ static int create_state(uint64_t n, int32_t dtype, ev_state** out) {
   s->dtype = dtype;
   EV_CUDA(cudaGetDevice(&s->device));
   EV_CUDA(cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, s->device));
+  keep_pool_warm(s->device);
   const size_t bytes = size_t(s->len()) * s->amp_bytes();
   cudaError_t e = cudaMalloc(&s->amps, bytes);
   if (e != cudaSuccess) {

@@ -598,14 +598,10 @@ static int batch_once(const ev_batch_circuit* items, uint64_t count, int dtype, 
   k_batch_uniforms<<<unsigned((count + 127) / 128), 128, 0, A.stream>>>(args.circs, count, args.uni);
   int per_sm = 0;
   if (dtype == EV_C128) {
-    EV_CUDA(cudaFuncSetAttribute(k_batch<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    EV_CUDA(cudaFuncSetAttribute(k_batch<double2>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 int(cudaSharedmemCarveoutMaxShared)));
+    EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_batch<double2>)));
     EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<double2>, threads, smem));
   } else {
-    EV_CUDA(cudaFuncSetAttribute(k_batch<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-    EV_CUDA(cudaFuncSetAttribute(k_batch<float2>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                 int(cudaSharedmemCarveoutMaxShared)));
+    EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_batch<float2>)));
     EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<float2>, threads, smem));
   }
   if (per_sm < 1) return fail(EV_ERR_INVALID_ARGUMENT, "batch: configuration does not fit an SM");

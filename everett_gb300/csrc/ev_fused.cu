@@ -630,10 +630,7 @@ template <int KB, int VAR>
 static int launch_tc(ev_state* s, const FusedDesc* dd, const unsigned char* db, uint64_t nsteps,
                      int* derr) {
   using Sh = TcShape<KB, VAR>;
-  EV_CUDA(cudaFuncSetAttribute(k_fused_tc<KB, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               Sh::SMEM));
-  EV_CUDA(cudaFuncSetAttribute(k_fused_tc<KB, VAR>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                               int(cudaSharedmemCarveoutMaxShared)));
+  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_fused_tc<KB, VAR>)));
   // resident CTAs from the SM's shared-memory budget (dynamic + static +
   // the 1 KiB the runtime reserves per CTA)
   cudaFuncAttributes fa{};
@@ -665,9 +662,7 @@ template <int KB>
 static int launch_fp32(ev_state* s, const FusedDesc* dd, const float2* du, uint64_t nsteps) {
   constexpr int D = 1 << KB;
   const int smem = int(sizeof(float2)) * (kRows * D + D * D);
-  EV_CUDA(cudaFuncSetAttribute(k_fused_fp32<KB>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  EV_CUDA(cudaFuncSetAttribute(k_fused_fp32<KB>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                               int(cudaSharedmemCarveoutMaxShared)));
+  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_fused_fp32<KB>)));
   uint64_t grid = uint64_t(s->num_sms) * 2;
   if (grid > nsteps) grid = nsteps;
   k_fused_fp32<KB><<<unsigned(grid), 256, smem, s->stream>>>(static_cast<float2*>(s->amps), dd, du);

@@ -14,6 +14,11 @@ namespace ev {
 int fail(int code, const char* fmt, ...);
 // Clears the thread's last error.
 void clear_error();
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in
+// maximum and prefers the max-shared carveout, once per kernel.  Launches
+// then pass their own (smaller) sizes; setting the limit per launch would
+// race between host threads launching the same kernel with different sizes.
+int prepare_smem_kernel(const void* func);
 // True when EV_DEBUG is set in the environment (launch configurations are
 // then printed to stderr).
 bool debug_enabled();

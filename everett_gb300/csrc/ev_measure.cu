@@ -328,11 +328,11 @@ int reduce_norm(const ev_state* s, double* out_host) {
 static int ensure_mass(ev_state* s) {
   const uint64_t need = s->len() - 1;
   if (s->mass && s->mass_len >= need) return EV_OK;
-  if (s->mass) cudaFree(s->mass);
+  if (s->mass) cudaFreeAsync(s->mass, s->stream);
   s->mass = nullptr;
   s->mass_len = 0;
   void* p = nullptr;
-  EV_CUDA(cudaMalloc(&p, need * sizeof(double)));
+  EV_CUDA(cudaMallocAsync(&p, need * sizeof(double), s->stream));
   s->mass = static_cast<double*>(p);
   s->mass_len = need;
   return EV_OK;
@@ -500,11 +500,11 @@ extern "C" int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* o
   for (uint64_t j = 0; j < nu; ++j) uni[j] = rng.next_f64();
   void* du = nullptr;
   void* dout = nullptr;
-  EV_CUDA(cudaMalloc(&du, nu * sizeof(double)));
+  EV_CUDA(cudaMallocAsync(&du, nu * sizeof(double), s->stream));
   int rc = EV_OK;
-  if (cudaMalloc(&dout, shots * sizeof(uint64_t)) != cudaSuccess) {
+  if (cudaMallocAsync(&dout, shots * sizeof(uint64_t), s->stream) != cudaSuccess) {
     cudaGetLastError();
-    cudaFree(du);
+    cudaFreeAsync(du, s->stream);
     return fail(EV_ERR_OOM, "ev_sample: cannot allocate %llu shots", (unsigned long long)shots);
   }
   cudaError_t e = cudaMemcpyAsync(du, uni.data(), nu * sizeof(double), cudaMemcpyHostToDevice,
@@ -526,8 +526,8 @@ extern "C" int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* o
     e = cudaMemcpyAsync(out, dout, shots * sizeof(uint64_t), cudaMemcpyDeviceToHost, s->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) rc = fail(EV_ERR_CUDA, "ev_sample: %s", cudaGetErrorString(e));
-  cudaFree(du);
-  cudaFree(dout);
+  cudaFreeAsync(du, s->stream);
+  cudaFreeAsync(dout, s->stream);
   return rc;
 }
 

@@ -83,9 +83,7 @@ static int launch_tile(ev_state* s, uint64_t ntiles, const TilePlan& plan, const
   const size_t ops_at = (sizeof(V) * (size_t(1) << plan.k) +
                          sizeof(uint64_t) * (size_t(1) << (plan.k - plan.L)) + 15) & ~size_t(15);
   const size_t smem = ops_at + sizeof(TileOp) * size_t(nops) + 64;
-  EV_CUDA(cudaFuncSetAttribute(k_tile<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
-  EV_CUDA(cudaFuncSetAttribute(k_tile<V>, cudaFuncAttributePreferredSharedMemoryCarveout,
-                               int(cudaSharedmemCarveoutMaxShared)));
+  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_tile<V>)));
   int per_sm = 0;
   EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<V>, kTileThreads, smem));
   if (per_sm < 1) per_sm = 1;
@@ -105,7 +103,8 @@ int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, i
               const uint8_t* pred, uint64_t* passes_out) {
   const int n = int(s->n);
   int k = tile_bits > 0 ? tile_bits : default_tile_bits(s->dtype);
-  if (k > 14) k = 14;
+  const int kcap = s->dtype == EV_C128 ? 13 : 14;  // tile + records within 227 KiB
+  if (k > kcap) k = kcap;
   if (k < 2) k = 2;
   if (k > n) k = n;
   const int L = std::min(k, 4);

@@ -235,3 +235,59 @@ def tfim_raw(rng: Rng, nmin: int = 8, nmax: int = 20, smin: int = 10, smax: int 
         r["q0"] = i
         r["m"][:8] = Gate1.rx(2.0 * h[i] * dt).as_f64()
     return RawCircuit(n, np.tile(step, steps))
+
+
+def random_layers_raw(n: int, depth: int, seed: int = 1) -> RawCircuit:
+    """random_layers with the same draws and matrices, as op records."""
+    from . import _native as N
+    rng = Rng.seed_from_u64(seed)
+    recs = []
+    for layer in range(depth):
+        for q in range(n):
+            for ctor in (Gate1.rz, Gate1.ry, Gate1.rz):
+                r = np.zeros((), dtype=N.OP_DTYPE)
+                r["kind"] = N.OP_APPLY1
+                r["q0"] = q
+                r["m"][:8] = ctor(math.tau * rng.next_f64()).as_f64()
+                recs.append(r)
+        for i in range(0 if layer % 2 == 0 else 1, n - 1, 2):
+            r = np.zeros((), dtype=N.OP_DTYPE)
+            r["kind"] = N.OP_APPLY2
+            r["q0"], r["q1"] = i, i + 1
+            r["m"][:] = Gate2.cnot().as_f64()
+            recs.append(r)
+    return RawCircuit(n, np.array(recs, dtype=N.OP_DTYPE))
+
+
+def serve_request(rng: Rng, nmin: int = 10, nmax: int = 26):
+    """One request of the serving mix: n ~ U{nmin..nmax}; 40% random layers
+    at depth 2n, 20% QFT of a random basis state, 20% GHZ with a mid-circuit
+    measurement of qubit 0 and an X on the last qubit if it read 1, 20%
+    TFIM Trotter (steps 10..50).  Returns (kind, circuit)."""
+    n = nmin + int(rng.next_u64() % (nmax - nmin + 1))
+    u = rng.next_f64()
+    if u < 0.4:
+        return "random", random_layers_raw(n, 2 * n, seed=rng.next_u64())
+    if u < 0.6:
+        return "qft", qft_on_basis(n, int(rng.next_u64() % (1 << n)))
+    if u < 0.8:
+        return "ghz_measure", ghz_midmeasure(n)
+    J = [0.5 + rng.next_f64() for _ in range(n - 1)]
+    h = [0.5 + rng.next_f64() for _ in range(n)]
+    steps = 10 + int(rng.next_u64() % 41)
+    return "tfim", _tfim_raw_from(n, J, h, 0.05, steps)
+
+
+def _tfim_raw_from(n, J, h, dt, steps) -> RawCircuit:
+    from . import _native as N
+    step = np.zeros(2 * n - 1, dtype=N.OP_DTYPE)
+    for i in range(n - 1):
+        step[i]["kind"] = N.OP_APPLY2
+        step[i]["q0"], step[i]["q1"] = i, i + 1
+        step[i]["m"][:] = Gate2.rzz(2.0 * J[i] * dt).as_f64()
+    for i in range(n):
+        r = step[n - 1 + i]
+        r["kind"] = N.OP_APPLY1
+        r["q0"] = i
+        r["m"][:8] = Gate1.rx(2.0 * h[i] * dt).as_f64()
+    return RawCircuit(n, np.tile(step, steps))

@@ -245,6 +245,60 @@ typedef struct ev_batch_stats {
 int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const ev_batch_options* opts,
                  ev_batch_stats* stats);
 
+/* ---- serving (no reference counterpart) ------------------------------------
+ * A continuous-batching request loop.  Requests are admitted in arrival
+ * order while the state memory of admitted requests (2^n x 16 or 8 bytes)
+ * stays within the budget; admitted requests run concurrently on separate
+ * streams, and small gate-only requests admitted together share one batched
+ * launch.  Mid-circuit measurement and classical control stay on the device.
+ * A request's result does not depend on what else is in flight. */
+typedef struct ev_server ev_server;
+
+typedef struct ev_server_options {
+  int32_t dtype;        /* EV_C64 (default) or EV_C128                     */
+  int32_t workers;      /* requests (or batches) in flight; 0 = 8          */
+  int32_t mode;         /* EV_MODE_* of single-request runs                */
+  int32_t variant;      /* EV_FUSED_* when mode is EV_MODE_FUSED           */
+  uint64_t hbm_budget;  /* state bytes admitted at once; 0 = 80% of free   */
+  int32_t batch_small;  /* 1: gate-only requests of <= batch_qubits qubits
+                           run through batched launches                    */
+  int32_t batch_qubits; /* 0 = 13 (complex64) / 12 (complex128)            */
+  int32_t start_paused; /* 1: admit nothing until ev_server_resume         */
+  int32_t reserved;
+} ev_server_options;
+
+typedef struct ev_server_result {
+  uint64_t id;
+  int32_t status;        /* EV_OK, EV_ERR_ADMISSION, EV_ERR_CANCELLED, ... */
+  int32_t num_classical;
+  uint64_t shots;        /* shots written to the submit-time buffer        */
+  double queue_ms;       /* submit -> admitted                             */
+  double latency_ms;     /* submit -> result ready                         */
+  uint8_t classical[64]; /* first 64 classical bits                        */
+} ev_server_result;
+
+typedef struct ev_server_stats {
+  uint64_t submitted, admitted, completed, failed, refused, cancelled;
+  uint64_t running, pending, batched_launches, batched_requests;
+  uint64_t reserved_bytes, budget_bytes;
+} ev_server_stats;
+
+int ev_server_create(const ev_server_options* opts, ev_server** out);
+/* Copies the circuit; shots_out (shots entries) must stay valid until the
+ * request's result has been polled.  A request whose state can never fit the
+ * budget completes at once with EV_ERR_ADMISSION. */
+int ev_server_submit(ev_server* s, const ev_circuit* c, uint64_t seed, uint64_t shots,
+                     uint64_t* shots_out, uint64_t* id);
+/* Cancels a request that has not been admitted yet. */
+int ev_server_cancel(ev_server* s, uint64_t id);
+/* Moves up to max finished results to out; waits up to wait_ms for one. */
+int ev_server_poll(ev_server* s, ev_server_result* out, int32_t max, int32_t* count,
+                   int32_t wait_ms);
+int ev_server_resume(ev_server* s);
+int ev_server_stats_get(ev_server* s, ev_server_stats* out);
+/* Runs every admitted and pending request to completion, then frees. */
+int ev_server_destroy(ev_server* s);
+
 /* ---- measurement hooks (no reference counterpart) ------------------------
  * Used by benchmarks and profilers: events on the state's stream, the number
  * of kernels the engine has launched for a state, per-kernel-class timing
