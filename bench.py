@@ -1,34 +1,45 @@
 #!/usr/bin/env python3
-"""Benchmark: gate-pass throughput of the statevector engine on one GB300.
+"""Benchmark of the statevector engine on one GB300.
 
-Workload: the seeded random-layer circuit at 30 qubits, depth 20 (1800
-single-qubit rotations Rz-Ry-Rz on every qubit per layer, 290 CNOTs in
-alternating bricks) on the plain complex128 path, state resident in HBM.
-A step is one full run of the circuit from |0...0>.
+Headline (value): the seeded random-layer circuit at 30 qubits, depth 20
+(Rz-Ry-Rz on every qubit per layer, CNOT bricks; 1800 rotations, 290
+CNOTs) on the plain complex128 path (tiled mode: bit-identical to the
+reference's arithmetic), state resident in HBM.  A step is one full run of
+the circuit from |0...0>.
 
-value   = sum over ops of the algorithmic bytes 2 * N_t * 16 (the bytes a
-          gate-by-gate run must move) / device time of the step, in GB/s
-e2e     = the same bytes / host wall time of a step through the C ABI:
-          op records copied in from pinned host memory, run, and the full
-          final state copied back to pinned host memory
-roofline: the shared-memory tile pass (the dominant kernel), its algorithmic
-          bytes per launch (one read and one write of the 2^n amplitudes)
-          over its live event-timed launch duration, against the measured HBM
-          copy bandwidth
-cpu_baseline: the CPU oracle (the reference's scalar loops restated in C++,
-          one core) on a bounded prefix of the same circuit family at 24
-          qubits, same unit
---impl reference: the same oracle with its independent loops split over
-          every host core, each step a bounded prefix at 26 qubits.
+  value         sum over ops of the algorithmic bytes 2 * N_t * 16 (what a
+                gate-by-gate run must move) / device time of a step, GB/s
+  e2e           the same bytes / host wall time of a step through the C ABI:
+                op records copied in from pinned host memory, the run, and
+                the full final state copied back to pinned host memory
+  roofline      the shared-memory tile pass (dominant kernel): one read and
+                one write of the 2^n amplitudes per launch over its live
+                event-timed launch duration, against the measured HBM copy
+                bandwidth (the pass is bound by the FP64 pipe instead; the
+                committed ncu summary gives its FP64 utilisation)
+  cpu_baseline  the CPU oracle (the reference's scalar loops restated in
+                C++) on one host core over a bounded prefix of the same
+                circuit family at 24 qubits, same unit
 
-With torchrun (N>1) every rank runs an independent replica on its own GPU
-(the path does not shard); value is the sum over ranks' work over the
-slowest rank's time.
+Additional measured sections (same run, rank 0): the complex64 fused
+tensor-core path on the same 30-qubit circuit (time, speed-up over
+complex128, fidelity against the complex128 state), the 30-qubit QFT,
+the 28-qubit Haar/CZ depth-40 circuit per fused arithmetic, the 4096-circuit
+TFIM batch, and the serving mix under Poisson arrivals.
+
+--impl reference times the same oracle with its independent loops split over
+every host core, each step a bounded prefix at 26 qubits.
+
+Under torchrun (N>1) every rank runs an independent replica on its own GPU
+(the path does not shard); value is the ranks' summed work over the slowest
+rank's time.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -46,7 +57,7 @@ METRIC = "30q gate GB/s (% HBM peak); batched circuits/s + p99 at fidelity>=1-1e
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=2)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--qubits", type=int, default=30)
@@ -54,6 +65,12 @@ def parse_args():
     ap.add_argument("--mode", default="tiled", choices=["tiled", "exact"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--case", default="headline",
+                    choices=["headline", "fused", "tiled64", "batch", "serve"],
+                    help="run one section alone (for profiling): the complex64 fused or tiled "
+                         "path on the random-layer circuit, the TFIM batch, or the serving mix")
+    ap.add_argument("--variant", default="bf16x3", choices=["bf16x3", "tf32x3", "fp32"])
     return ap.parse_args()
 
 
@@ -90,13 +107,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(kernel: str):
-    """DRAM bytes per launch from a committed ncu summary, if one exists."""
-    p = ROOT / "profiles" / f"{kernel}.txt"
+def ncu_figure(name: str, key: str):
+    """A number from a committed ncu summary (profiles/<name>.txt)."""
+    p = ROOT / "profiles" / f"{name}.txt"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("traffic_bytes_per_launch_full_size:"):
+        if line.startswith(key + ":"):
             return float(line.split(":", 1)[1])
     return None
 
@@ -168,7 +185,6 @@ def cpu_oracle_rate(n: int, depth: int, seconds: float, parallel: bool):
     done = 0
     nbytes = 0
     t0 = time.perf_counter()
-    # per-op calls through the run loop of the oracle (ops [done, done+1))
     while done < len(ops) and time.perf_counter() - t0 < seconds:
         O.apply_ops(c, amps, done, done + 1, parallel=parallel)
         nbytes += workloads.op_bytes(ops[done], n, 16)
@@ -207,14 +223,182 @@ def run_reference(args, dist: Dist):
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args, dist: Dist):
-    import ctypes as C
+class Stat(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("ms", C.c_double),
+                ("bytes", C.c_double)]
 
+
+def read_profile(L, h):
+    arr = (Stat * 16)()
+    cnt = C.c_int32()
+    L.ev_state_profile_read(h, arr, 16, C.byref(cnt))
+    out = {}
+    for i in range(min(cnt.value, 16)):
+        s = arr[i]
+        out[s.name.decode()] = {"launches": int(s.launches), "ms": round(s.ms, 3),
+                                "bytes": s.bytes}
+    return out
+
+
+def timed_runs(L, N, state, circuit, reps, **kw):
+    """Device ms per run (events on the state's stream) and the per-kernel
+    profile of the timed runs."""
+    from everett_gb300 import CudaStateVectorBackend
+    h = state.handle
+    N.check(L.ev_state_profile(h, 1))
+    N.check(L.ev_state_record_event(h, 0))
+    for _ in range(reps):
+        CudaStateVectorBackend.run_into(state, circuit, 0, **kw)
+    N.check(L.ev_state_record_event(h, 1))
+    ms = C.c_float()
+    N.check(L.ev_state_elapsed_ms(h, 0, 1, C.byref(ms)))
+    prof = read_profile(L, h)
+    N.check(L.ev_state_profile(h, 0))
+    return ms.value / reps, prof
+
+
+def fidelity(a, b) -> float:
+    ov = a.overlap(b)
+    return abs(ov) ** 2 / (a.norm_sqr() * b.norm_sqr())
+
+
+def roofline_of(prof, name, per_launch_bytes, peak, peak_kind, kernel, traffic):
+    k = prof.get(name)
+    if not k or not k["launches"]:
+        return None
+    avg_ms = k["ms"] / k["launches"]
+    achieved = per_launch_bytes / (avg_ms / 1000) / 1e9
+    return {"kernel": kernel, "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": f"{peak_kind} hbm_gbs",
+            "traffic": traffic, "launches": k["launches"], "avg_launch_ms": round(avg_ms, 3),
+            "algorithmic_bytes_per_launch": per_launch_bytes}
+
+
+def extras_c64(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, peak_kind):
+    from everett_gb300 import State
+    n = circuit.num_qubits()
+    st = State.zero(n, "complex64")
+    out = {}
+    for variant in ("bf16x3", "tf32x3"):
+        kw = dict(mode="fused", variant=variant, tile_bits=5)
+        timed_runs(L, N, st, circuit, 1, **kw)
+        ms, prof = timed_runs(L, N, st, circuit, 3, **kw)
+        out[variant] = {
+            "ms_per_run": round(ms, 2), "speedup_vs_complex128": round(c128_ms / ms, 1),
+            "gate_GBps_complex128_equivalent": round(bytes_per_step / (ms / 1e3) / 1e9, 1),
+            "fidelity_vs_complex128": fidelity(ref_state, st),
+            "roofline": roofline_of(prof, "fused_unitary", 2.0 * (1 << n) * 8, peak, peak_kind,
+                                    f"k_fused_tc<5,{variant}> (fused 5-qubit unitary, tcgen05)",
+                                    ncu_figure("k_fused_tc_bf16x3", "traffic_bytes_per_launch_full_size")
+                                    if variant == "bf16x3" else None)}
+    del st
+    return out
+
+
+def extras_qft(L, N, n, peak):
     import numpy as np
 
-    from everett_gb300 import CudaStateVectorBackend, State, _native, build, workloads
+    from everett_gb300 import State, workloads
+    j = 0x2A5A5A5A & ((1 << n) - 1)
+    c = workloads.qft_on_basis(n, j)
+    st = State.zero(n, "complex128")
+    timed_runs(L, N, st, c, 1, mode="tiled")
+    ms, prof = timed_runs(L, N, st, c, 2, mode="tiled")
+    rng = np.random.default_rng(1)
+    idx = rng.integers(0, 1 << n, size=2048)
+    err = 0.0
+    for k in idx:
+        k = int(k)
+        ph = (j * k) & ((1 << n) - 1)
+        ang = math.tau * ph / float(1 << n)
+        want = complex(math.cos(ang), math.sin(ang)) / math.sqrt(1 << n)
+        err = max(err, abs(st.amplitude(k) - want))
+    gb = workloads.gate_bytes(c, 16)
+    return {"workload": f"QFT of basis state {j} on {n} qubits, complex128 tiled",
+            "ops": len(c), "ms_per_run": round(ms, 2),
+            "gate_GBps": round(gb / (ms / 1e3) / 1e9, 1),
+            "max_abs_err_vs_closed_form_2048_sampled": err,
+            "passes": prof.get("tile_pass", {}).get("launches", 0) // 2}
+
+
+def extras_haar(L, N):
+    from everett_gb300 import State, workloads
+    n, depth = 28, 40
+    c = workloads.haar_layers(n, depth, seed=3)
+    ref = State.zero(n, "complex128")
+    ms128, _ = timed_runs(L, N, ref, c, 1, mode="tiled")
+    st = State.zero(n, "complex64")
+    out = {"workload": "Haar 1q on every qubit + CZ bricks, 28 qubits, depth 40 (1120 + 540 ops)",
+           "complex128_tiled_ms": round(ms128, 1), "fusion_qubits": 5}
+    for variant in ("bf16x3", "tf32x3", "fp32"):
+        kw = dict(mode="fused", variant=variant, tile_bits=5)
+        timed_runs(L, N, st, c, 1, **kw)
+        ms, prof = timed_runs(L, N, st, c, 2, **kw)
+        out[variant] = {"ms_per_run": round(ms, 1), "speedup_vs_complex128": round(ms128 / ms, 1),
+                        "fidelity_vs_complex128": fidelity(ref, st),
+                        "blocks": prof.get("fused_unitary", {}).get("launches", 0) // 2}
+    return out
+
+
+def extras_batch():
+    from everett_gb300 import Rng, State, CudaStateVectorBackend, batch, workloads
+    rng = Rng.seed_from_u64(2024)
+    cs = [workloads.tfim_raw(rng) for _ in range(4096)]
+    batch.run_batch(cs[:64], shots=1000, tile_bits=13, threads=256)
+    t0 = time.perf_counter()
+    res, st = batch.run_batch(cs, shots=1000, tile_bits=13, threads=256)
+    wall = time.perf_counter() - t0
+    sample = cs[::16]
+    states = {}
+    t0 = time.perf_counter()
+    for c in sample:
+        n = c.num_qubits()
+        if n not in states:
+            states[n] = State.zero(n, "complex64")
+        s = states[n]
+        CudaStateVectorBackend.run_into(s, c, 0, mode="tiled")
+        s.bloch_vector(0)
+        s.sample(1000, seed=1)
+    base = len(sample) / (time.perf_counter() - t0)
+    return {"workload": "4096 TFIM Trotter circuits, 8-20 qubits, 10-50 steps, complex64, "
+                        "<Z_0> + 1000 shots each", "circuits_per_s": round(4096 / wall, 1),
+            "wall_s": round(wall, 3), "device_ms": round(st["device_ms"], 1),
+            "one_run_per_circuit_circuits_per_s": round(base, 1),
+            "speedup": round(4096 / wall / base, 1), "queue_items": st["items"],
+            "tile_bits": st["tile_bits"], "threads": st["threads"]}
+
+
+def extras_serve():
+    from everett_gb300 import Rng, serve, workloads
+    rng = Rng.seed_from_u64(42)
+    reqs = [workloads.serve_request(rng, 10, 26) for _ in range(160)]
+    requests = [(c, i, 1000) for i, (_, c) in enumerate(reqs)]
+    srv = serve.Server(dtype="complex64", workers=8, mode="fused")
+    srv.run_all(requests[:16])
+    srv.close()
+    srv = serve.Server(dtype="complex64", workers=1, mode="fused", batch_small=False)
+    res, wall = serve.poisson_run(srv, requests, rate=1e6)
+    srv.close()
+    serial = serve.latency_summary(res, wall)
+    out = {"workload": "Poisson mix, 10-26 qubits: 40% random layers depth 2n, 20% QFT, "
+                       "20% GHZ + mid-circuit measurement + classical control, 20% TFIM; "
+                       "1000 shots each; complex64 fused BF16x3",
+           "serial_one_request_at_a_time": serial}
+    for rate in (50.0, 1e6):
+        srv = serve.Server(dtype="complex64", workers=8, mode="fused")
+        res, wall = serve.poisson_run(srv, requests, rate=rate, seed=int(rate) % 1000)
+        srv.close()
+        key = "saturated_all_at_once" if rate > 1e5 else f"poisson_{int(rate)}_per_s"
+        out[key] = serve.latency_summary(res, wall)
+    return out
+
+
+def run_ours(args, dist: Dist):
+    import numpy as np
+
+    from everett_gb300 import CudaStateVectorBackend, State, _native as N, build, workloads
     build.build()
-    L = _native.lib()
+    L = N.lib()
     n, depth = args.qubits, args.depth
     circuit = workloads.random_layers(n, depth, seed=1)
     bytes_per_step = workloads.gate_bytes(circuit, 16)
@@ -230,20 +414,20 @@ def run_ours(args, dist: Dist):
     dist.barrier()
     lc0 = C.c_uint64()
     L.ev_state_launch_count(h, C.byref(lc0))
-    _native.check(L.ev_state_profile(h, 1))
+    N.check(L.ev_state_profile(h, 1))
     gpu_index = int(os.environ.get("LOCAL_RANK", 0))
     with Clocks(gpu_index if dist.world == 1 else 0) as clk:
-        _native.check(L.ev_state_record_event(h, 0))
+        N.check(L.ev_state_record_event(h, 0))
         for _ in range(args.steps):
             step()
-        _native.check(L.ev_state_record_event(h, 1))
+        N.check(L.ev_state_record_event(h, 1))
         ms = C.c_float()
-        _native.check(L.ev_state_elapsed_ms(h, 0, 1, C.byref(ms)))
+        N.check(L.ev_state_elapsed_ms(h, 0, 1, C.byref(ms)))
     total_ms = ms.value
     lc1 = C.c_uint64()
     L.ev_state_launch_count(h, C.byref(lc1))
     prof = read_profile(L, h)
-    _native.check(L.ev_state_profile(h, 0))
+    N.check(L.ev_state_profile(h, 0))
     dist.barrier()
     worst_ms = dist.max(total_ms)
     value = dist.world * bytes_per_step * args.steps / (worst_ms / 1000) / 1e9
@@ -253,21 +437,20 @@ def run_ours(args, dist: Dist):
     if not args.no_e2e:
         ops, ctrl, npool = circuit.to_ev()
         pinned_ops = C.c_void_p()
-        _native.check(L.ev_host_alloc(ops.nbytes, C.byref(pinned_ops)))
+        N.check(L.ev_host_alloc(ops.nbytes, C.byref(pinned_ops)))
         out = C.c_void_p()
         out_bytes = (1 << n) * 16
-        _native.check(L.ev_host_alloc(out_bytes, C.byref(out)))
+        N.check(L.ev_host_alloc(out_bytes, C.byref(out)))
         C.memmove(pinned_ops, ops.ctypes.data, ops.nbytes)
-        circ = _native.EvCircuit(n, 0, pinned_ops.value, len(ops), ctrl.ctypes.data, npool)
-        opts = _native.EvRunOptions(_native.C128, 1 if args.mode == "tiled" else 0, 0, 0)
+        circ = N.EvCircuit(n, 0, pinned_ops.value, len(ops), ctrl.ctypes.data, npool)
+        opts = N.EvRunOptions(N.C128, 1 if args.mode == "tiled" else 0, 0, 0)
         cl = np.zeros(1, dtype=np.uint8)
         dist.barrier()
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            _native.check(L.ev_state_run(h, C.byref(circ), 0, C.byref(opts), cl.ctypes.data))
-            _native.check(L.ev_state_download(h, out, 1 << n))
-        e2e_s = time.perf_counter() - t0
-        e2e_s = dist.max(e2e_s)
+            N.check(L.ev_state_run(h, C.byref(circ), 0, C.byref(opts), cl.ctypes.data))
+            N.check(L.ev_state_download(h, out, 1 << n))
+        e2e_s = dist.max(time.perf_counter() - t0)
         L.ev_host_free(pinned_ops)
         L.ev_host_free(out)
         e2e = {"value": round(dist.world * bytes_per_step * args.steps / e2e_s / 1e9, 2),
@@ -275,26 +458,34 @@ def run_ours(args, dist: Dist):
                "d2h_bytes_per_step": int(out_bytes)}
 
     peak, peak_kind = measured_peaks()
-    tile = prof.get("tile_pass")
-    roofline = None
-    if tile and tile["launches"]:
-        per_launch_bytes = 2.0 * (1 << n) * 16
-        avg_ms = tile["ms"] / tile["launches"]
-        achieved = per_launch_bytes / (avg_ms / 1000) / 1e9
-        roofline = {"kernel": "k_tile<double2> (shared-memory tile pass, complex128)",
-                    "bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
-                    "unit": "GB/s", "frac": round(achieved / peak, 4),
-                    "peak_source": f"{peak_kind} hbm_gbs",
-                    "traffic": ncu_traffic("k_tile_c128"),
-                    "launches": tile["launches"], "avg_launch_ms": round(avg_ms, 3),
-                    "algorithmic_bytes_per_launch": per_launch_bytes}
+    roofline = roofline_of(prof, "tile_pass", 2.0 * (1 << n) * 16, peak, peak_kind,
+                           "k_tile<double2> (shared-memory tile pass, complex128)",
+                           ncu_figure("k_tile_c128", "traffic_bytes_per_launch_full_size"))
+    if roofline is not None:
+        roofline["note"] = ("compute-bound on the FP64 pipe (GB300 issues FP64 at 1/64 of the "
+                            "FP32 rate); ncu: fp64 pipe busy "
+                            f"{ncu_figure('k_tile_c128', 'fp64_pipe_pct')}% in rotation passes")
 
     cpu = None
+    extras = {}
     if dist.rank == 0:
         rate, ops_done, dt = cpu_oracle_rate(min(n, 24), depth, args.cpu_seconds, parallel=False)
         cpu = {"value": round(rate, 3), "unit": "GB/s", "cores": 1, "kind": "port",
                "sample": f"first {ops_done} ops of the random-layer circuit at {min(n, 24)} "
                          f"qubits, {dt:.1f} s, scalar oracle (the reference's loops)"}
+        if not args.no_extras:
+            c128_ms = worst_ms / args.steps
+            for key, fn in (("complex64_fused_same_circuit",
+                             lambda: extras_c64(L, N, state, circuit, c128_ms, bytes_per_step,
+                                                peak, peak_kind)),
+                            ("qft", lambda: extras_qft(L, N, n, peak)),
+                            ("haar28_depth40", lambda: extras_haar(L, N)),
+                            ("batch_tfim4096", extras_batch),
+                            ("serve_mix", extras_serve)):
+                try:
+                    extras[key] = fn()
+                except Exception as exc:  # report, do not hide
+                    extras[key] = {"error": f"{type(exc).__name__}: {exc}"}
 
     if dist.rank == 0:
         line = {
@@ -314,29 +505,34 @@ def run_ours(args, dist: Dist):
             "gpu_launches": int(lc1.value - lc0.value),
             "clocks": clk.summary(),
             "kernel_profile": prof,
+            "extras": extras,
         }
         print(json.dumps(line), flush=True)
 
 
-def read_profile(L, h):
-    import ctypes as C
-
-    class Stat(C.Structure):
-        _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("ms", C.c_double),
-                    ("bytes", C.c_double)]
-    arr = (Stat * 16)()
-    cnt = C.c_int32()
-    L.ev_state_profile_read(h, arr, 16, C.byref(cnt))
-    out = {}
-    for i in range(min(cnt.value, 16)):
-        s = arr[i]
-        out[s.name.decode()] = {"launches": int(s.launches), "ms": round(s.ms, 3),
-                                "bytes": s.bytes}
-    return out
+def run_case(args):
+    """One section alone, printing its own JSON line (a profiling target)."""
+    from everett_gb300 import State, _native as N, build, workloads
+    build.build()
+    if args.case in ("batch", "serve"):
+        print(json.dumps({"case": args.case, **(extras_batch() if args.case == "batch" else extras_serve())}))
+        return
+    L = N.lib()
+    c = workloads.random_layers(args.qubits, args.depth, seed=1)
+    st = State.zero(args.qubits, "complex64")
+    kw = dict(mode="fused", variant=args.variant, tile_bits=5) if args.case == "fused" else dict(mode="tiled")
+    for _ in range(args.warmup):
+        timed_runs(L, N, st, c, 1, **kw)
+    ms, prof = timed_runs(L, N, st, c, args.steps, **kw)
+    print(json.dumps({"case": args.case, "qubits": args.qubits, "depth": args.depth, **kw,
+                      "ms_per_run": round(ms, 3), "kernel_profile": prof}))
 
 
 def main():
     args = parse_args()
+    if args.case != "headline":
+        run_case(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", 1))
     if world > 1:
         os.environ["CUDA_VISIBLE_DEVICES"] = os.environ.get("LOCAL_RANK", "0")

@@ -76,6 +76,7 @@ _SIGS = {
     "ev_norm_sqr": [_P, _DP],
     "ev_normalize": [_P],
     "ev_probability": [_P, _U64, _DP],
+    "ev_amplitude": [_P, _U64, _P],
     "ev_overlap": [_P, _P, _P],
     "ev_fidelity": [_P, _P, _DP],
     "ev_bloch_vector": [_P, _U64, _P],

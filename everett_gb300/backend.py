@@ -106,6 +106,11 @@ class State:
         N.check(N.lib().ev_probability(self._h, basis, C.byref(out)))
         return out.value
 
+    def amplitude(self, basis: int) -> complex:
+        out = (C.c_double * 2)()
+        N.check(N.lib().ev_amplitude(self._h, basis, out))
+        return complex(out[0], out[1])
+
     def overlap(self, other: "State") -> complex:
         out = (C.c_double * 2)()
         N.check(N.lib().ev_overlap(self._h, other._h, out))

@@ -112,6 +112,35 @@ __global__ void __launch_bounds__(kRedThreads)
   if (threadIdx.x < 4) partials[blockIdx.x * 4 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
+// <other|self> for states of different amplitude types (both promoted to f64).
+template <typename VA, typename VB>
+__global__ void __launch_bounds__(kRedThreads)
+    k_overlap_mixed(const VA* __restrict__ a, const VB* __restrict__ b, uint64_t count,
+                    uint64_t chunk, double* __restrict__ partials) {
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
+  const uint64_t hi = lo + chunk < count ? lo + chunk : count;
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) {
+    const VA x = a[i];
+    const VB y = b[i];
+    const double2 r = cmul(make_double2(double(y.x), -double(y.y)), make_double2(double(x.x), double(x.y)));
+    acc[0] += r.x;
+    acc[1] += r.y;
+  }
+  __shared__ double sh[2][kRedThreads];
+  sh[0][threadIdx.x] = acc[0];
+  sh[1][threadIdx.x] = acc[1];
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 4) partials[blockIdx.x * 4 + threadIdx.x] = threadIdx.x < 2 ? sh[threadIdx.x][0] : 0.0;
+}
+
 // Sums nblocks x 4 partials in a fixed order into result[0..4).
 __global__ void __launch_bounds__(kRedThreads)
     k_finish(const double* __restrict__ partials, int nblocks, double* __restrict__ result,
@@ -438,18 +467,58 @@ extern "C" int ev_probability(const ev_state* s, uint64_t basis, double* out) {
   return EV_OK;
 }
 
+extern "C" int ev_amplitude(const ev_state* s, uint64_t basis, double out[2]) {
+  clear_error();
+  if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_amplitude: null argument");
+  if (basis >= s->len())
+    return fail(EV_ERR_INVALID_ARGUMENT, "basis state %llu out of range", (unsigned long long)basis);
+  EV_CUDA(cudaSetDevice(s->device));
+  if (s->dtype == EV_C128) {
+    EV_CUDA(cudaMemcpyAsync(out, static_cast<const double2*>(s->amps) + basis, 16,
+                            cudaMemcpyDeviceToHost, s->stream));
+    EV_CUDA(cudaStreamSynchronize(s->stream));
+  } else {
+    float v[2];
+    EV_CUDA(cudaMemcpyAsync(v, static_cast<const float2*>(s->amps) + basis, 8,
+                            cudaMemcpyDeviceToHost, s->stream));
+    EV_CUDA(cudaStreamSynchronize(s->stream));
+    out[0] = v[0];
+    out[1] = v[1];
+  }
+  return EV_OK;
+}
+
 extern "C" int ev_overlap(const ev_state* self, const ev_state* other, double out[2]) {
   clear_error();
   if (!self || !other || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_overlap: null argument");
   if (self->n != other->n)
     return fail(EV_ERR_DIMENSION_MISMATCH, "states must have equal qubit counts (%llu vs %llu)",
                 (unsigned long long)self->n, (unsigned long long)other->n);
-  if (self->dtype != other->dtype)
-    return fail(EV_ERR_INVALID_ARGUMENT, "states must have the same amplitude type");
   EV_CUDA(cudaSetDevice(self->device));
   // other's pending work must be complete before self's stream reads it
   EV_CUDA(cudaStreamSynchronize(other->stream));
-  EV_TRY(reduce<R_OVERLAP>(self, other, self->len(), 0, nullptr));
+  if (self->dtype != other->dtype) {
+    const uint64_t count = self->len();
+    const uint64_t want = (count + 4095) / 4096;
+    int nb = int(want < 1 ? 1 : want);
+    const int cap = self->num_sms * 4 < kMaxRedBlocks ? self->num_sms * 4 : kMaxRedBlocks;
+    if (nb > cap) nb = cap;
+    const uint64_t chunk = (count + nb - 1) / nb;
+    if (self->dtype == EV_C64)
+      k_overlap_mixed<float2, double2><<<nb, kRedThreads, 0, self->stream>>>(
+          static_cast<const float2*>(self->amps), static_cast<const double2*>(other->amps), count,
+          chunk, self->scratch.partials);
+    else
+      k_overlap_mixed<double2, float2><<<nb, kRedThreads, 0, self->stream>>>(
+          static_cast<const double2*>(self->amps), static_cast<const float2*>(other->amps), count,
+          chunk, self->scratch.partials);
+    k_finish<<<1, kRedThreads, 0, self->stream>>>(self->scratch.partials, nb, self->scratch.result,
+                                                 nullptr);
+    self->launches += 2;
+    EV_CUDA(cudaGetLastError());
+  } else {
+    EV_TRY(reduce<R_OVERLAP>(self, other, self->len(), 0, nullptr));
+  }
   double r[2];
   EV_TRY(fetch_result(self, r, 2));
   out[0] = r[0];

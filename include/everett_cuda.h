@@ -176,7 +176,10 @@ int ev_measure_qubit_noalloc(double* amps, uint64_t n, uint64_t k, double u,
 int ev_norm_sqr(const ev_state* s, double* out);
 int ev_normalize(ev_state* s);
 int ev_probability(const ev_state* s, uint64_t basis, double* out);
-/* <other|self> as [re, im]. */
+/* One amplitude as [re, im] (State::amplitudes()[basis], src/state.rs:81-83). */
+int ev_amplitude(const ev_state* s, uint64_t basis, double out[2]);
+/* <other|self> as [re, im]; the two states may differ in amplitude type
+ * (both are promoted to f64). */
 int ev_overlap(const ev_state* self, const ev_state* other, double out[2]);
 int ev_fidelity(const ev_state* self, const ev_state* other, double* out);
 /* [<X>, <Y>, <Z>] of one qubit (State::bloch_vector). */
