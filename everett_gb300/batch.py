@@ -23,7 +23,7 @@ class EvBatchCircuit(C.Structure):
 
 class EvBatchOptions(C.Structure):
     _fields_ = [("dtype", C.c_int32), ("tile_bits", C.c_int32), ("threads", C.c_int32),
-                ("autotune", C.c_int32)]
+                ("autotune", C.c_int32), ("test_stall", C.c_int32), ("reserved", C.c_int32)]
 
 
 class EvBatchStats(C.Structure):
@@ -40,7 +40,7 @@ class BatchResult:
 
 
 def run_batch(circuits, seeds=None, shots=1000, dtype="complex64", tile_bits=0, threads=0,
-              autotune=False, return_states=False):
+              autotune=False, return_states=False, test_stall=False):
     """Runs ``circuits`` in one batch; returns (results, stats dict)."""
     count = len(circuits)
     seeds = list(range(count)) if seeds is None else list(seeds)
@@ -62,7 +62,7 @@ def run_batch(circuits, seeds=None, shots=1000, dtype="complex64", tile_bits=0, 
         it.amps_out = am.ctypes.data if am is not None else None
         results.append((sh, ez, am))
     opts = EvBatchOptions(N.C128 if dtype in ("complex128", "c128") else N.C64, int(tile_bits),
-                          int(threads), 1 if autotune else 0)
+                          int(threads), 1 if autotune else 0, 1 if test_stall else 0, 0)
     st = EvBatchStats()
     N.check(N.lib().ev_batch_run(items, count, C.byref(opts), C.byref(st)))
     out = [BatchResult(float(ez[0]), sh[:shots[i]],

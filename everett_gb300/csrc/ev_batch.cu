@@ -61,7 +61,7 @@ struct PassRef {
   uint32_t op0, nops;
 };
 
-enum : uint32_t { BI_WHOLE = 0, BI_TILE = 1, BI_FINAL = 2 };
+enum : uint32_t { BI_WHOLE = 0, BI_TILE = 1, BI_FINAL = 2, BI_STALL = 3 };
 struct BatchItem {
   uint32_t circ, pass, tile, kind;
 };
@@ -191,7 +191,10 @@ __global__ void __launch_bounds__(512, 2) k_batch(BatchArgs a, int kmax) {
     const BatchCirc c = a.circs[it.circ];
     V* st = static_cast<V*>(a.states) + c.state;
     if (it.kind != BI_WHOLE && !(it.kind == BI_TILE && it.pass == 0)) {
-      const unsigned want = it.kind == BI_FINAL ? c.npasses * unsigned(c.ntiles) : it.pass * unsigned(c.ntiles);
+      // BI_STALL (test hook) waits for a count no item ever reaches
+      const unsigned want = it.kind == BI_STALL  ? 0xFFFFFFFFu
+                            : it.kind == BI_FINAL ? c.npasses * unsigned(c.ntiles)
+                                                  : it.pass * unsigned(c.ntiles);
       if (t == 0) {
         s_ok = wait_count(a.done + it.circ, want) ? 1 : 0;
         if (!s_ok) atomicExch(a.err, 1);
@@ -453,7 +456,7 @@ int max_tile_bits(int dtype) { return dtype == EV_C128 ? 13 : 14; }
 
 // Runs one configuration; fills stats (device_ms, host_ms, items).
 static int batch_once(const ev_batch_circuit* items, uint64_t count, int dtype, int kmax,
-                      int threads, ev_batch_stats* st) {
+                      int threads, ev_batch_stats* st, bool stall = false) {
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();
   Arena& A = g_arena;
@@ -532,6 +535,7 @@ static int batch_once(const ev_batch_circuit* items, uint64_t count, int dtype, 
   }
   for (uint32_t ci : large) q.push_back({ci, 0, 0, BI_FINAL});
   for (; si < small.size(); ++si) q.push_back({small[si], 0, 0, BI_WHOLE});
+  if (stall) q.push_back({0, 0, 0, BI_STALL});
   // meta blob: circs | items | passes | plans | ops | mats
   std::vector<PassRef> passes;
   std::vector<TilePlan> plans;
@@ -737,7 +741,8 @@ extern "C" int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const
   if (kbits < 4) kbits = 4;
   if (threads != 256 && threads != 512)
     return fail(EV_ERR_INVALID_ARGUMENT, "batch: threads must be 256 or 512");
-  const int rc = batch_once(items, count, dtype, kbits, threads, stats);
+  const int rc = batch_once(items, count, dtype, kbits, threads, stats,
+                            opts != nullptr && opts->test_stall != 0);
   if (rc == EV_OK && stats) stats->from_cache = from_cache;
   return rc;
 }

@@ -28,6 +28,7 @@
 #include <cuda_bf16.h>
 
 #include <cstdio>
+#include <cstdlib>
 
 #include <algorithm>
 #include <complex>
@@ -51,6 +52,8 @@ struct FusedDesc {
   uint8_t rlo[128], flo[128];  // local index l: low 7 bits -> (r part, f part)
   uint8_t rhi[64], fhi[64];    // high bits of l -> (r part, f part)
   uint8_t comp_hi[64];         // qubits outside T, ascending (row-step index bits)
+  uint16_t lrow[128];          // (r, f) -> local index: lrow[r] | lf[f]
+  uint16_t lf[64];
   int32_t ncomp_hi;
   int32_t k;
   int32_t lowbits;  // T holds qubits 0..lowbits-1
@@ -213,6 +216,13 @@ static void build_desc(const Block& b, int n, FusedDesc* d) {
     split(uint64_t(j) << 7, &r, &f);
     d->rhi[j] = uint8_t(r);
     d->fhi[j] = uint8_t(f);
+  }
+  // inverse maps: local bit positions of R and F inside T
+  {
+    std::vector<int> rpos, fpos;
+    for (size_t i = 0; i < T.size(); ++i) ((fmask >> T[i]) & 1 ? fpos : rpos).push_back(int(i));
+    for (int r = 0; r < kRows; ++r) d->lrow[r] = uint16_t(pdep(uint64_t(r), rpos));
+    for (int f = 0; f < (1 << k); ++f) d->lf[f] = uint16_t(pdep(uint64_t(f), fpos));
   }
   d->ncomp_hi = int(comp.size());
   for (size_t i = 0; i < comp.size(); ++i) d->comp_hi[i] = uint8_t(comp[i]);
@@ -570,6 +580,278 @@ __global__ void __launch_bounds__(kTcThreads)
   }
 }
 
+// ---- tcgen05 kernel with TMA-staged streaming -------------------------------
+//
+// The same pass as k_fused_tc, with HBM traffic moved to the bulk-copy (TMA)
+// engine.  A step's 128 x 2^k amplitudes are contiguous runs of 2^lowbits
+// amplitudes (>= 1 KiB): thread 0 issues one cp.async.bulk per run into a
+// shared-memory stage, STAGES steps ahead, completing on the stage's
+// mbarrier (expect_tx).  The warps convert the stage into the split A
+// operand, thread 0 issues the MMAs, the warps write the results back into
+// the same stage (the input is already in A), and thread 0 streams the stage
+// to HBM with bulk stores, waits until they have read it, and refills it
+// with a later step.  On a wait that gives up, the kernel records the error,
+// drains its outstanding copies (bounded), frees TMEM and returns.
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
+               "r"(smem_addr(src)), "r"(bytes)
+               : "memory");
+}
+
+template <int KB, int VAR, int STAGES>
+struct TmaShape {
+  using Sh = TcShape<KB, VAR>;
+  static constexpr int RAW = kRows * Sh::D * 8;  // one step of complex64 amplitudes
+  static constexpr int SMEM = 2 * Sh::A_BYTES + 2 * Sh::B_BYTES + STAGES * RAW + 1024;
+};
+
+constexpr int kTmaThreads = kTcThreads + 32;  // 8 compute warps + 1 producer warp
+
+__device__ __forceinline__ void compute_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kTcThreads) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+template <int KB, int VAR, int STAGES>
+__global__ void __launch_bounds__(kTmaThreads)
+    k_fused_tma(float2* __restrict__ s, const FusedDesc* __restrict__ gd,
+                const unsigned char* __restrict__ bmat, int* __restrict__ err) {
+  using Sh = TcShape<KB, VAR>;
+  using Tm = TmaShape<KB, VAR, STAGES>;
+  constexpr int D = Sh::D, K = Sh::K, ESZ = Sh::ESZ;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ FusedDesc d;
+  __shared__ __align__(8) uint64_t full_bar[STAGES];
+  __shared__ __align__(8) uint64_t empty_bar[STAGES];
+  __shared__ __align__(8) uint64_t mma_bar;
+  __shared__ uint32_t tmem_slot;
+  __shared__ volatile int s_ok;
+  unsigned char* sm = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* a_hi = sm;
+  unsigned char* a_lo = sm + Sh::A_BYTES;
+  unsigned char* b_hi = sm + 2 * Sh::A_BYTES;
+  unsigned char* b_lo = b_hi + Sh::B_BYTES;
+  unsigned char* raw0 = b_lo + Sh::B_BYTES;
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  for (int i = tid; i < int(sizeof(FusedDesc) / 8); i += blockDim.x)
+    reinterpret_cast<uint64_t*>(&d)[i] = reinterpret_cast<const uint64_t*>(gd)[i];
+  for (int e = tid; e < K * K; e += blockDim.x) {
+    const int nrow = e / K, kk = e % K;
+    const uint32_t off = sw128_off(nrow, kk, K, ESZ);
+    if constexpr (ESZ == 4) {
+      *reinterpret_cast<uint32_t*>(b_hi + off) = reinterpret_cast<const uint32_t*>(bmat)[e];
+      *reinterpret_cast<uint32_t*>(b_lo + off) = reinterpret_cast<const uint32_t*>(bmat)[K * K + e];
+    } else {
+      *reinterpret_cast<uint16_t*>(b_hi + off) = reinterpret_cast<const uint16_t*>(bmat)[e];
+      *reinterpret_cast<uint16_t*>(b_lo + off) = reinterpret_cast<const uint16_t*>(bmat)[K * K + e];
+    }
+  }
+  if (tid == 0) {
+    for (int st = 0; st < STAGES; ++st) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full_bar[st])));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&empty_bar[st])));
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mma_bar)));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    s_ok = 1;
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(&tmem_slot)),
+                 "r"(uint32_t(Sh::TMEM_COLS)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  const int nruns = (kRows * D) >> d.lowbits;
+  const uint32_t run_bytes = 8u << d.lowbits;
+  const uint64_t stride = gridDim.x;
+
+  if (warp == kTcThreads / 32) {
+    // ---- producer warp: all HBM traffic through the bulk-copy engine ----
+    if ((tid & 31) == 0) {
+      uint32_t pending = 0, ephase = 0;
+      uint32_t armed[STAGES] = {};  // loads issued into each stage so far
+      auto load = [&](uint64_t step, int st) {
+        const uint64_t base = step_base(d, step);
+        unsigned char* dst = raw0 + size_t(st) * Tm::RAW;
+        mbar_expect_tx(&full_bar[st], uint32_t(Tm::RAW));
+        for (int j = 0; j < nruns; ++j)
+          bulk_g2s(dst + size_t(j) * run_bytes, s + (base | d.hitab[j]), run_bytes, &full_bar[st]);
+        pending |= 1u << st;
+        armed[st] += 1;
+      };
+      for (int st = 0; st < STAGES; ++st) {
+        const uint64_t step = blockIdx.x + uint64_t(st) * stride;
+        if (step < d.nsteps) load(step, st);
+      }
+      uint64_t i = 0;
+      for (uint64_t step = blockIdx.x; step < d.nsteps; step += stride, ++i) {
+        const int st = int(i % STAGES);
+        // the compute warps have consumed the stage and written results into it
+        if (!mbar_wait(&empty_bar[st], (ephase >> st) & 1u, kWaitLimit) || !s_ok) {
+          atomicExch(err, 1);
+          s_ok = 0;
+          break;
+        }
+        ephase ^= 1u << st;
+        pending &= ~(1u << st);
+        const uint64_t base = step_base(d, step);
+        for (int j = 0; j < nruns; ++j)
+          bulk_s2g(s + (base | d.hitab[j]), raw0 + size_t(st) * Tm::RAW + size_t(j) * run_bytes,
+                   run_bytes);
+        asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        const uint64_t next = step + uint64_t(STAGES) * stride;
+        if (next < d.nsteps) {
+          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          load(next, st);
+        }
+      }
+      // drain: a load still in flight completes phase (armed - 1) of its
+      // barrier (bounded wait); then every bulk store
+      for (int st = 0; st < STAGES; ++st)
+        if (pending & (1u << st)) mbar_wait(&full_bar[st], (armed[st] - 1) & 1u, kWaitLimit);
+      asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    }
+  } else {
+    // ---- compute warps ----
+    const uint32_t idesc = (1u << 4) | (Elem<VAR>::fmt << 7) | (Elem<VAR>::fmt << 10) |
+                           (uint32_t(K >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
+    const int quarter = warp & 3, half = warp >> 2;
+    const int row = quarter * 32 + (tid & 31);
+    constexpr int G = D / 4;
+    constexpr int GPT = G / (kTcThreads / kRows);
+    const uint32_t rsw = uint32_t((row >> 3) * 1024 + (row & 7) * 128);
+    const uint32_t rx = uint32_t(row & 7);
+    const uint32_t lrow = d.lrow[row];
+    uint32_t fphase = 0, mphase = 0;
+    uint64_t i = 0;
+    for (uint64_t step = blockIdx.x; step < d.nsteps; step += stride, ++i) {
+      const int st = int(i % STAGES);
+      float2* raw = reinterpret_cast<float2*>(raw0 + size_t(st) * Tm::RAW);
+      if (!mbar_wait(&full_bar[st], (fphase >> st) & 1u, kWaitLimit)) {
+        atomicExch(err, 1);
+        s_ok = 0;
+      }
+      compute_sync();
+      if (!s_ok) break;
+      fphase ^= 1u << st;
+#pragma unroll
+      for (int gi = 0; gi < GPT; ++gi) {
+        const int g = half + 2 * gi;
+        float2 x[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) x[q] = raw[lrow | d.lf[4 * g + q]];
+        if constexpr (VAR == EV_FUSED_TF32X3) {
+          const uint32_t kb = uint32_t(g / 4) * kRows * 128 + rsw;
+          const uint32_t c0 = uint32_t(2 * (g % 4));
+          float hi[8], lo[8];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            hi[2 * q] = __uint_as_float(__float_as_uint(x[q].x) & 0xFFFFE000u);
+            hi[2 * q + 1] = __uint_as_float(__float_as_uint(x[q].y) & 0xFFFFE000u);
+            lo[2 * q] = x[q].x - hi[2 * q];
+            lo[2 * q + 1] = x[q].y - hi[2 * q + 1];
+          }
+          const uint32_t o0 = kb + ((c0 ^ rx) << 4), o1 = kb + (((c0 + 1) ^ rx) << 4);
+          *reinterpret_cast<float4*>(a_hi + o0) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+          *reinterpret_cast<float4*>(a_hi + o1) = make_float4(hi[4], hi[5], hi[6], hi[7]);
+          *reinterpret_cast<float4*>(a_lo + o0) = make_float4(lo[0], lo[1], lo[2], lo[3]);
+          *reinterpret_cast<float4*>(a_lo + o1) = make_float4(lo[4], lo[5], lo[6], lo[7]);
+        } else {
+          const uint32_t o = uint32_t(g / 8) * kRows * 128 + rsw + ((uint32_t(g % 8) ^ rx) << 4);
+          uint32_t hw[4], lw[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const __nv_bfloat16 hr = __float2bfloat16_rn(x[q].x), hm = __float2bfloat16_rn(x[q].y);
+            const __nv_bfloat16 lr = __float2bfloat16_rn(x[q].x - __bfloat162float(hr));
+            const __nv_bfloat16 lm = __float2bfloat16_rn(x[q].y - __bfloat162float(hm));
+            hw[q] = uint32_t(__bfloat16_as_ushort(hr)) | (uint32_t(__bfloat16_as_ushort(hm)) << 16);
+            lw[q] = uint32_t(__bfloat16_as_ushort(lr)) | (uint32_t(__bfloat16_as_ushort(lm)) << 16);
+          }
+          *reinterpret_cast<uint4*>(a_hi + o) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+          *reinterpret_cast<uint4*>(a_lo + o) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      compute_sync();
+      if (tid == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t ah = smem_addr(a_hi), al = smem_addr(a_lo);
+        const uint32_t bh = smem_addr(b_hi), bl = smem_addr(b_lo);
+        constexpr int per_row = 128 / ESZ;
+        uint32_t acc = 0;
+#pragma unroll
+        for (int kk = 0; kk < K; kk += Elem<VAR>::kstep) {
+          const int kb = kk / per_row;
+          const uint32_t kin = uint32_t((kk % per_row) * ESZ);
+          const uint32_t ao = uint32_t(kb * kRows * 128) + kin;
+          const uint32_t bo = uint32_t(kb * K * 128) + kin;
+          mma_issue<VAR>(tmem, sw128_desc(ah + ao), sw128_desc(bh + bo), idesc, acc);
+          acc = 1;
+          mma_issue<VAR>(tmem, sw128_desc(ah + ao), sw128_desc(bl + bo), idesc, 1);
+          mma_issue<VAR>(tmem, sw128_desc(al + ao), sw128_desc(bh + bo), idesc, 1);
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_addr(&mma_bar))
+            : "memory");
+      }
+      if (!mbar_wait(&mma_bar, mphase, kWaitLimit)) {
+        atomicExch(err, 1);
+        s_ok = 0;
+      }
+      compute_sync();
+      if (!s_ok) break;
+      mphase ^= 1u;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t lane_base = tmem + (uint32_t(quarter * 32) << 16);
+#pragma unroll
+      for (int c0 = half * (K / 2); c0 < (half + 1) * (K / 2); c0 += 16) {
+        uint32_t w[16];
+        tmem_ld16(lane_base + uint32_t(c0), w);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          raw[lrow | d.lf[c0 / 2 + j]] =
+              make_float2(__uint_as_float(w[2 * j]), __uint_as_float(w[2 * j + 1]));
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      compute_sync();
+      if (tid == 0) mbar_arrive(&empty_bar[st]);
+    }
+  }
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(uint32_t(Sh::TMEM_COLS)));
+  }
+}
+
 // ---- host: launch ---------------------------------------------------------------
 
 static uint32_t tf32_hi_bits(float x) {
@@ -658,6 +940,33 @@ static int launch_tc(ev_state* s, const FusedDesc* dd, const unsigned char* db, 
   return EV_OK;
 }
 
+template <int KB, int VAR, int STAGES>
+static int launch_tma(ev_state* s, const FusedDesc* dd, const unsigned char* db, uint64_t nsteps,
+                      int* derr) {
+  using Tm = TmaShape<KB, VAR, STAGES>;
+  using Sh = TcShape<KB, VAR>;
+  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_fused_tma<KB, VAR, STAGES>)));
+  cudaFuncAttributes fa{};
+  EV_CUDA(cudaFuncGetAttributes(&fa, k_fused_tma<KB, VAR, STAGES>));
+  int smem_sm = 0, regs_sm = 0;
+  EV_CUDA(cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, s->device));
+  EV_CUDA(cudaDeviceGetAttribute(&regs_sm, cudaDevAttrMaxRegistersPerMultiprocessor, s->device));
+  int per_sm = smem_sm / int(Tm::SMEM + fa.sharedSizeBytes + 1024);
+  const int by_regs = regs_sm / ((fa.numRegs + 7) / 8 * 8 * kTmaThreads);
+  if (per_sm > by_regs) per_sm = by_regs;
+  if (per_sm > 512 / Sh::TMEM_COLS) per_sm = 512 / Sh::TMEM_COLS;
+  if (per_sm < 1) per_sm = 1;
+  uint64_t grid = uint64_t(s->num_sms) * per_sm;
+  if (grid > nsteps) grid = nsteps;
+  if (debug_enabled())
+    fprintf(stderr, "[ev] k_fused_tma<%d,%d,%d> smem %d+%zu per CTA, %d CTAs/SM, grid %llu\n", KB,
+            VAR, STAGES, Tm::SMEM, size_t(fa.sharedSizeBytes), per_sm, (unsigned long long)grid);
+  k_fused_tma<KB, VAR, STAGES><<<unsigned(grid), kTmaThreads, Tm::SMEM, s->stream>>>(
+      static_cast<float2*>(s->amps), dd, db, derr);
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
 template <int KB>
 static int launch_fp32(ev_state* s, const FusedDesc* dd, const float2* du, uint64_t nsteps) {
   constexpr int D = 1 << KB;
@@ -727,6 +1036,11 @@ int fused_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, i
   EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dbuf), total, s->stream));
   EV_CUDA(cudaMemcpyAsync(dbuf, host.data(), total, cudaMemcpyHostToDevice, s->stream));
   int* derr = reinterpret_cast<int*>(s->scratch.counter + 1);
+  // Register-staged streaming (default: the faster of the two on GB300, see
+  // the measured comparison in the design notes) or the warp-specialised
+  // TMA-staged pipeline (EV_FUSED_STAGING=tma), read at every call.
+  const char* staging = getenv("EV_FUSED_STAGING");
+  const bool use_tma = staging != nullptr && std::strcmp(staging, "tma") == 0;
   int rc = EV_OK;
   for (size_t i = 0; i < blocks.size() && rc == EV_OK; ++i) {
     const FusedDesc* dd = reinterpret_cast<const FusedDesc*>(dbuf) + i;
@@ -737,9 +1051,11 @@ int fused_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, i
     const int kb = int(blocks[i].F.size());
     if (tc) {
       if (variant == EV_FUSED_TF32X3)
-        rc = launch_tc<5, EV_FUSED_TF32X3>(s, dd, dm, nsteps, derr);
+        rc = use_tma ? launch_tma<5, EV_FUSED_TF32X3, 3>(s, dd, dm, nsteps, derr)
+                     : launch_tc<5, EV_FUSED_TF32X3>(s, dd, dm, nsteps, derr);
       else if (kb == 5)
-        rc = launch_tc<5, EV_FUSED_BF16X3>(s, dd, dm, nsteps, derr);
+        rc = use_tma ? launch_tma<5, EV_FUSED_BF16X3, 3>(s, dd, dm, nsteps, derr)
+                     : launch_tc<5, EV_FUSED_BF16X3>(s, dd, dm, nsteps, derr);
       else
         rc = launch_tc<6, EV_FUSED_BF16X3>(s, dd, dm, nsteps, derr);
     } else {

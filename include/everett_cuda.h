@@ -232,6 +232,10 @@ typedef struct ev_batch_options {
   int32_t tile_bits; /* qubits per shared-memory tile; 0 = autotuned       */
   int32_t threads;   /* threads per resident CTA (256 / 512); 0 = autotuned */
   int32_t autotune;  /* 1: time candidates when no cached choice exists   */
+  int32_t test_stall; /* test hook: 1 adds a queue item whose dependency is
+                         never met, so a bounded device wait runs out and
+                         the call returns EV_ERR_TIMEOUT                  */
+  int32_t reserved;
 } ev_batch_options;
 
 typedef struct ev_batch_stats {

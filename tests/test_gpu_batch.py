@@ -12,7 +12,7 @@ import pytest
 
 import oracle as O
 from everett_gb300 import Circuit, Gate1, Rng, batch, workloads
-from everett_gb300.error import InvalidArgument
+from everett_gb300.error import DeviceTimeout, InvalidArgument
 
 pytestmark = pytest.mark.gpu
 
@@ -83,3 +83,18 @@ def test_batch_rejects_measurement_and_autotunes(gpu, tmp_path):
         assert s2["from_cache"] and (s2["tile_bits"], s2["threads"]) == (s1["tile_bits"], s1["threads"])
     finally:
         del os.environ["EV_AUTOTUNE_CACHE"]
+
+
+def test_batch_bounded_wait_reports_timeout(gpu):
+    """A queue item whose dependency is never met: the device wait gives up
+    after its bound, the call reports EV_ERR_TIMEOUT, and the context stays
+    usable for the next batch (no fault, no trap, no hang)."""
+    circs = tfim_mix(4, 3, 8, seed=1)
+    with pytest.raises(DeviceTimeout):
+        batch.run_batch(circs, shots=10, dtype="complex128", tile_bits=6, threads=256,
+                        test_stall=True)
+    res, _ = batch.run_batch(circs, shots=10, dtype="complex128", tile_bits=6, threads=256,
+                             return_states=True)
+    for c, r in zip(circs, res):
+        want, _, _ = O.run_seeded(c, 0)
+        assert np.array_equal(r.amplitudes, want)

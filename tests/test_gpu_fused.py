@@ -70,3 +70,15 @@ def test_fused_midcircuit_measurement(gpu, variant, k):
 def test_fused_small_registers_use_tile_pass(gpu):
     for n in (1, 3, 7, 11):
         check(workloads.random_layers(n, 6, seed=n), "tf32x3", 5)
+
+
+@pytest.mark.parametrize("variant", ["bf16x3", "tf32x3"])
+def test_fused_tma_staging(gpu, variant, monkeypatch):
+    """The warp-specialised TMA-staged pipeline gives the same results."""
+    monkeypatch.setenv("EV_FUSED_STAGING", "tma")
+    check(workloads.random_layers(15, 10, seed=12), variant, 5)
+    check(workloads.haar_layers(16, 6, seed=13), variant, 5)
+    c = workloads.ghz_midmeasure(14)
+    c.compose(workloads.random_layers(14, 3, seed=2))
+    ex, wbits, _, _ = check(c, variant, 5, seed=3)
+    assert ex.classical() == wbits
