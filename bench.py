@@ -67,9 +67,10 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--case", default="headline",
-                    choices=["headline", "fused", "tiled64", "batch", "serve"],
+                    choices=["headline", "fused", "tiled64", "batch", "serve", "prepared"],
                     help="run one section alone (for profiling): the complex64 fused or tiled "
-                         "path on the random-layer circuit, the TFIM batch, or the serving mix")
+                         "path on the random-layer circuit, the TFIM batch, the serving mix, "
+                         "or prepared-graph replay")
     ap.add_argument("--variant", default="bf16x3", choices=["bf16x3", "tf32x3", "fp32"])
     return ap.parse_args()
 
@@ -393,6 +394,37 @@ def extras_serve():
     return out
 
 
+def extras_prepared():
+    """Replaying one circuit as a recorded CUDA graph against planning and
+    launching it at every run (ev_state_run), same circuit and seeds."""
+    from everett_gb300 import CudaStateVectorBackend, State, workloads
+    out = {}
+    for n, dtype, mode, depth in ((12, "complex128", "exact", 20), (20, "complex64", "tiled", 20)):
+        c = workloads.ghz_midmeasure(n).compose(workloads.random_layers(n, depth, 7))
+        c.measure(1, 0)
+        st = State.zero(n, dtype)
+        prep = CudaStateVectorBackend.prepare(st, c, mode=mode)
+        reps = 200
+        for seed in range(5):
+            prep.launch(seed)
+            CudaStateVectorBackend.run_into(st, c, seed, mode=mode)
+        t0 = time.perf_counter()
+        for seed in range(reps):
+            CudaStateVectorBackend.run_into(st, c, seed, mode=mode)
+        plain = reps / (time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        for seed in range(reps):
+            prep.launch(seed)
+        graph = reps / (time.perf_counter() - t0)
+        out[f"{n}q_{dtype}_{mode}"] = {
+            "workload": f"GHZ + mid-circuit measurement + X_if, then random layers depth {depth}, "
+                        f"{n} qubits, {dtype}, {mode} mode, {len(c)} ops",
+            "kernels_per_run": prep.kernels(), "runs_per_s_run_into": round(plain, 1),
+            "runs_per_s_prepared_graph": round(graph, 1), "speedup": round(graph / plain, 2)}
+        prep.close()
+    return out
+
+
 def run_ours(args, dist: Dist):
     import numpy as np
 
@@ -481,7 +513,8 @@ def run_ours(args, dist: Dist):
                             ("qft", lambda: extras_qft(L, N, n, peak)),
                             ("haar28_depth40", lambda: extras_haar(L, N)),
                             ("batch_tfim4096", extras_batch),
-                            ("serve_mix", extras_serve)):
+                            ("serve_mix", extras_serve),
+                            ("prepared_graph", extras_prepared)):
                 try:
                     extras[key] = fn()
                 except Exception as exc:  # report, do not hide
@@ -514,8 +547,9 @@ def run_case(args):
     """One section alone, printing its own JSON line (a profiling target)."""
     from everett_gb300 import State, _native as N, build, workloads
     build.build()
-    if args.case in ("batch", "serve"):
-        print(json.dumps({"case": args.case, **(extras_batch() if args.case == "batch" else extras_serve())}))
+    if args.case in ("batch", "serve", "prepared"):
+        fn = {"batch": extras_batch, "serve": extras_serve, "prepared": extras_prepared}[args.case]
+        print(json.dumps({"case": args.case, **fn()}))
         return
     L = N.lib()
     c = workloads.random_layers(args.qubits, args.depth, seed=1)

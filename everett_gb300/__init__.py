@@ -7,7 +7,7 @@ reference's public surface (Circuit, Gate1/Gate2, Op, State, Execution, Rng).
 """
 from . import algorithms, batch, serve, workloads
 from ._native import device_count
-from .backend import CudaStateVectorBackend, Execution, State
+from .backend import CudaStateVectorBackend, Execution, PreparedRun, State
 from .circuit import Apply1, Apply2, Circuit, Controlled, IfClassic, Measure
 from .error import (ClassicalBitOutOfRange, DimensionMismatch, DuplicateQubit, EverettError,
                     QubitOutOfRange)
@@ -15,7 +15,8 @@ from .gate import Gate1, Gate2
 from .rng import Rng
 
 __all__ = [
-    "algorithms", "batch", "serve", "workloads", "device_count", "CudaStateVectorBackend", "Execution", "State",
+    "algorithms", "batch", "serve", "workloads", "device_count", "CudaStateVectorBackend", "Execution", "PreparedRun",
+    "State",
     "Apply1", "Apply2", "Circuit", "Controlled", "IfClassic", "Measure", "ClassicalBitOutOfRange",
     "DimensionMismatch", "DuplicateQubit", "EverettError", "QubitOutOfRange", "Gate1", "Gate2",
     "Rng",

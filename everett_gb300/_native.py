@@ -90,6 +90,10 @@ _SIGS = {
     "ev_state_profile": [_P, _I32],
     "ev_state_profile_read": [_P, _P, _I32, C.POINTER(_I32)],
     "ev_batch_run": [_P, _U64, _P, _P],
+    "ev_prepare": [_P, _P, _P, C.POINTER(_P)],
+    "ev_prepared_launch": [_P, _U64, _P],
+    "ev_prepared_kernels": [_P, C.POINTER(_U64)],
+    "ev_prepared_destroy": [_P],
     "ev_server_create": [_P, C.POINTER(_P)],
     "ev_server_submit": [_P, C.POINTER(EvCircuit), _U64, _U64, _P, C.POINTER(_U64)],
     "ev_server_cancel": [_P, _U64],

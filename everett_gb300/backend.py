@@ -173,6 +173,51 @@ class Execution:
         return self._state
 
 
+class PreparedRun:
+    """A circuit planned once for a state and recorded as one CUDA graph.
+
+    ``launch(seed)`` replays the whole run (reset, gates, device-side
+    measurement and classical control) with a single graph launch and gives
+    the classical register; the state then holds the run's final amplitudes,
+    exactly as after ``CudaStateVectorBackend.run_into`` with the same seed.
+    """
+
+    def __init__(self, state: State, circuit: Circuit, mode="exact", tile_bits=0,
+                 variant="tf32x3"):
+        c = circuit.ev_struct()
+        opts = _options(state.dtype(), mode, tile_bits, variant)
+        h = C.c_void_p()
+        N.check(N.lib().ev_prepare(state.handle, C.byref(c), C.byref(opts), C.byref(h)))
+        self._h = h
+        self._state = state  # the state must outlive the prepared run
+        self._ncl = circuit.num_classical()
+        self._classical = np.zeros(max(1, self._ncl), dtype=np.uint8)
+
+    def launch(self, seed: int = 0) -> list:
+        N.check(N.lib().ev_prepared_launch(self._h, seed, self._classical.ctypes.data))
+        return [bool(b) for b in self._classical[:self._ncl]]
+
+    def kernels(self) -> int:
+        out = C.c_uint64()
+        N.check(N.lib().ev_prepared_kernels(self._h, C.byref(out)))
+        return out.value
+
+    def state(self) -> State:
+        return self._state
+
+    def close(self) -> None:
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                N.lib().ev_prepared_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+
 def _options(dtype, mode, tile_bits, variant="tf32x3") -> N.EvRunOptions:
     o = N.EvRunOptions()
     o.dtype = _DTYPES[dtype]
@@ -226,6 +271,14 @@ class CudaStateVectorBackend:
         N.check(N.lib().ev_state_run(state.handle, C.byref(c), seed, C.byref(opts),
                                      classical.ctypes.data))
         return [bool(b) for b in classical[:ncl]]
+
+    @staticmethod
+    def prepare(state: State, circuit: Circuit, mode="exact", tile_bits=0,
+                variant="tf32x3") -> PreparedRun:
+        """Plans a circuit for a state once and records it as a CUDA graph;
+        each ``launch(seed)`` of the result equals ``run_into`` with that
+        seed."""
+        return PreparedRun(state, circuit, mode, tile_bits, variant)
 
     # Backend trait (src/backend/mod.rs:25-39)
     def state(self) -> State:

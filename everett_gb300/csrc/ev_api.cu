@@ -93,7 +93,7 @@ static cudaEvent_t take_event(ev_state* s) {
 }
 
 ProfScope::ProfScope(ev_state* st, int c, double b) : s(st), cls(c), bytes(b) {
-  if (s->profiling) {
+  if (s->profiling && !s->capturing) {
     a = take_event(s);
     if (a) cudaEventRecord(a, s->stream);
   }
@@ -198,21 +198,6 @@ static int validate(const ev_circuit* c) {
 
 // ---- run --------------------------------------------------------------
 
-// Device buffers of one run: classical register, uniforms, nested-IF bits.
-// Stream-ordered allocations: no device-wide synchronisation, so runs on
-// different states overlap.
-struct RunBuffers {
-  cudaStream_t stream = nullptr;
-  uint8_t* classical = nullptr;
-  double* uniforms = nullptr;
-  uint64_t* ifbits = nullptr;
-  ~RunBuffers() {
-    if (classical) cudaFreeAsync(classical, stream);
-    if (uniforms) cudaFreeAsync(uniforms, stream);
-    if (ifbits) cudaFreeAsync(ifbits, stream);
-  }
-};
-
 // Keeps freed stream-ordered memory in the device pool instead of returning
 // it to the driver at every synchronisation.
 void keep_pool_warm(int device) {
@@ -227,13 +212,57 @@ void keep_pool_warm(int device) {
   done[device] = true;
 }
 
-int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int tile_bits,
-              const uint8_t* pred, uint64_t* passes_out);
-int fused_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int kbits,
-              int variant, uint64_t* blocks_out);
+// Uniforms of a prepared run, drawn on the device from the seed that the
+// graph copied in (the same generator as the host's Rng, src/rng.rs:18-58).
+__global__ void k_run_uniforms(const uint64_t* seed, double* out, uint64_t n) {
+  DevRng r(*seed);
+  for (uint64_t j = 0; j < n; ++j) out[j] = r.next_f64();
+}
 
-static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run_options* o,
-                   uint8_t* classical_out) {
+enum RunStepKind { RS_APPLY1 = 0, RS_APPLY2, RS_CTRL, RS_MEASURE, RS_PRED_AND, RS_SEGMENT };
+
+// One launch group of a planned run.  Everything a step needs is held here
+// or in the uploaded blob, so a plan outlives the circuit it came from.
+struct RunStep {
+  int kind = 0;
+  int pred = 0;        // 0: unconditional; 1: classical[pbit]; 2: the AND of an IF chain
+  uint64_t pbit = 0;
+  uint64_t q0 = 0, q1 = 0, mask = 0;
+  size_t bits_off = 0;  // RS_PRED_AND: classical bit list in the blob
+  int nbits = 0;
+  double m[32];
+  SegStep seg;
+};
+
+// A run planned once: steps, one device blob (IF bit lists, tile plans and
+// records, fused descriptors and operand images), classical register and
+// uniforms.  Executing it only enqueues memsets, copies and kernels on the
+// state's stream, so it can be captured into a CUDA graph.
+struct RunPlan {
+  cudaStream_t stream = nullptr;
+  std::vector<RunStep> steps;
+  PlanBlob blob;
+  uint64_t nmeas = 0, num_classical = 0;
+  bool normalize = false;
+  unsigned char* dblob = nullptr;
+  uint8_t* classical = nullptr;
+  double* uniforms = nullptr;
+  uint64_t* dseed = nullptr;
+  void release() {
+    if (dblob) cudaFreeAsync(dblob, stream);
+    if (classical) cudaFreeAsync(classical, stream);
+    if (uniforms) cudaFreeAsync(uniforms, stream);
+    if (dseed) cudaFreeAsync(dseed, stream);
+    dblob = nullptr;
+    classical = nullptr;
+    uniforms = nullptr;
+    dseed = nullptr;
+  }
+  ~RunPlan() { release(); }
+};
+
+static int build_plan(ev_state* s, const ev_circuit* c, const ev_run_options* o, bool device_seed,
+                      RunPlan* plan) {
   const int mode = o ? o->mode : EV_MODE_EXACT;
   const int tile_bits = o ? o->tile_bits : 0;
   const int variant = o ? o->variant : 0;
@@ -241,30 +270,13 @@ static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run
     return fail(EV_ERR_INVALID_ARGUMENT, "fused mode needs complex64 amplitudes");
   if (mode < EV_MODE_EXACT || mode > EV_MODE_FUSED)
     return fail(EV_ERR_INVALID_ARGUMENT, "unknown run mode %d", mode);
-  RunBuffers rb;
-  rb.stream = s->stream;
-  // count Measure records and the nesting of IF chains
-  uint64_t nmeas = 0, nif = 0;
-  for (uint64_t j = 0; j < c->nops; ++j) {
-    if (c->ops[j].kind == EV_OP_MEASURE) ++nmeas;
-    if (c->ops[j].kind == EV_OP_IF) ++nif;
-  }
-  const uint64_t ncl = c->num_classical ? c->num_classical : 1;
-  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&rb.classical), ncl, s->stream));
-  EV_CUDA(cudaMemsetAsync(rb.classical, 0, ncl, s->stream));
-  std::vector<double> uni(nmeas ? nmeas : 1, 0.0);
-  Rng rng(seed);
-  for (uint64_t j = 0; j < nmeas; ++j) uni[j] = rng.next_f64();
-  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&rb.uniforms), uni.size() * sizeof(double), s->stream));
-  EV_CUDA(cudaMemcpyAsync(rb.uniforms, uni.data(), uni.size() * sizeof(double),
-                          cudaMemcpyHostToDevice, s->stream));
-  // counter[0]: uniforms consumed; counter[1]: device timeout flag
-  EV_CUDA(cudaMemsetAsync(s->scratch.counter, 0, 2 * sizeof(uint32_t), s->stream));
-  if (nif)
-    EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&rb.ifbits), nif * sizeof(uint64_t), s->stream));
-  // The host copy of the nested-IF bit lists must outlive the async copy.
-  std::vector<uint64_t> host_ifbits(nif ? nif : 1);
-  uint64_t if_used = 0;
+  plan->stream = s->stream;
+  plan->num_classical = c->num_classical;
+  // complex64 runs end with an FP64 renormalisation: FP32-rounded gate
+  // matrices are unitary only to ~1e-7, and the drift of the norm over a deep
+  // circuit would otherwise dominate the error against the f64 result.
+  plan->normalize = s->dtype == EV_C64;
+  std::vector<SegStep> segs;
   uint64_t pos = 0;
   while (pos < c->nops) {
     // collect an IF prefix chain
@@ -274,64 +286,146 @@ static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run
       if (nchain < 64) chain[nchain++] = c->ops[pos].q0;
       ++pos;
     }
-    const uint8_t* pred = nullptr;
+    RunStep head;
     if (nchain == 1) {
-      pred = rb.classical + chain[0];
+      head.pred = 1;
+      head.pbit = chain[0];
     } else if (nchain > 1) {
-      std::memcpy(&host_ifbits[if_used], chain, nchain * sizeof(uint64_t));
-      EV_CUDA(cudaMemcpyAsync(rb.ifbits + if_used, &host_ifbits[if_used], nchain * sizeof(uint64_t),
-                              cudaMemcpyHostToDevice, s->stream));
-      EV_TRY(launch_pred_and(s, rb.classical, rb.ifbits + if_used, nchain, s->scratch.pred));
-      if_used += nchain;
-      pred = s->scratch.pred;
+      RunStep st;
+      st.kind = RS_PRED_AND;
+      st.bits_off = plan->blob.add(chain, nchain * sizeof(uint64_t));
+      st.nbits = nchain;
+      plan->steps.push_back(st);
+      head.pred = 2;
     }
-    // tiled mode: fuse a run of unconditional gate records
+    // tiled and fused modes: one segment per run of unconditional gates
     if (mode != EV_MODE_EXACT && nchain == 0 && c->ops[pos].kind != EV_OP_MEASURE) {
       uint64_t end = pos;
       while (end < c->nops && c->ops[end].kind != EV_OP_MEASURE && c->ops[end].kind != EV_OP_IF)
         ++end;
-      uint64_t passes = 0;
-      if (mode == EV_MODE_TILED)
-        EV_TRY(tiled_run(s, c, pos, end, tile_bits, nullptr, &passes));
-      else
-        EV_TRY(fused_run(s, c, pos, end, tile_bits, variant, &passes));
+      segs.clear();
+      EV_TRY(plan_segment(s, c, pos, end, mode, tile_bits, variant, &plan->blob, &segs));
+      for (const SegStep& g : segs) {
+        RunStep st;
+        st.kind = RS_SEGMENT;
+        st.seg = g;
+        plan->steps.push_back(st);
+      }
       pos = end;
       continue;
     }
     const ev_op& op = c->ops[pos];
+    RunStep st = head;
+    st.q0 = op.q0;
+    st.q1 = op.q1;
     switch (op.kind) {
       case EV_OP_APPLY1:
-        EV_TRY(launch_apply1(s, op.q0, op.m, pred));
+        st.kind = RS_APPLY1;
+        std::memcpy(st.m, op.m, 8 * sizeof(double));
         break;
       case EV_OP_APPLY2:
-        EV_TRY(launch_apply2(s, op.q0, op.q1, op.m, pred));
+        st.kind = RS_APPLY2;
+        std::memcpy(st.m, op.m, 32 * sizeof(double));
         break;
-      case EV_OP_CONTROLLED: {
-        uint64_t mask = 0;
-        for (uint32_t j = 0; j < op.nctrl; ++j) mask |= uint64_t(1) << c->ctrl_pool[op.ctrl_off + j];
-        EV_TRY(launch_controlled(s, mask, op.q0, op.m, pred));
+      case EV_OP_CONTROLLED:
+        st.kind = RS_CTRL;
+        for (uint32_t j = 0; j < op.nctrl; ++j) st.mask |= uint64_t(1) << c->ctrl_pool[op.ctrl_off + j];
+        std::memcpy(st.m, op.m, 8 * sizeof(double));
         break;
-      }
       case EV_OP_MEASURE:
-        EV_TRY(launch_measure(s, op.q0, 0.0, rb.uniforms, rb.classical + op.q1, pred));
+        st.kind = RS_MEASURE;
+        ++plan->nmeas;
         break;
     }
+    plan->steps.push_back(st);
     ++pos;
   }
-  // complex64 runs end with an FP64 renormalisation: FP32-rounded gate
-  // matrices are unitary only to ~1e-7, and the drift of the norm over a deep
-  // circuit would otherwise dominate the error against the f64 result.
-  if (s->dtype == EV_C64) EV_TRY(launch_normalize(s));
-  if (c->num_classical) {
-    EV_CUDA(cudaMemcpyAsync(classical_out, rb.classical, c->num_classical, cudaMemcpyDeviceToHost,
-                            s->stream));
+  // device buffers: stream-ordered, so planning never synchronises the device
+  const uint64_t ncl = c->num_classical ? c->num_classical : 1;
+  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&plan->classical), ncl, s->stream));
+  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&plan->uniforms),
+                          (plan->nmeas ? plan->nmeas : 1) * sizeof(double), s->stream));
+  if (device_seed)
+    EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&plan->dseed), sizeof(uint64_t), s->stream));
+  if (!plan->blob.host.empty()) {
+    EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&plan->dblob), plan->blob.host.size(), s->stream));
+    EV_CUDA(cudaMemcpyAsync(plan->dblob, plan->blob.host.data(), plan->blob.host.size(),
+                            cudaMemcpyHostToDevice, s->stream));
+  }
+  return EV_OK;
+}
+
+// Enqueues a planned run.  zero: reset the state to |0...0> first.  The
+// classical register and the two device flags are copied to the host
+// buffers given (flags[1] != 0: a bounded device wait gave up).
+static int execute_plan(ev_state* s, const RunPlan& plan, bool zero, uint8_t* classical_host,
+                        uint32_t* flags_host) {
+  if (zero) EV_TRY(state_zero(s));
+  const uint64_t ncl = plan.num_classical ? plan.num_classical : 1;
+  EV_CUDA(cudaMemsetAsync(plan.classical, 0, ncl, s->stream));
+  // counter[0]: uniforms consumed; counter[1]: device timeout flag
+  EV_CUDA(cudaMemsetAsync(s->scratch.counter, 0, 2 * sizeof(uint32_t), s->stream));
+  if (plan.dseed && plan.nmeas) {
+    k_run_uniforms<<<1, 1, 0, s->stream>>>(plan.dseed, plan.uniforms, plan.nmeas);
+    s->launches += 1;
+    EV_CUDA(cudaGetLastError());
+  }
+  for (const RunStep& st : plan.steps) {
+    const uint8_t* pred = st.pred == 1   ? plan.classical + st.pbit
+                          : st.pred == 2 ? s->scratch.pred
+                                         : nullptr;
+    switch (st.kind) {
+      case RS_APPLY1:
+        EV_TRY(launch_apply1(s, st.q0, st.m, pred));
+        break;
+      case RS_APPLY2:
+        EV_TRY(launch_apply2(s, st.q0, st.q1, st.m, pred));
+        break;
+      case RS_CTRL:
+        EV_TRY(launch_controlled(s, st.mask, st.q0, st.m, pred));
+        break;
+      case RS_MEASURE:
+        EV_TRY(launch_measure(s, st.q0, 0.0, plan.uniforms, plan.classical + st.q1, pred));
+        break;
+      case RS_PRED_AND:
+        EV_TRY(launch_pred_and(s, plan.classical,
+                               reinterpret_cast<const uint64_t*>(plan.dblob + st.bits_off), st.nbits,
+                               s->scratch.pred));
+        break;
+      case RS_SEGMENT:
+        if (st.seg.fused)
+          EV_TRY(launch_fused_step(s, st.seg, plan.dblob));
+        else
+          EV_TRY(launch_tile_step(s, st.seg, plan.dblob));
+        break;
+    }
+  }
+  if (plan.normalize) EV_TRY(launch_normalize(s));
+  if (plan.num_classical)
+    EV_CUDA(cudaMemcpyAsync(classical_host, plan.classical, plan.num_classical,
+                            cudaMemcpyDeviceToHost, s->stream));
+  EV_CUDA(cudaMemcpyAsync(flags_host, s->scratch.counter, 2 * sizeof(uint32_t),
+                          cudaMemcpyDeviceToHost, s->stream));
+  return EV_OK;
+}
+
+static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run_options* o,
+                   uint8_t* classical_out) {
+  RunPlan plan;
+  EV_TRY(build_plan(s, c, o, false, &plan));
+  // uniforms from the host generator, one per Measure record (the host
+  // vector lives until the stream has been synchronised)
+  std::vector<double> uni(plan.nmeas);
+  if (plan.nmeas) {
+    Rng rng(seed);
+    for (uint64_t j = 0; j < plan.nmeas; ++j) uni[j] = rng.next_f64();
+    EV_CUDA(cudaMemcpyAsync(plan.uniforms, uni.data(), uni.size() * sizeof(double),
+                            cudaMemcpyHostToDevice, s->stream));
   }
   uint32_t flags[2] = {0, 0};
-  EV_CUDA(cudaMemcpyAsync(flags, s->scratch.counter, sizeof(flags), cudaMemcpyDeviceToHost,
-                          s->stream));
+  EV_TRY(execute_plan(s, plan, false, classical_out, flags));
   EV_CUDA(cudaStreamSynchronize(s->stream));
-  if (flags[1] != 0)
-    return fail(EV_ERR_TIMEOUT, "a bounded device wait gave up during the run");
+  if (flags[1] != 0) return fail(EV_ERR_TIMEOUT, "a bounded device wait gave up during the run");
   return EV_OK;
 }
 
@@ -564,6 +658,122 @@ extern "C" int ev_state_run(ev_state* s, const ev_circuit* c, uint64_t seed,
   EV_CUDA(cudaSetDevice(s->device));
   EV_TRY(state_zero(s));
   return run_ops(s, c, seed, opts, classical_out);
+}
+
+// ---- prepared runs ----------------------------------------------------------
+
+struct ev_prepared {
+  ev_state* s = nullptr;
+  ev::RunPlan plan;
+  unsigned char* pinned = nullptr;  // seed (8 B), flags (8 B), classical register
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  uint64_t kernels = 0;
+  uint64_t* seed_host() { return reinterpret_cast<uint64_t*>(pinned); }
+  uint32_t* flags_host() { return reinterpret_cast<uint32_t*>(pinned + 8); }
+  uint8_t* classical_host() { return pinned + 16; }
+};
+
+static void free_prepared(ev_prepared* p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->plan.release();
+  cudaStreamSynchronize(p->s->stream);
+  if (p->pinned) cudaFreeHost(p->pinned);
+  cudaGetLastError();
+  delete p;
+}
+
+extern "C" int ev_prepare(ev_state* s, const ev_circuit* c, const ev_run_options* opts,
+                          ev_prepared** out) {
+  clear_error();
+  if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_prepare: null argument");
+  EV_TRY(validate(c));
+  if (c->num_qubits != s->n)
+    return fail(EV_ERR_DIMENSION_MISMATCH, "circuit has %llu qubits, state has %llu",
+                (unsigned long long)c->num_qubits, (unsigned long long)s->n);
+  if (opts && opts->dtype != s->dtype)
+    return fail(EV_ERR_INVALID_ARGUMENT, "run options name a different amplitude type");
+  EV_CUDA(cudaSetDevice(s->device));
+  ev_prepared* p = new ev_prepared();
+  p->s = s;
+  int rc = build_plan(s, c, opts, true, &p->plan);
+  if (rc == EV_OK) {
+    cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&p->pinned), 16 + (c->num_classical | 1));
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      p->pinned = nullptr;
+      rc = fail(EV_ERR_OOM, "cannot allocate pinned run buffers");
+    }
+  }
+  if (rc == EV_OK) {
+    // Record the launch-only half of the run.  Relaxed capture: kernel
+    // attribute queries made while launching stay legal.
+    const uint64_t before = s->launches;
+    cudaError_t e = cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed);
+    if (e != cudaSuccess) {
+      rc = fail(EV_ERR_CUDA, "cudaStreamBeginCapture: %s", cudaGetErrorString(e));
+    } else {
+      s->capturing = true;
+      e = cudaMemcpyAsync(p->plan.dseed, p->seed_host(), sizeof(uint64_t), cudaMemcpyHostToDevice,
+                          s->stream);
+      rc = e == cudaSuccess ? execute_plan(s, p->plan, true, p->classical_host(), p->flags_host())
+                            : fail(EV_ERR_CUDA, "seed copy: %s", cudaGetErrorString(e));
+      s->capturing = false;
+      const cudaError_t e2 = cudaStreamEndCapture(s->stream, &p->graph);
+      if (rc == EV_OK && e2 != cudaSuccess)
+        rc = fail(EV_ERR_CUDA, "cudaStreamEndCapture: %s", cudaGetErrorString(e2));
+    }
+    p->kernels = s->launches - before;
+    s->launches = before;
+  }
+  if (rc == EV_OK) {
+    const cudaError_t e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+    if (e != cudaSuccess) rc = fail(EV_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+  }
+  if (rc == EV_OK) {
+    // planning's uploads must land before the first replay
+    const cudaError_t e = cudaStreamSynchronize(s->stream);
+    if (e != cudaSuccess) rc = fail(EV_ERR_CUDA, "ev_prepare: %s", cudaGetErrorString(e));
+  }
+  if (rc != EV_OK) {
+    cudaGetLastError();
+    free_prepared(p);
+    return rc;
+  }
+  *out = p;
+  return EV_OK;
+}
+
+extern "C" int ev_prepared_launch(ev_prepared* p, uint64_t seed, uint8_t* classical_out) {
+  clear_error();
+  if (!p) return fail(EV_ERR_INVALID_ARGUMENT, "ev_prepared_launch: null argument");
+  const uint64_t ncl = p->plan.num_classical;
+  if (ncl && !classical_out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_prepared_launch: null classical output");
+  ev_state* s = p->s;
+  EV_CUDA(cudaSetDevice(s->device));
+  *p->seed_host() = seed;  // read by the graph's first copy
+  EV_CUDA(cudaGraphLaunch(p->exec, s->stream));
+  EV_CUDA(cudaStreamSynchronize(s->stream));
+  s->launches += p->kernels;
+  if (ncl) std::memcpy(classical_out, p->classical_host(), ncl);
+  if (p->flags_host()[1] != 0) return fail(EV_ERR_TIMEOUT, "a bounded device wait gave up during the run");
+  return EV_OK;
+}
+
+extern "C" int ev_prepared_kernels(const ev_prepared* p, uint64_t* out) {
+  clear_error();
+  if (!p || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_prepared_kernels: null argument");
+  *out = p->kernels;
+  return EV_OK;
+}
+
+extern "C" int ev_prepared_destroy(ev_prepared* p) {
+  clear_error();
+  if (!p) return EV_OK;
+  cudaSetDevice(p->s->device);
+  free_prepared(p);
+  return EV_OK;
 }
 
 // ---- measurement hooks ------------------------------------------------------

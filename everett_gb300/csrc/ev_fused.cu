@@ -981,8 +981,8 @@ static int launch_fp32(ev_state* s, const FusedDesc* dd, const float2* du, uint6
 
 int default_fused_bits() { return 5; }
 
-int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int tile_bits,
-              const uint8_t* pred, uint64_t* passes_out);
+int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int tile_bits,
+               PlanBlob* blob, std::vector<SegStep>* out);
 
 // Fusion width actually used for a variant and a request (0 = default).
 int fused_width(int variant, int kbits) {
@@ -994,84 +994,82 @@ int fused_width(int variant, int kbits) {
   return k;
 }
 
-int fused_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int kbits,
-              int variant, uint64_t* blocks_out) {
+// Plans a gate run into fused-unitary passes: descriptors and operand
+// images go into the blob.
+static int plan_fused(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int kbits,
+                      int variant, PlanBlob* blob, std::vector<SegStep>* out) {
   if (s->dtype != EV_C64) return fail(EV_ERR_INVALID_ARGUMENT, "fused mode needs a complex64 state");
   if (variant < EV_FUSED_TF32X3 || variant > EV_FUSED_FP32)
     return fail(EV_ERR_INVALID_ARGUMENT, "unknown fused variant %d", variant);
   const int n = int(s->n);
   const int k = fused_width(variant, kbits);
   // registers too small for 128-row steps run through the tile pass
-  if (n < k + 7) return tiled_run(s, c, first, last, 0, nullptr, blocks_out);
+  if (n < k + 7) return plan_tiled(s, c, first, last, 0, blob, out);
   const bool tc = variant != EV_FUSED_FP32;
-  std::vector<Block> blocks = fuse_ops(c, first, last, n, k);
-  if (blocks_out) *blocks_out = blocks.size();
-  if (blocks.empty()) return EV_OK;
-  // one device buffer: descriptors, then per-block matrices
-  std::vector<std::vector<unsigned char>> mats(blocks.size());
-  for (size_t i = 0; i < blocks.size(); ++i) {
-    if (tc) {
-      build_bmat(blocks[i], variant, &mats[i]);
-    } else {
-      const int D = 1 << blocks[i].F.size();
-      mats[i].resize(size_t(D) * D * sizeof(float2));
-      float2* u = reinterpret_cast<float2*>(mats[i].data());
-      for (int e = 0; e < D * D; ++e)
-        u[e] = make_float2(float(blocks[i].U[e].real()), float(blocks[i].U[e].imag()));
-    }
-  }
-  const size_t desc_bytes = (blocks.size() * sizeof(FusedDesc) + 255) / 256 * 256;
-  std::vector<size_t> mat_off(blocks.size());
-  size_t total = desc_bytes;
-  for (size_t i = 0; i < blocks.size(); ++i) {
-    mat_off[i] = total;
-    total += (mats[i].size() + 255) / 256 * 256;
-  }
-  std::vector<unsigned char> host(total, 0);
-  for (size_t i = 0; i < blocks.size(); ++i) {
-    build_desc(blocks[i], n, reinterpret_cast<FusedDesc*>(host.data()) + i);
-    std::memcpy(host.data() + mat_off[i], mats[i].data(), mats[i].size());
-  }
-  unsigned char* dbuf = nullptr;
-  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dbuf), total, s->stream));
-  EV_CUDA(cudaMemcpyAsync(dbuf, host.data(), total, cudaMemcpyHostToDevice, s->stream));
-  int* derr = reinterpret_cast<int*>(s->scratch.counter + 1);
   // Register-staged streaming (default: the faster of the two on GB300, see
   // the measured comparison in the design notes) or the warp-specialised
-  // TMA-staged pipeline (EV_FUSED_STAGING=tma), read at every call.
+  // TMA-staged pipeline (EV_FUSED_STAGING=tma), read when a run is planned.
   const char* staging = getenv("EV_FUSED_STAGING");
   const bool use_tma = staging != nullptr && std::strcmp(staging, "tma") == 0;
-  int rc = EV_OK;
-  for (size_t i = 0; i < blocks.size() && rc == EV_OK; ++i) {
-    const FusedDesc* dd = reinterpret_cast<const FusedDesc*>(dbuf) + i;
-    const unsigned char* dm = dbuf + mat_off[i];
-    const uint64_t nsteps = reinterpret_cast<const FusedDesc*>(host.data())[i].nsteps;
-    ProfScope prof(s, P_FUSED, 2.0 * double(s->len()) * 8.0);
-    s->launches += 1;
-    const int kb = int(blocks[i].F.size());
+  std::vector<Block> blocks = fuse_ops(c, first, last, n, k);
+  std::vector<unsigned char> mat;
+  for (const Block& b : blocks) {
     if (tc) {
-      if (variant == EV_FUSED_TF32X3)
-        rc = use_tma ? launch_tma<5, EV_FUSED_TF32X3, 3>(s, dd, dm, nsteps, derr)
-                     : launch_tc<5, EV_FUSED_TF32X3>(s, dd, dm, nsteps, derr);
-      else if (kb == 5)
-        rc = use_tma ? launch_tma<5, EV_FUSED_BF16X3, 3>(s, dd, dm, nsteps, derr)
-                     : launch_tc<5, EV_FUSED_BF16X3>(s, dd, dm, nsteps, derr);
-      else
-        rc = launch_tc<6, EV_FUSED_BF16X3>(s, dd, dm, nsteps, derr);
+      build_bmat(b, variant, &mat);
     } else {
-      const float2* du = reinterpret_cast<const float2*>(dm);
-      switch (kb) {
-        case 1: rc = launch_fp32<1>(s, dd, du, nsteps); break;
-        case 2: rc = launch_fp32<2>(s, dd, du, nsteps); break;
-        case 3: rc = launch_fp32<3>(s, dd, du, nsteps); break;
-        case 4: rc = launch_fp32<4>(s, dd, du, nsteps); break;
-        case 5: rc = launch_fp32<5>(s, dd, du, nsteps); break;
-        default: rc = launch_fp32<6>(s, dd, du, nsteps); break;
-      }
+      const int D = 1 << b.F.size();
+      mat.assign(size_t(D) * D * sizeof(float2), 0);
+      float2* u = reinterpret_cast<float2*>(mat.data());
+      for (int e = 0; e < D * D; ++e) u[e] = make_float2(float(b.U[e].real()), float(b.U[e].imag()));
     }
+    FusedDesc d;
+    std::memset(&d, 0, sizeof(d));
+    build_desc(b, n, &d);
+    SegStep st;
+    st.fused = 1;
+    st.off0 = blob->add(&d, sizeof(d));
+    st.off1 = blob->add(mat.data(), mat.size());
+    st.k = int(b.F.size());
+    st.variant = variant;
+    st.tma = use_tma ? 1 : 0;
+    st.count = d.nsteps;
+    out->push_back(st);
   }
-  cudaFreeAsync(dbuf, s->stream);
-  return rc;
+  return EV_OK;
+}
+
+int launch_fused_step(ev_state* s, const SegStep& st, const unsigned char* dblob) {
+  const FusedDesc* dd = reinterpret_cast<const FusedDesc*>(dblob + st.off0);
+  const unsigned char* dm = dblob + st.off1;
+  int* derr = reinterpret_cast<int*>(s->scratch.counter + 1);
+  ProfScope prof(s, P_FUSED, 2.0 * double(s->len()) * 8.0);
+  s->launches += 1;
+  const uint64_t nsteps = st.count;
+  const bool tma = st.tma != 0;
+  if (st.variant == EV_FUSED_TF32X3)
+    return tma ? launch_tma<5, EV_FUSED_TF32X3, 3>(s, dd, dm, nsteps, derr)
+               : launch_tc<5, EV_FUSED_TF32X3>(s, dd, dm, nsteps, derr);
+  if (st.variant == EV_FUSED_BF16X3) {
+    if (st.k == 5)
+      return tma ? launch_tma<5, EV_FUSED_BF16X3, 3>(s, dd, dm, nsteps, derr)
+                 : launch_tc<5, EV_FUSED_BF16X3>(s, dd, dm, nsteps, derr);
+    return launch_tc<6, EV_FUSED_BF16X3>(s, dd, dm, nsteps, derr);
+  }
+  const float2* du = reinterpret_cast<const float2*>(dm);
+  switch (st.k) {
+    case 1: return launch_fp32<1>(s, dd, du, nsteps);
+    case 2: return launch_fp32<2>(s, dd, du, nsteps);
+    case 3: return launch_fp32<3>(s, dd, du, nsteps);
+    case 4: return launch_fp32<4>(s, dd, du, nsteps);
+    case 5: return launch_fp32<5>(s, dd, du, nsteps);
+    default: return launch_fp32<6>(s, dd, du, nsteps);
+  }
+}
+
+int plan_segment(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int mode,
+                 int bits, int variant, PlanBlob* blob, std::vector<SegStep>* out) {
+  if (mode == EV_MODE_FUSED) return plan_fused(s, c, first, last, bits, variant, blob, out);
+  return plan_tiled(s, c, first, last, bits, blob, out);
 }
 
 }  // namespace ev

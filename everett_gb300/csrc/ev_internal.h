@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
 #include "../../include/everett_cuda.h"
@@ -83,6 +84,7 @@ struct ev_state {
   int tc_ctas_per_sm = 0;         // last tensor-core launch: resident CTAs per SM
   cudaEvent_t slots[16] = {};
   bool profiling = false;
+  bool capturing = false;  // launches are being recorded into a graph
   std::vector<ev::ProfRec> pending;
   std::vector<cudaEvent_t> event_pool;
   ev::ProfStat stats[ev::P_COUNT] = {};
@@ -126,6 +128,38 @@ int launch_measure(ev_state* s, uint64_t k, double u_host, const double* u_dev,
 // pred_out = AND of classical[bits[i]]
 int launch_pred_and(ev_state* s, const uint8_t* classical, const uint64_t* bits, int nbits,
                     uint8_t* pred_out);
+
+// Host bytes gathered while planning a run, uploaded once (256-byte
+// aligned sections).
+struct PlanBlob {
+  std::vector<unsigned char> host;
+  size_t add(const void* p, size_t n) {
+    const size_t off = (host.size() + 255) / 256 * 256;
+    host.resize(off + n);
+    if (n) memcpy(host.data() + off, p, n);
+    return off;
+  }
+};
+
+// One shared-memory tile pass or one fused-unitary pass of a planned run.
+struct SegStep {
+  int fused = 0;        // 0: tile pass, 1: fused unitary
+  size_t off0 = 0;      // tile: TilePlan offset; fused: FusedDesc offset (in the blob)
+  size_t off1 = 0;      // tile: first op record; fused: matrix operands
+  int nops = 0;         // tile: op records
+  int k = 0, L = 0;     // tile: tile bits, contiguous low bits; fused: k = qubits
+  int variant = 0;      // fused: EV_FUSED_*
+  int tma = 0;          // fused: TMA-staged pipeline
+  uint64_t count = 0;   // tile: tiles; fused: 128-row steps
+};
+
+// Plans ops [first, last) of a gate run (mode EV_MODE_TILED or
+// EV_MODE_FUSED) into segment steps whose data are appended to the blob.
+int plan_segment(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int mode,
+                 int bits, int variant, PlanBlob* blob, std::vector<SegStep>* out);
+// Launches one planned segment step (dblob = the uploaded blob).
+int launch_tile_step(ev_state* s, const SegStep& st, const unsigned char* dblob);
+int launch_fused_step(ev_state* s, const SegStep& st, const unsigned char* dblob);
 
 int reduce_norm(const ev_state* s, double* out_host);
 // Queues State::normalize (FP64 norm, then scaling) on the state's stream.

@@ -99,8 +99,9 @@ static int launch_tile(ev_state* s, uint64_t ntiles, const TilePlan& plan, const
 
 int default_tile_bits(int dtype) { return dtype == EV_C128 ? 12 : 13; }
 
-int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int tile_bits,
-              const uint8_t* pred, uint64_t* passes_out) {
+// Plans a gate run into tile passes; plans and records go into the blob.
+int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int tile_bits,
+               PlanBlob* blob, std::vector<SegStep>* out) {
   const int n = int(s->n);
   int k = tile_bits > 0 ? tile_bits : default_tile_bits(s->dtype);
   const int kcap = s->dtype == EV_C128 ? 13 : 14;  // tile + records within 227 KiB
@@ -113,10 +114,8 @@ int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, i
   // complex64 may reorder commuting ops; complex128 keeps the reference's order
   std::vector<Pass> passes =
       plan_passes(c, first, last, n, k, L, uint64_t(kMaxPassOps), s->dtype == EV_C64);
-  std::vector<TileOp> ops(last - first);
-  std::vector<std::pair<int, int>> ranges;  // (offset, count) into ops per pass
-  std::vector<TilePlan> plans;
-  uint64_t w = 0;
+  const uint64_t ntiles = uint64_t(1) << (n - k);
+  std::vector<TileOp> ops;
   for (const Pass& p : passes) {
     TilePlan plan{};
     plan.k = k;
@@ -132,35 +131,29 @@ int tiled_run(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, i
       } else {
         plan.comp[plan.ncomp++] = uint8_t(q);
       }
-    for (size_t j = 0; j < p.ops.size(); ++j) encode_op(c, c->ops[p.ops[j]], p.tset, local, &ops[w + j]);
-    ranges.push_back({int(w), int(p.ops.size())});
-    plans.push_back(plan);
-    w += p.ops.size();
+    ops.assign(p.ops.size(), TileOp{});
+    for (size_t j = 0; j < p.ops.size(); ++j) encode_op(c, c->ops[p.ops[j]], p.tset, local, &ops[j]);
+    SegStep st;
+    st.fused = 0;
+    st.off0 = blob->add(&plan, sizeof(plan));
+    st.off1 = blob->add(ops.data(), ops.size() * sizeof(TileOp));
+    st.nops = int(ops.size());
+    st.k = k;
+    st.L = L;
+    st.count = ntiles;
+    out->push_back(st);
   }
-  // one device buffer: plans, then op records
-  const size_t plan_bytes = (passes.size() * sizeof(TilePlan) + 255) / 256 * 256;
-  const size_t total = plan_bytes + std::max<size_t>(1, ops.size()) * sizeof(TileOp);
-  std::vector<unsigned char> host(total, 0);
-  std::memcpy(host.data(), plans.data(), passes.size() * sizeof(TilePlan));
-  std::memcpy(host.data() + plan_bytes, ops.data(), ops.size() * sizeof(TileOp));
-  unsigned char* dbuf = nullptr;
-  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dbuf), total, s->stream));
-  EV_CUDA(cudaMemcpyAsync(dbuf, host.data(), total, cudaMemcpyHostToDevice, s->stream));
-  const TilePlan* dplans = reinterpret_cast<const TilePlan*>(dbuf);
-  const TileOp* dops = reinterpret_cast<const TileOp*>(dbuf + plan_bytes);
-  int rc = EV_OK;
-  const uint64_t ntiles = uint64_t(1) << (n - k);
-  for (size_t i = 0; i < passes.size() && rc == EV_OK; ++i) {
-    if (s->dtype == EV_C128)
-      rc = launch_tile<double2>(s, ntiles, plans[i], dplans + i, dops + ranges[i].first,
-                                ranges[i].second, pred);
-    else
-      rc = launch_tile<float2>(s, ntiles, plans[i], dplans + i, dops + ranges[i].first,
-                               ranges[i].second, pred);
-  }
-  cudaFreeAsync(dbuf, s->stream);
-  if (passes_out) *passes_out = passes.size();
-  return rc;
+  return EV_OK;
+}
+
+int launch_tile_step(ev_state* s, const SegStep& st, const unsigned char* dblob) {
+  TilePlan plan{};
+  plan.k = st.k;
+  plan.L = st.L;
+  const TilePlan* dplan = reinterpret_cast<const TilePlan*>(dblob + st.off0);
+  const TileOp* dops = reinterpret_cast<const TileOp*>(dblob + st.off1);
+  if (s->dtype == EV_C128) return launch_tile<double2>(s, st.count, plan, dplan, dops, st.nops, nullptr);
+  return launch_tile<float2>(s, st.count, plan, dplan, dops, st.nops, nullptr);
 }
 
 }  // namespace ev

@@ -252,6 +252,23 @@ typedef struct ev_batch_stats {
 int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const ev_batch_options* opts,
                  ev_batch_stats* stats);
 
+/* ---- prepared runs (no reference counterpart) ------------------------------
+ * A circuit planned once for one state and recorded as a CUDA graph.  Each
+ * launch replays the whole run with one graph launch: reset to |0...0>, the
+ * gate, tile or fused passes, device-side measurement and classical control,
+ * and the final renormalisation of complex64 runs.  A launch gives exactly
+ * what ev_state_run gives for the same circuit, options and seed.  The
+ * circuit may be freed after ev_prepare; the state must outlive the prepared
+ * run, and no other call may use the state while a launch is in flight. */
+typedef struct ev_prepared ev_prepared;
+
+int ev_prepare(ev_state* s, const ev_circuit* c, const ev_run_options* opts, ev_prepared** out);
+/* Runs the prepared circuit with the measurement stream seeded by seed and
+ * copies the classical register (num_classical bytes, 0/1) to classical_out. */
+int ev_prepared_launch(ev_prepared* p, uint64_t seed, uint8_t* classical_out);
+int ev_prepared_kernels(const ev_prepared* p, uint64_t* out); /* kernels per launch */
+int ev_prepared_destroy(ev_prepared* p);
+
 /* ---- serving (no reference counterpart) ------------------------------------
  * A continuous-batching request loop.  Requests are admitted in arrival
  * order while the state memory of admitted requests (2^n x 16 or 8 bytes)
