@@ -67,10 +67,11 @@ def parse_args():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--case", default="headline",
-                    choices=["headline", "fused", "tiled64", "batch", "serve", "prepared"],
+                    choices=["headline", "fused", "tiled64", "batch", "serve", "prepared",
+                             "kernels"],
                     help="run one section alone (for profiling): the complex64 fused or tiled "
                          "path on the random-layer circuit, the TFIM batch, the serving mix, "
-                         "or prepared-graph replay")
+                         "prepared-graph replay, or each streaming kernel class alone")
     ap.add_argument("--variant", default="bf16x3", choices=["bf16x3", "tf32x3", "fp32"])
     return ap.parse_args()
 
@@ -425,6 +426,91 @@ def extras_prepared():
     return out
 
 
+def extras_kernels(n: int, peak: float):
+    """Each streaming kernel class alone on an n-qubit state, timed with CUDA
+    events on the state's stream, against the measured copy bandwidth.
+    Bytes are the algorithmic bytes the engine's kernel moves (2 * N_t * B for
+    a gate; measure: the half with bit k read, then the kept half read and all
+    written; normalize: one read for the norm, then a read and a write;
+    sampling: one read of the state plus a write and a read of the 2^n - 1
+    doubles of the probability tree).
+
+    complex128 arithmetic is FP64, which GB300 issues at a small fraction of
+    its FP32 rate, so each complex128 case also carries its FP64 floor: the
+    FP64 instructions its kernel issues per state amplitude (dmul, dadd, dfma
+    counted from the source: a complex product in the reference's FMA form is
+    4, a complex add 2) times 2^n, over the measured FMA issue rate."""
+    import ctypes as C
+
+    import numpy as np
+
+    from everett_gb300 import Gate1, Gate2, Rng, State, _native as N, workloads
+    L = N.lib()
+    rate = C.c_double()
+    N.check(L.ev_probe_fp64(C.byref(rate)))
+    g_dense = workloads.haar_1q(Rng.seed_from_u64(5))
+    rng = np.random.default_rng(3)
+    g2 = Gate2(rng.normal(size=16) + 1j * rng.normal(size=16))
+    out = {"fp64_fma_per_s_measured": float(f"{rate.value:.4g}")}
+    for dtype, B in (("complex128", 16), ("complex64", 8)):
+        st = State.zero(n, dtype)
+        other = State.zero(n, dtype)
+        N.check(L.ev_normalize(st.handle))
+        h = st.handle
+        Nn = 1 << n
+        hi, lo = n - 1, 0
+        # name, call, algorithmic bytes, FP64 instructions per amplitude (complex128)
+        cases = [
+            ("1q_dense_high", lambda: st.apply_1q(hi, g_dense), 2 * Nn * B, 10),
+            ("1q_dense_low", lambda: st.apply_1q(lo, g_dense), 2 * Nn * B, 10),
+            ("1q_real_h", lambda: st.apply_1q(hi - 3, Gate1.h()), 2 * Nn * B, 6),
+            ("1q_diag_rz", lambda: st.apply_1q(hi - 1, Gate1.rz(0.3)), 2 * Nn * B, 4),
+            ("1q_phase", lambda: st.apply_1q(hi - 2, Gate1.phase(0.3)), Nn * B, 2),
+            ("1q_anti_x", lambda: st.apply_1q(7, Gate1.x()), 2 * Nn * B, 4),
+            ("cnot", lambda: st.apply_2q(hi, 3, Gate2.cnot()), Nn * B, 0),
+            ("cz", lambda: st.apply_2q(hi, 3, Gate2.cz()), Nn * B // 2, 0),
+            ("swap", lambda: st.apply_2q(hi, 3, Gate2.swap()), Nn * B, 0),
+            ("2q_dense", lambda: st.apply_2q(hi, 3, g2), 2 * Nn * B, 22),
+            ("controlled_1q_1ctrl", lambda: st.apply_controlled_1q([hi], 5, g_dense), Nn * B, 5),
+            ("measure_high", lambda: st.measure_qubit(hi, 0.25), 2 * Nn * B, 2),
+            ("measure_low", lambda: st.measure_qubit(lo, 0.25), 2 * Nn * B, 2),
+            ("norm_sqr", lambda: st.norm_sqr(), Nn * B, 2),
+            ("normalize", lambda: st.normalize(), 3 * Nn * B, 4),
+            ("overlap", lambda: st.overlap(other), 2 * Nn * B, 4),
+            ("sample_1000_shots", lambda: st.sample(1000, seed=1), Nn * B + 16 * Nn, 3),
+        ]
+        res = {}
+        for name, fn, nbytes, fp64 in cases:
+            fn()
+            reps = 3
+            N.check(L.ev_state_record_event(h, 0))
+            for _ in range(reps):
+                fn()
+            N.check(L.ev_state_record_event(h, 1))
+            ms = C.c_float()
+            N.check(L.ev_state_elapsed_ms(h, 0, 1, C.byref(ms)))
+            per = ms.value / reps
+            gbs = nbytes / (per / 1e3) / 1e9
+            r = {"ms": round(per, 3), "GB_s": round(gbs, 1), "frac": round(gbs / peak, 3)}
+            if dtype == "complex128" and fp64:
+                floor = fp64 * Nn / rate.value * 1e3
+                hbm = nbytes / (peak * 1e9) * 1e3
+                r["fp64_floor_ms"] = round(floor, 3)
+                r["bound"] = "fp64" if floor > hbm else "hbm"
+                r["frac_of_bound"] = round(max(floor, hbm) / per, 3)
+            res[name] = r
+            if name.startswith("measure"):
+                N.check(L.ev_normalize(h))  # undo the collapse's zeroed half for later cases
+                st.apply_1q(hi, Gate1.h())
+                st.apply_1q(lo, Gate1.h())
+        out[dtype] = res
+        del st, other
+    out["note"] = (f"{n} qubits; frac against the measured copy bandwidth {peak:.0f} GB/s; "
+                   "complex128 cases with FP64 arithmetic also against the measured FP64 FMA "
+                   "rate (frac_of_bound = the larger floor over the time)")
+    return out
+
+
 def run_ours(args, dist: Dist):
     import numpy as np
 
@@ -547,6 +633,10 @@ def run_case(args):
     """One section alone, printing its own JSON line (a profiling target)."""
     from everett_gb300 import State, _native as N, build, workloads
     build.build()
+    if args.case == "kernels":
+        peak, _ = measured_peaks()
+        print(json.dumps({"case": "kernels", **extras_kernels(args.qubits, peak)}))
+        return
     if args.case in ("batch", "serve", "prepared"):
         fn = {"batch": extras_batch, "serve": extras_serve, "prepared": extras_prepared}[args.case]
         print(json.dumps({"case": args.case, **fn()}))

@@ -838,6 +838,66 @@ extern "C" int ev_state_profile_read(ev_state* s, ev_kernel_stat* out, int32_t m
   return EV_OK;
 }
 
+namespace ev {
+// Eight independent FMA chains per thread; the final compare keeps every
+// chain live without a store per thread.
+__global__ void __launch_bounds__(256) k_probe_fp64(double* out, int iters, double seed) {
+  double a[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) a[c] = seed + double(threadIdx.x + c);
+  const double m = 0.9999999, add = 1e-7;
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) a[c] = __fma_rn(a[c], m, add);
+  double t = 0.0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) t += a[c];
+  if (t == -1.0) out[0] = t;
+}
+}  // namespace ev
+
+extern "C" int ev_probe_fp64(double* fma_per_s) {
+  clear_error();
+  if (!fma_per_s) return fail(EV_ERR_INVALID_ARGUMENT, "ev_probe_fp64: null output");
+  int dev = 0, sms = 0;
+  EV_CUDA(cudaGetDevice(&dev));
+  EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  cudaStream_t st = nullptr;
+  EV_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  double* out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = EV_OK;
+  const int iters = 1 << 15, blocks = sms * 8;
+  if (cudaMallocAsync(reinterpret_cast<void**>(&out), sizeof(double), st) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    rc = fail(EV_ERR_CUDA, "ev_probe_fp64: setup failed");
+  } else {
+    k_probe_fp64<<<blocks, 256, 0, st>>>(out, iters, 1.0);  // warm-up
+    double best = 0.0;
+    for (int rep = 0; rep < 3 && rc == EV_OK; ++rep) {  // best of three
+      cudaEventRecord(e0, st);
+      k_probe_fp64<<<blocks, 256, 0, st>>>(out, iters, 2.0 + rep);
+      cudaEventRecord(e1, st);
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.f) {
+        rc = fail(EV_ERR_CUDA, "ev_probe_fp64: timing failed");
+      } else {
+        const double r = double(blocks) * 256.0 * double(iters) * 8.0 / (double(ms) * 1e-3);
+        if (r > best) best = r;
+      }
+    }
+    if (rc == EV_OK) *fma_per_s = best;
+  }
+  if (out) cudaFreeAsync(out, st);
+  cudaStreamSynchronize(st);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  cudaGetLastError();
+  return rc;
+}
+
 extern "C" int ev_host_alloc(uint64_t bytes, void** out) {
   clear_error();
   if (!out) return fail(EV_ERR_INVALID_ARGUMENT, "null output");

@@ -76,6 +76,47 @@ __device__ __forceinline__ uint64_t insert0(uint64_t i, int k) {
   return ((i >> k) << (k + 1)) | (i & low);
 }
 
+// ---- double-float arithmetic on the FP32 pipe ------------------------------
+// GB300 issues FP64 at a small fraction of the FP32 rate, so complex64
+// reductions keep their per-element work in FP32 without giving up FP64-level
+// accuracy: a product of two floats is split exactly into p + e
+// (e = fma(a, b, -p)), and sums are carried as unevaluated pairs hi + lo
+// (Knuth's TwoSum, then a Fast2Sum renormalisation), a representation with
+// about 48 significant bits.
+
+// Exact float -> double by bit manipulation on the integer pipe: normal
+// numbers and zeros directly, subnormals, infinities and NaNs through the
+// conversion instruction.
+__device__ __forceinline__ double f2d_exact(float f) {
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xFFu;
+  if (e == 0u && (u & 0x7FFFFFu) == 0u) return __longlong_as_double((long long)(uint64_t(u) << 32));
+  if (e == 0u || e == 0xFFu) return double(f);
+  const uint64_t bits = (uint64_t(u & 0x80000000u) << 32) | (uint64_t(e + 896u) << 52) |
+                        (uint64_t(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
+}
+
+struct FF {
+  float hi = 0.f, lo = 0.f;
+  // (hi, lo) += x
+  __device__ __forceinline__ void add(float x) {
+    const float s = __fadd_rn(hi, x);
+    const float bp = __fsub_rn(s, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+    const float t = __fadd_rn(lo, err);
+    hi = __fadd_rn(s, t);
+    lo = __fsub_rn(t, __fsub_rn(hi, s));
+  }
+  // (hi, lo) += a * b, the product taken exactly
+  __device__ __forceinline__ void add_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    lo = __fadd_rn(lo, __fmaf_rn(a, b, -p));
+    add(p);
+  }
+  __device__ __forceinline__ double value() const { return f2d_exact(hi) + f2d_exact(lo); }
+};
+
 }  // namespace ev
 
 namespace ev {

@@ -52,53 +52,9 @@ __device__ __forceinline__ void red_term(const V* __restrict__ a, const V* __res
   }
 }
 
-// Block b reduces the contiguous counter range [b*chunk, (b+1)*chunk) and
-// writes 4 partials; the tree inside the block has a fixed shape.
-// Compensated f32 accumulation of |x|^2 for complex64 norms: each square is
-// split exactly into p + e (p = x*x, e = fma(x, x, -p)), the p terms are
-// summed with Neumaier's compensated sum and the (tiny) e terms plainly;
-// every 64 elements the partial joins the f64 accumulator.  Keeps the f64
-// pipe out of the per-element path while the result agrees with an f64 sum
-// to ~1e-14 relative.
-struct CompSum {
-  float s = 0.f, c = 0.f;
-  __device__ __forceinline__ void add(float x) {
-    const float t = s + x;
-    c += fabsf(s) >= fabsf(x) ? (s - t) + x : (x - t) + s;
-    s = t;
-  }
-  __device__ __forceinline__ void add_sq(float x) {
-    const float p = x * x;
-    c += __fmaf_rn(x, x, -p);
-    add(p);
-  }
-};
-
-template <int OP, typename V>
-__global__ void __launch_bounds__(kRedThreads)
-    k_reduce(const V* __restrict__ a, const V* __restrict__ b, uint64_t count, uint64_t chunk,
-             int k, double* __restrict__ partials, const uint8_t* pred) {
-  if (pred != nullptr && *pred == 0) return;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
-  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
-  const uint64_t hi = lo + chunk < count ? lo + chunk : count;
-  if constexpr (sizeof(V) == 8 && (OP == R_NORM || OP == R_P1)) {
-    CompSum cs;
-    int n = 0;
-    for (uint64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) {
-      const V x = OP == R_NORM ? a[i] : a[insert0(i, k) | (uint64_t(1) << k)];
-      cs.add_sq(x.x);
-      cs.add_sq(x.y);
-      if (++n == 64) {
-        acc[0] += double(cs.s) + double(cs.c);
-        cs = CompSum();
-        n = 0;
-      }
-    }
-    acc[0] += double(cs.s) + double(cs.c);
-  } else {
-    for (uint64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) red_term<OP>(a, b, i, k, acc);
-  }
+// Block-wide sum of 4 per-thread accumulators in a fixed tree order; thread
+// 0..3 write the block's partials.
+__device__ __forceinline__ void block_partials(double acc[4], double* __restrict__ partials) {
   __shared__ double sh[4][kRedThreads];
 #pragma unroll
   for (int c = 0; c < 4; ++c) sh[c][threadIdx.x] = acc[c];
@@ -110,6 +66,189 @@ __global__ void __launch_bounds__(kRedThreads)
     __syncthreads();
   }
   if (threadIdx.x < 4) partials[blockIdx.x * 4 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// Block b reduces the contiguous counter range [b*chunk, (b+1)*chunk) and
+// writes 4 partials; the tree inside the block has a fixed shape.  (Bloch
+// vectors and complex128 overlaps; the hot sums have kernels of their own
+// below.)
+template <int OP, typename V>
+__global__ void __launch_bounds__(kRedThreads)
+    k_reduce(const V* __restrict__ a, const V* __restrict__ b, uint64_t count, uint64_t chunk,
+             int k, double* __restrict__ partials, const uint8_t* pred) {
+  if (pred != nullptr && *pred == 0) return;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
+  const uint64_t hi = lo + chunk < count ? lo + chunk : count;
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) red_term<OP>(a, b, i, k, acc);
+  block_partials(acc, partials);
+}
+
+// Terms are taken in pairs (2q, 2q+1) so that every access is a 16-byte (or
+// 32-byte) contiguous load; a block's range starts on an even term.
+constexpr int kFlush = 32;  // pairs per double-float run before the f64 flush
+
+__device__ __forceinline__ float4 ld4(const float2* p) { return *reinterpret_cast<const float4*>(p); }
+
+// The two amplitudes of terms 2q, 2q+1: all amplitudes (norm) or those with
+// bit k set (p1).
+template <int OP, typename V>
+__device__ __forceinline__ void sq_pair(const V* __restrict__ a, uint64_t q, int k, V* t0, V* t1) {
+  if constexpr (OP == R_NORM) {
+    *t0 = a[2 * q];
+    *t1 = a[2 * q + 1];
+  } else {
+    if (k > 0) {
+      const uint64_t j = insert0(2 * q, k) | (uint64_t(1) << k);
+      *t0 = a[j];
+      *t1 = a[j + 1];
+    } else {
+      *t0 = a[4 * q + 1];
+      *t1 = a[4 * q + 3];
+    }
+  }
+}
+
+// Sum of |a_j|^2 (norm, p1).  complex64: double-float on the FP32 pipe,
+// flushed to f64 every kFlush pairs (agrees with an f64 sum to ~1e-14
+// relative); complex128: two f64 FMAs per amplitude.  Each thread issues a
+// group of kGroup loads before any arithmetic, so enough bytes are in flight
+// to cover HBM latency.
+constexpr int kGroup = 8;
+
+template <int OP>
+__device__ __forceinline__ float4 sq_load_c64(const float2* __restrict__ a, uint64_t q, int k) {
+  if (OP == R_NORM) return ld4(a + 2 * q);
+  if (k > 0) return ld4(a + (insert0(2 * q, k) | (uint64_t(1) << k)));
+  const float4 u0 = ld4(a + 4 * q), u1 = ld4(a + 4 * q + 2);
+  return make_float4(u0.z, u0.w, u1.z, u1.w);
+}
+
+template <int OP, typename V>
+__global__ void __launch_bounds__(kRedThreads)
+    k_reduce_sq(const V* __restrict__ a, uint64_t count, uint64_t chunk, int k,
+                double* __restrict__ partials, const uint8_t* pred) {
+  if (pred != nullptr && *pred == 0) return;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
+  const uint64_t hi = lo + chunk < count ? lo + chunk : count;
+  const uint64_t q0 = lo / 2, q1 = hi / 2;
+  for (uint64_t base = q0 + threadIdx.x; base < q1; base += uint64_t(kFlush) * kRedThreads) {
+    if constexpr (sizeof(V) == 8) {
+      const float2* af = reinterpret_cast<const float2*>(a);
+      FF f;
+      for (int g = 0; g < kFlush; g += kGroup) {
+        float4 v[kGroup];
+#pragma unroll
+        for (int r = 0; r < kGroup; ++r) {
+          const uint64_t q = base + uint64_t(g + r) * kRedThreads;
+          v[r] = q < q1 ? sq_load_c64<OP>(af, q, k) : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int r = 0; r < kGroup; ++r) {
+          f.add_prod(v[r].x, v[r].x);
+          f.add_prod(v[r].y, v[r].y);
+          f.add_prod(v[r].z, v[r].z);
+          f.add_prod(v[r].w, v[r].w);
+        }
+      }
+      acc[0] += f.value();
+    } else {
+      for (int g = 0; g < kFlush; g += kGroup) {
+        V t[kGroup][2];
+#pragma unroll
+        for (int r = 0; r < kGroup; ++r) {
+          const uint64_t q = base + uint64_t(g + r) * kRedThreads;
+          if (q < q1) {
+            sq_pair<OP>(a, q, k, &t[r][0], &t[r][1]);
+          } else {
+            t[r][0] = t[r][1] = make_double2(0.0, 0.0);
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < kGroup; ++r) {
+          acc[r & 1] = __fma_rn(t[r][0].x, t[r][0].x, acc[r & 1]);
+          acc[r & 1] = __fma_rn(t[r][0].y, t[r][0].y, acc[r & 1]);
+          acc[r & 1] = __fma_rn(t[r][1].x, t[r][1].x, acc[r & 1]);
+          acc[r & 1] = __fma_rn(t[r][1].y, t[r][1].y, acc[r & 1]);
+        }
+      }
+    }
+  }
+  // an odd count leaves one term for the last block
+  if ((count & 1) && hi == count && hi > lo && threadIdx.x == 0) {
+    const uint64_t i = count - 1;
+    const V x = OP == R_NORM ? a[i] : a[insert0(i, k) | (uint64_t(1) << k)];
+    acc[2] += nsq(x);
+  }
+  acc[0] += acc[1] + acc[2];
+  acc[1] = acc[2] = 0.0;
+  block_partials(acc, partials);
+}
+
+// <other|self> for two complex128 states: re and im each as a chain of f64
+// FMAs (4 per amplitude instead of a complex product and two adds).
+__global__ void __launch_bounds__(kRedThreads)
+    k_overlap_c128(const double2* __restrict__ a, const double2* __restrict__ b, uint64_t count,
+                   uint64_t chunk, double* __restrict__ partials) {
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
+  const uint64_t hi = lo + chunk < count ? lo + chunk : count;
+  for (uint64_t base = lo + threadIdx.x; base < hi; base += uint64_t(kGroup) * kRedThreads) {
+    double2 x[kGroup], y[kGroup];
+#pragma unroll
+    for (int r = 0; r < kGroup; ++r) {
+      const uint64_t i = base + uint64_t(r) * kRedThreads;
+      x[r] = i < hi ? a[i] : make_double2(0.0, 0.0);
+      y[r] = i < hi ? b[i] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int r = 0; r < kGroup; ++r) {
+      acc[0] = __fma_rn(y[r].x, x[r].x, acc[0]);
+      acc[0] = __fma_rn(y[r].y, x[r].y, acc[0]);
+      acc[1] = __fma_rn(y[r].x, x[r].y, acc[1]);
+      acc[1] = __fma_rn(-y[r].y, x[r].x, acc[1]);
+    }
+  }
+  block_partials(acc, partials);
+}
+
+// <other|self> = sum conj(other_j) * self_j for two complex64 states:
+// double-float products and sums, flushed to f64 every kFlush pairs.
+__global__ void __launch_bounds__(kRedThreads)
+    k_overlap_c64(const float2* __restrict__ a, const float2* __restrict__ b, uint64_t count,
+                  uint64_t chunk, double* __restrict__ partials) {
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
+  const uint64_t hi = lo + chunk < count ? lo + chunk : count;
+  const uint64_t q0 = lo / 2, q1 = hi / 2;
+  for (uint64_t base = q0 + threadIdx.x; base < q1; base += uint64_t(kFlush) * kRedThreads) {
+    FF re, im;
+#pragma unroll 4
+    for (int r = 0; r < kFlush; ++r) {
+      const uint64_t q = base + uint64_t(r) * kRedThreads;
+      if (q < q1) {
+        const float4 x = ld4(a + 2 * q), y = ld4(b + 2 * q);
+        re.add_prod(y.x, x.x);
+        re.add_prod(y.y, x.y);
+        im.add_prod(y.x, x.y);
+        im.add_prod(-y.y, x.x);
+        re.add_prod(y.z, x.z);
+        re.add_prod(y.w, x.w);
+        im.add_prod(y.z, x.w);
+        im.add_prod(-y.w, x.z);
+      }
+    }
+    acc[0] += re.value();
+    acc[1] += im.value();
+  }
+  if ((count & 1) && hi == count && hi > lo && threadIdx.x == 0) {
+    const float2 x = a[count - 1], y = b[count - 1];
+    const double2 r = cmul(make_double2(y.x, -double(y.y)), make_double2(x.x, x.y));
+    acc[0] += r.x;
+    acc[1] += r.y;
+  }
+  block_partials(acc, partials);
 }
 
 // <other|self> for states of different amplitude types (both promoted to f64).
@@ -240,12 +379,25 @@ __global__ void k_pred_and(const uint8_t* __restrict__ classical, const uint64_t
 // mass level q (2^q entries) lives at offset 2^q - 1.  mass[n-1][r] =
 // |a_r|^2 + |a_{r+2^(n-1)}|^2 and mass[q][r] = mass[q+1][r] + mass[q+1][r+2^q].
 
+// complex128 leaves use the oracle's arithmetic (nsq + nsq, f64), so shots
+// match its tree exactly; complex64 leaves are the double-float sum of the
+// four exact float squares, rounded to f64 once (~1e-14 relative).
+__device__ __forceinline__ double leaf_mass(double2 u, double2 v) { return __dadd_rn(nsq(u), nsq(v)); }
+__device__ __forceinline__ double leaf_mass(float2 u, float2 v) {
+  FF f;
+  f.add_prod(u.x, u.x);
+  f.add_prod(u.y, u.y);
+  f.add_prod(v.x, v.x);
+  f.add_prod(v.y, v.y);
+  return f.value();
+}
+
 template <typename V>
 __global__ void __launch_bounds__(256)
     k_mass_leaf(const V* __restrict__ a, uint64_t half, double* __restrict__ out) {
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   for (uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < half; r += stride)
-    out[r] = __dadd_rn(nsq(a[r]), nsq(a[r + half]));
+    out[r] = leaf_mass(a[r], a[r + half]);
 }
 
 __global__ void __launch_bounds__(256)
@@ -286,24 +438,52 @@ __global__ void __launch_bounds__(256)
 
 // ---- host ------------------------------------------------------------------
 
+// Blocks and the (even) per-block term range of a reduction over count terms.
+static void red_grid(uint64_t count, int sms, int max_blocks, int* nb_out, uint64_t* chunk_out) {
+  const uint64_t want = (count + 4095) / 4096;
+  int nb = int(want < 1 ? 1 : want);
+  int cap = sms * 8 < kMaxRedBlocks ? sms * 8 : kMaxRedBlocks;
+  if (cap > max_blocks) cap = max_blocks;
+  if (nb > cap) nb = cap;
+  uint64_t chunk = (count + nb - 1) / nb;
+  chunk = (chunk + 1) & ~uint64_t(1);
+  *nb_out = nb;
+  *chunk_out = chunk;
+}
+
 template <int OP>
 static int reduce(const ev_state* s, const ev_state* other, uint64_t count, int k,
                   const uint8_t* pred) {
-  const uint64_t want = (count + 4095) / 4096;
-  int nb = int(want < 1 ? 1 : want);
-  const int cap = s->num_sms * 4 < kMaxRedBlocks ? s->num_sms * 4 : kMaxRedBlocks;
-  if (nb > cap) nb = cap;
-  const uint64_t chunk = (count + nb - 1) / nb;
-  if (s->dtype == EV_C128)
+  int nb = 0;
+  uint64_t chunk = 0;
+  red_grid(count, s->num_sms, kMaxRedBlocks, &nb, &chunk);
+  const bool c128 = s->dtype == EV_C128;
+  if constexpr (OP == R_NORM || OP == R_P1) {
+    if (c128)
+      k_reduce_sq<OP, double2><<<nb, kRedThreads, 0, s->stream>>>(
+          static_cast<const double2*>(s->amps), count, chunk, k, s->scratch.partials, pred);
+    else
+      k_reduce_sq<OP, float2><<<nb, kRedThreads, 0, s->stream>>>(
+          static_cast<const float2*>(s->amps), count, chunk, k, s->scratch.partials, pred);
+  } else if (OP == R_OVERLAP && !c128) {
+    k_overlap_c64<<<nb, kRedThreads, 0, s->stream>>>(static_cast<const float2*>(s->amps),
+                                                    static_cast<const float2*>(other->amps), count,
+                                                    chunk, s->scratch.partials);
+  } else if (OP == R_OVERLAP) {
+    k_overlap_c128<<<nb, kRedThreads, 0, s->stream>>>(static_cast<const double2*>(s->amps),
+                                                     static_cast<const double2*>(other->amps), count,
+                                                     chunk, s->scratch.partials);
+  } else if (c128) {
     k_reduce<OP, double2><<<nb, kRedThreads, 0, s->stream>>>(
         static_cast<const double2*>(s->amps),
         other ? static_cast<const double2*>(other->amps) : nullptr, count, chunk, k,
         s->scratch.partials, pred);
-  else
+  } else {
     k_reduce<OP, float2><<<nb, kRedThreads, 0, s->stream>>>(
         static_cast<const float2*>(s->amps),
         other ? static_cast<const float2*>(other->amps) : nullptr, count, chunk, k,
         s->scratch.partials, pred);
+  }
   k_finish<<<1, kRedThreads, 0, s->stream>>>(s->scratch.partials, nb, s->scratch.result, pred);
   s->launches += 2;
   EV_CUDA(cudaGetLastError());
@@ -621,7 +801,7 @@ extern "C" int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* o
 // streams, no ordering between them) race; calls on one stream, or otherwise
 // ordered, are safe.
 namespace {
-constexpr int kNoAllocBlocks = 1024;
+constexpr int kNoAllocBlocks = 2048;
 constexpr uint64_t kNoAllocMaxQubits = 40;
 __device__ __align__(256) double g_noalloc_scratch[kNoAllocBlocks * 4 + 12];
 std::mutex g_noalloc_mu;
@@ -661,16 +841,13 @@ extern "C" int ev_measure_qubit_noalloc(double* amps, uint64_t n, uint64_t k, do
   double* meas = result + 8;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   double2* a = reinterpret_cast<double2*>(amps);
-  // same grid as the state-owned path, so the sums (and results) agree
+  // same kernel and grid as the state-owned path, so the sums (and results)
+  // agree
   const uint64_t count = (uint64_t(1) << n) / 2;
-  const uint64_t want = (count + 4095) / 4096;
-  int nb = int(want < 1 ? 1 : want);
-  int cap = sms * 4 < kMaxRedBlocks ? sms * 4 : kMaxRedBlocks;
-  if (cap > kNoAllocBlocks) cap = kNoAllocBlocks;
-  if (nb > cap) nb = cap;
-  const uint64_t chunk = (count + nb - 1) / nb;
-  k_reduce<R_P1, double2><<<nb, kRedThreads, 0, st>>>(a, nullptr, count, chunk, int(k), partials,
-                                                      nullptr);
+  int nb = 0;
+  uint64_t chunk = 0;
+  red_grid(count, sms, kNoAllocBlocks, &nb, &chunk);
+  k_reduce_sq<R_P1, double2><<<nb, kRedThreads, 0, st>>>(a, count, chunk, int(k), partials, nullptr);
   k_finish<<<1, kRedThreads, 0, st>>>(partials, nb, result, nullptr);
   k_decide<<<1, 1, 0, st>>>(result, u, nullptr, nullptr, meas, nullptr, nullptr);
   const uint64_t gw = (count + 255) / 256, gcap = uint64_t(sms) * 8;

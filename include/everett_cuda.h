@@ -341,6 +341,11 @@ typedef struct ev_kernel_stat {
 int ev_state_profile(ev_state* s, int32_t enable); /* enabling clears stats */
 int ev_state_profile_read(ev_state* s, ev_kernel_stat* out, int32_t max, int32_t* count);
 
+/* Measured FP64 FMA issue rate of the current device (FMA instructions per
+ * second, from independent FMA chains on every SM): the roofline of the
+ * complex128 kernels, whose arithmetic is FP64. */
+int ev_probe_fp64(double* fma_per_s);
+
 int ev_host_alloc(uint64_t bytes, void** out); /* page-locked host memory */
 int ev_host_free(void* p);
 

@@ -139,6 +139,47 @@ def test_observables_match_oracle(gpu):  # state.rs:94-185
     assert abs(d.norm_sqr() - 1) < 1e-12
 
 
+def test_complex64_reductions_match_oracle(gpu):
+    """complex64 norms, p1, overlaps and measurement (double-float sums on
+    the FP32 pipe, FP64 results) against the oracle evaluated in f64 on the
+    same complex64 amplitudes: 1e-12, at sizes that exercise the pair and
+    odd-tail paths (n = 1, 2, 3) and multi-block grids."""
+    for n in (1, 2, 3, 9, 17, 21):
+        amps, _, _ = O.run_seeded(workloads.random_layers(n, 3, seed=n))
+        other, _, _ = O.run_seeded(workloads.random_layers(n, 3, seed=n + 50))
+        a32 = amps.astype(np.complex64).astype(np.complex128)
+        o32 = other.astype(np.complex64).astype(np.complex128)
+        st = State.from_amplitudes(amps, dtype="complex64")
+        so = State.from_amplitudes(other, dtype="complex64")
+        assert abs(st.norm_sqr() - O.norm_sqr(a32)) < 1e-12, n
+        assert abs(st.overlap(so) - O.overlap(a32, o32)) < 1e-12, n
+        for k in sorted({0, min(1, n - 1), n - 1}):
+            st.upload(a32)
+            u = 0.37
+            got = st.measure_qubit(k, u)
+            p1 = float(np.sum(np.abs(a32[(np.arange(1 << n) >> k) & 1 == 1]) ** 2))
+            assert got == (u < p1), (n, k)
+    # a state concentrated on one amplitude: relative accuracy must hold
+    a = np.zeros(1 << 12, dtype=np.complex128)
+    a[77] = np.float32(0.999)
+    a[5] = np.float32(1e-3) * 1j
+    st = State.from_amplitudes(a, dtype="complex64")
+    want = O.norm_sqr(a.astype(np.complex64).astype(np.complex128))
+    assert abs(st.norm_sqr() - want) < 1e-14
+
+
+def test_complex64_shots_match_tree(gpu):
+    """complex64 sampling: the tree's leaves are double-float sums rounded to
+    f64 once, so shots equal the oracle's tree on the same amplitudes except
+    where a uniform falls within ~1e-14 of a conditional probability (none
+    at these sizes and seeds)."""
+    for n, seed in ((1, 3), (5, 4), (16, 5)):
+        amps, _, _ = O.run_seeded(workloads.random_layers(n, 4, seed=n))
+        st = State.from_amplitudes(amps, dtype="complex64")
+        a32 = np.ascontiguousarray(st.amplitudes())
+        assert np.array_equal(st.sample(2000, seed=seed), O.sample_tree(a32, seed, 2000)), n
+
+
 @pytest.mark.parametrize("mode", ["exact", "tiled"])
 def test_run_random_layers_bit_exact(gpu, mode):
     for n, depth, seed in ((5, 6, 1), (12, 10, 2), (16, 8, 3)):
