@@ -10,7 +10,7 @@ from ._native import device_count
 from .backend import CudaStateVectorBackend, Execution, PreparedRun, State
 from .circuit import Apply1, Apply2, Circuit, Controlled, IfClassic, Measure
 from .error import (ClassicalBitOutOfRange, DimensionMismatch, DuplicateQubit, EverettError,
-                    QubitOutOfRange)
+                    QasmError, QubitOutOfRange)
 from .gate import Gate1, Gate2
 from .rng import Rng
 
@@ -18,6 +18,6 @@ __all__ = [
     "algorithms", "batch", "serve", "workloads", "device_count", "CudaStateVectorBackend", "Execution", "PreparedRun",
     "State",
     "Apply1", "Apply2", "Circuit", "Controlled", "IfClassic", "Measure", "ClassicalBitOutOfRange",
-    "DimensionMismatch", "DuplicateQubit", "EverettError", "QubitOutOfRange", "Gate1", "Gate2",
+    "DimensionMismatch", "DuplicateQubit", "EverettError", "QasmError", "QubitOutOfRange", "Gate1", "Gate2",
     "Rng",
 ]

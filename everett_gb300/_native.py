@@ -32,6 +32,7 @@ ERR_QUBIT_OUT_OF_RANGE = 1
 ERR_CLASSICAL_BIT_OUT_OF_RANGE = 2
 ERR_DUPLICATE_QUBIT = 3
 ERR_DIMENSION_MISMATCH = 4
+ERR_QASM = 6
 ERR_INVALID_ARGUMENT = 16
 ERR_OOM = 17
 ERR_CUDA = 18
@@ -90,6 +91,11 @@ _SIGS = {
     "ev_state_profile": [_P, _I32],
     "ev_state_profile_read": [_P, _P, _I32, C.POINTER(_I32)],
     "ev_batch_run": [_P, _U64, _P, _P],
+    "ev_qasm_parse": [C.c_char_p, _U64, C.POINTER(_P), C.POINTER(_U64), C.POINTER(_U64)],
+    "ev_program_circuit": [_P, C.POINTER(EvCircuit)],
+    "ev_program_free": [_P],
+    "ev_qasm_emit": [C.POINTER(EvCircuit), _P, _U64, C.POINTER(_U64)],
+    "ev_server_submit_qasm": [_P, C.c_char_p, _U64, _U64, _U64, _P, C.POINTER(_U64)],
     "ev_prepare": [_P, _P, _P, C.POINTER(_P)],
     "ev_prepared_launch": [_P, _U64, _P],
     "ev_prepared_kernels": [_P, C.POINTER(_U64)],

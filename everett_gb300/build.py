@@ -1,6 +1,7 @@
 """Builds the engine's shared library for sm_103a with nvcc.
 
-Every ``csrc/*.cu`` translation unit is compiled in parallel into
+Every ``csrc/*.cu`` translation unit (nvcc) and every host-only
+``csrc/*.cpp`` unit (the host C++ compiler) is compiled in parallel into
 ``_build/`` and linked into ``everett_gb300/libeverett_gb300.so`` (in-tree,
 so the tests and the benchmark load exactly this file).  A unit is rebuilt
 only when it or a header is newer than its object.
@@ -20,13 +21,17 @@ LIB = HERE / "libeverett_gb300.so"
 INCLUDE = HERE.parent / "include"
 
 NVCC = os.environ.get("NVCC", "nvcc")
+CXX = os.environ.get("CXX", "g++")
+# host units: sin and cos stay separate libm calls (no sincos fusion), as the
+# reference's gate constructors make them
+CXXFLAGS = ["-O2", "-fPIC", "-std=c++17", "-fno-builtin-sin", "-fno-builtin-cos"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
 
 
 def _sources() -> list[Path]:
-    return sorted(CSRC.glob("*.cu"))
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
 
 
 def _headers() -> list[Path]:
@@ -38,12 +43,15 @@ def _compile(src: Path, verbose: bool) -> Path:
     newest_dep = max([src.stat().st_mtime] + [h.stat().st_mtime for h in _headers()])
     if obj.exists() and obj.stat().st_mtime >= newest_dep:
         return obj
-    cmd = [NVCC, *ARCH, *FLAGS, "-c", str(src), "-o", str(obj)]
+    if src.suffix == ".cpp":
+        cmd = [CXX, *CXXFLAGS, "-c", str(src), "-o", str(obj)]
+    else:
+        cmd = [NVCC, *ARCH, *FLAGS, "-c", str(src), "-o", str(obj)]
     if verbose:
         print(" ".join(cmd), flush=True)
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
-        raise RuntimeError(f"nvcc failed on {src.name}:\n{res.stdout}\n{res.stderr}")
+        raise RuntimeError(f"{cmd[0]} failed on {src.name}:\n{res.stdout}\n{res.stderr}")
     return obj
 
 

@@ -52,6 +52,10 @@ class IfClassic:
 Op = Union[Apply1, Apply2, Controlled, Measure, IfClassic]
 
 
+def _gate1(m) -> Gate1:
+    return Gate1(complex(m[0], m[1]), complex(m[2], m[3]), complex(m[4], m[5]), complex(m[6], m[7]))
+
+
 class Circuit:
     def __init__(self, num_qubits: int, num_classical: int = 0):
         self._n = int(num_qubits)
@@ -210,6 +214,63 @@ class Circuit:
         c.ctrl_pool = ctrl.ctypes.data
         c.pool_len = npool
         return c
+
+    # OpenQASM 3 (src/circuit.rs:308-326)
+    @classmethod
+    def from_qasm(cls, src: str) -> "Circuit":
+        """Circuit::from_qasm: the engine's reader (ev_qasm_parse), the same
+        subset, circuit and errors as src/qasm/parse.rs; raises QasmError."""
+        import ctypes as C
+        data = src.encode("utf-8")
+        h = C.c_void_p()
+        N.check(N.lib().ev_qasm_parse(data, len(data), C.byref(h), None, None))
+        try:
+            view = N.EvCircuit()
+            N.check(N.lib().ev_program_circuit(h, C.byref(view)))
+            recs = np.zeros(0, dtype=N.OP_DTYPE)
+            pool = np.zeros(0, dtype=np.uint64)
+            if view.nops:
+                raw = (C.c_char * (view.nops * N.OP_DTYPE.itemsize)).from_address(view.ops)
+                recs = np.frombuffer(raw, dtype=N.OP_DTYPE).copy()
+            if view.pool_len:
+                raw = (C.c_char * (view.pool_len * 8)).from_address(view.ctrl_pool)
+                pool = np.frombuffer(raw, dtype=np.uint64).copy()
+            c = cls(view.num_qubits, view.num_classical)
+        finally:
+            N.lib().ev_program_free(h)
+        pos = 0
+
+        def take():
+            nonlocal pos
+            r = recs[pos]
+            pos += 1
+            kind = int(r["kind"])
+            m = r["m"]
+            if kind == N.OP_APPLY1:
+                return Apply1(_gate1(m), int(r["q0"]))
+            if kind == N.OP_APPLY2:
+                return Apply2(Gate2(m[0::2] + 1j * m[1::2]), int(r["q0"]), int(r["q1"]))
+            if kind == N.OP_CONTROLLED:
+                off, k = int(r["ctrl_off"]), int(r["nctrl"])
+                return Controlled(tuple(int(q) for q in pool[off:off + k]), _gate1(m), int(r["q0"]))
+            if kind == N.OP_MEASURE:
+                return Measure(int(r["q0"]), int(r["q1"]))
+            return IfClassic(int(r["q0"]), take())
+
+        while pos < len(recs):
+            c._push(take())
+        return c
+
+    def to_qasm(self) -> str:
+        """Circuit::to_qasm: the engine's writer (ev_qasm_emit, emit.rs:17);
+        raises QasmError for a gate without a stdgates.inc name."""
+        import ctypes as C
+        c = self.ev_struct()
+        n = C.c_uint64()
+        N.check(N.lib().ev_qasm_emit(C.byref(c), None, 0, C.byref(n)))
+        buf = C.create_string_buffer(n.value + 1)
+        N.check(N.lib().ev_qasm_emit(C.byref(c), buf, n.value + 1, C.byref(n)))
+        return buf.raw[:n.value].decode("utf-8")
 
     def validate(self) -> None:
         """Circuit::validate (circuit.rs:245-306), via the engine's check."""

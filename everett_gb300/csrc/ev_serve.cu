@@ -310,6 +310,19 @@ extern "C" int ev_server_submit(ev_server* s, const ev_circuit* c, uint64_t seed
   return EV_OK;
 }
 
+extern "C" int ev_server_submit_qasm(ev_server* s, const char* src, uint64_t len, uint64_t seed,
+                                     uint64_t shots, uint64_t* shots_out, uint64_t* id) {
+  clear_error();
+  if (!s || !id) return fail(EV_ERR_INVALID_ARGUMENT, "ev_server_submit_qasm: null argument");
+  ev_program* prog = nullptr;
+  EV_TRY(ev_qasm_parse(src, len, &prog, nullptr, nullptr));
+  ev_circuit c;
+  int rc = ev_program_circuit(prog, &c);
+  if (rc == EV_OK) rc = ev_server_submit(s, &c, seed, shots, shots_out, id);  // copies the records
+  ev_program_free(prog);
+  return rc;
+}
+
 extern "C" int ev_server_cancel(ev_server* s, uint64_t id) {
   if (!s) return fail(EV_ERR_INVALID_ARGUMENT, "null server");
   std::lock_guard<std::mutex> lock(s->mu);

@@ -31,6 +31,24 @@ class DimensionMismatch(EverettError):
     code = N.ERR_DIMENSION_MISMATCH
 
 
+class QasmError(EverettError):
+    """Error::Qasm { line, col, message } (src/error.rs:45-52); str() reads
+    "OpenQASM 3 error at L:C: message" as the reference's Display does."""
+
+    code = N.ERR_QASM
+
+    def __init__(self, text: str = "", line: int = 0, col: int = 0, message: str = ""):
+        super().__init__(text)
+        self.line, self.col, self.message = line, col, message
+        if text and not message:
+            head = "OpenQASM 3 error at "
+            if text.startswith(head):
+                pos, _, rest = text[len(head):].partition(": ")
+                l, _, c = pos.partition(":")
+                if l.isdigit() and c.isdigit():
+                    self.line, self.col, self.message = int(l), int(c), rest
+
+
 class InvalidArgument(EverettError):
     code = N.ERR_INVALID_ARGUMENT
 
@@ -56,7 +74,8 @@ class Cancelled(EverettError):
 
 
 _BY_CODE = {cls.code: cls for cls in (
-    QubitOutOfRange, ClassicalBitOutOfRange, DuplicateQubit, DimensionMismatch, InvalidArgument,
+    QubitOutOfRange, ClassicalBitOutOfRange, DuplicateQubit, DimensionMismatch, QasmError,
+    InvalidArgument,
     DeviceOutOfMemory, CudaError, DeviceTimeout, AdmissionRefused, Cancelled)}
 
 

@@ -79,6 +79,17 @@ class Server:
             self._buffers[rid.value] = (buf, shots, keep)
         return rid.value
 
+    def submit_qasm(self, src: str, seed: int = 0, shots: int = 1000) -> int:
+        """Submits OpenQASM 3 text; a parse error raises QasmError here."""
+        buf = np.zeros(max(1, shots), dtype=np.uint64)
+        data = src.encode("utf-8")
+        rid = C.c_uint64()
+        with self._lock:
+            N.check(N.lib().ev_server_submit_qasm(self._h, data, len(data), seed, shots,
+                                                  buf.ctypes.data, C.byref(rid)))
+            self._buffers[rid.value] = (buf, shots, None)
+        return rid.value
+
     def cancel(self, rid: int) -> None:
         N.check(N.lib().ev_server_cancel(self._h, rid))
 

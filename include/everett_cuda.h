@@ -40,6 +40,7 @@ enum {
   EV_ERR_CLASSICAL_BIT_OUT_OF_RANGE = 2, /* Error::ClassicalBitOutOfRange */
   EV_ERR_DUPLICATE_QUBIT = 3,            /* Error::DuplicateQubit         */
   EV_ERR_DIMENSION_MISMATCH = 4,         /* Error::DimensionMismatch      */
+  EV_ERR_QASM = 6,                       /* Error::Qasm (line:col in the message) */
   EV_ERR_INVALID_ARGUMENT = 16, /* null pointer, bad dtype, malformed op list */
   EV_ERR_OOM = 17,              /* device allocation refused              */
   EV_ERR_CUDA = 18,             /* a CUDA runtime call failed             */
@@ -269,6 +270,24 @@ int ev_prepared_launch(ev_prepared* p, uint64_t seed, uint8_t* classical_out);
 int ev_prepared_kernels(const ev_prepared* p, uint64_t* out); /* kernels per launch */
 int ev_prepared_destroy(ev_prepared* p);
 
+/* ---- OpenQASM 3 (src/qasm/mod.rs, parse.rs, emit.rs) -------------------------
+ * ev_qasm_parse replaces Circuit::from_qasm (src/circuit.rs:324, parse.rs:813):
+ * the same subset, circuit and errors.  On EV_ERR_QASM the message reads
+ * "OpenQASM 3 error at L:C: ..." and err_line / err_col (either may be NULL)
+ * receive L and C (0 when the reference reports no position).  The program
+ * owns its op records; ev_program_circuit gives a view valid until
+ * ev_program_free.  ev_qasm_emit replaces Circuit::to_qasm (emit.rs:17):
+ * *len receives the text's length; with buf non-NULL the text and a NUL are
+ * written if cap allows (EV_ERR_INVALID_ARGUMENT otherwise).  Gates without
+ * a stdgates.inc name and nested IfClassic are EV_ERR_QASM. */
+typedef struct ev_program ev_program;
+
+int ev_qasm_parse(const char* src, uint64_t len, ev_program** out, uint64_t* err_line,
+                  uint64_t* err_col);
+int ev_program_circuit(const ev_program* p, ev_circuit* out);
+int ev_program_free(ev_program* p);
+int ev_qasm_emit(const ev_circuit* c, char* buf, uint64_t cap, uint64_t* len);
+
 /* ---- serving (no reference counterpart) ------------------------------------
  * A continuous-batching request loop.  Requests are admitted in arrival
  * order while the state memory of admitted requests (2^n x 16 or 8 bytes)
@@ -313,6 +332,10 @@ int ev_server_create(const ev_server_options* opts, ev_server** out);
  * budget completes at once with EV_ERR_ADMISSION. */
 int ev_server_submit(ev_server* s, const ev_circuit* c, uint64_t seed, uint64_t shots,
                      uint64_t* shots_out, uint64_t* id);
+/* Submits OpenQASM 3 text (parsed at once with ev_qasm_parse's rules; a
+ * parse error is returned here as EV_ERR_QASM and nothing is queued). */
+int ev_server_submit_qasm(ev_server* s, const char* src, uint64_t len, uint64_t seed,
+                          uint64_t shots, uint64_t* shots_out, uint64_t* id);
 /* Cancels a request that has not been admitted yet. */
 int ev_server_cancel(ev_server* s, uint64_t id);
 /* Moves up to max finished results to out; waits up to wait_ms for one. */
