@@ -452,6 +452,13 @@ def extras_kernels(n: int, peak: float):
     rng = np.random.default_rng(3)
     g2 = Gate2(rng.normal(size=16) + 1j * rng.normal(size=16))
     out = {"fp64_fma_per_s_measured": float(f"{rate.value:.4g}")}
+    prng = np.random.default_rng(9)
+    zdiag = ["+" + "".join("Z" if b else "I" for b in prng.integers(0, 2, n)) for _ in range(8)]
+    # eight strings with one X part and one Y pattern (one pass), Z varying
+    xpart, ypart = prng.integers(0, 2, n), prng.integers(0, 2, n)
+    xshared = ["+" + "".join(("XY"[int(y)] if xb else "IZ"[int(b)])
+                             for xb, y, b in zip(xpart, ypart, prng.integers(0, 2, n)))
+               for _ in range(8)]
     for dtype, B in (("complex128", 16), ("complex64", 8)):
         st = State.zero(n, dtype)
         other = State.zero(n, dtype)
@@ -478,6 +485,8 @@ def extras_kernels(n: int, peak: float):
             ("normalize", lambda: st.normalize(), 3 * Nn * B, 4),
             ("overlap", lambda: st.overlap(other), 2 * Nn * B, 4),
             ("sample_1000_shots", lambda: st.sample(1000, seed=1), Nn * B + 16 * Nn, 3),
+            ("pauli_8_diagonal_terms", lambda: st.pauli_expectation(zdiag), Nn * B, 10),
+            ("pauli_8_terms_shared_x", lambda: st.pauli_expectation(xshared), Nn * B, 5),
         ]
         res = {}
         for name, fn, nbytes, fp64 in cases:

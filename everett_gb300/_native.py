@@ -91,6 +91,7 @@ _SIGS = {
     "ev_state_profile": [_P, _I32],
     "ev_state_profile_read": [_P, _P, _I32, C.POINTER(_I32)],
     "ev_batch_run": [_P, _U64, _P, _P],
+    "ev_pauli_expectation": [_P, _P, _P, _P, _U64, _P],
     "ev_qasm_parse": [C.c_char_p, _U64, C.POINTER(_P), C.POINTER(_U64), C.POINTER(_U64)],
     "ev_program_circuit": [_P, C.POINTER(EvCircuit)],
     "ev_program_free": [_P],

@@ -126,6 +126,11 @@ class State:
         N.check(N.lib().ev_bloch_vector(self._h, qubit, out))
         return [out[0], out[1], out[2]]
 
+    def pauli_expectation(self, paulis) -> np.ndarray:
+        """<psi|P|psi> for each Pauli string (PauliString or text like "+XZI")."""
+        from .observables import expectations
+        return expectations(self, paulis)
+
     def sample(self, shots: int, seed: int = 0) -> np.ndarray:
         """Full-register shots (bit q of each value = qubit q)."""
         out = np.empty(shots, dtype=np.uint64)

@@ -731,6 +731,188 @@ extern "C" int ev_bloch_vector(const ev_state* s, uint64_t qubit, double out[3])
   return EV_OK;
 }
 
+// ---- Pauli-string expectations (PauliString::expectation,
+// src/backend/stabilizer.rs:79-125) ------------------------------------------
+// The reference applies P to a copy of the state and takes Re <psi|P psi>.
+// Here terms that share an X mask x are summed in one pass without a copy:
+//   x == 0:  <P> = sign * sum_j s_j |a_j|^2
+//   x != 0:  pairs (j, j ^ x) with the highest bit of x clear in j, and
+//            w = conj(a_{j^x}) a_j;  with y = popc(x & z) (the Y count),
+//            y even: <P> = sign * (-1)^(y/2) * 2 sum s_j Re w
+//            y odd:  <P> = sign * (y % 4 == 1 ? -1 : 1) * 2 sum s_j Im w
+// where s_j = (-1)^popc(j & z).  Each pair is read once for all its terms.
+constexpr int kPauliTerms = 8;
+struct PauliPass {
+  uint64_t z[kPauliTerms];
+  int nterms;
+  int part;  // 0: |a_j|^2 (x == 0), 1: Re w, 2: Im w
+};
+
+template <typename V>
+__global__ void __launch_bounds__(kRedThreads)
+    k_pauli(const V* __restrict__ a, uint64_t count, uint64_t chunk, uint64_t xmask, int hbit,
+            PauliPass pp, double* __restrict__ partials) {
+  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
+  const uint64_t hi = lo + chunk < count ? lo + chunk : count;
+  double acc[kPauliTerms];
+#pragma unroll
+  for (int t = 0; t < kPauliTerms; ++t) acc[t] = 0.0;
+  for (uint64_t base = lo + threadIdx.x; base < hi; base += uint64_t(kFlush) * kRedThreads) {
+    FF f[kPauliTerms];
+#pragma unroll 2
+    for (int r = 0; r < kFlush; ++r) {
+      const uint64_t i = base + uint64_t(r) * kRedThreads;
+      if (i >= hi) break;
+      const uint64_t j = pp.part == 0 ? i : insert0(i, hbit);
+      const V x = a[j];
+      V y = x;
+      if (pp.part != 0) y = a[j ^ xmask];
+      if constexpr (sizeof(V) == 8) {
+        FF v;  // the term, exactly split: hi + lo
+        if (pp.part == 0) {
+          v.add_prod(x.x, x.x);
+          v.add_prod(x.y, x.y);
+        } else if (pp.part == 1) {
+          v.add_prod(y.x, x.x);
+          v.add_prod(y.y, x.y);
+        } else {
+          v.add_prod(y.x, x.y);
+          v.add_prod(-y.y, x.x);
+        }
+#pragma unroll
+        for (int t = 0; t < kPauliTerms; ++t)
+          if (t < pp.nterms) {
+            const bool neg = __popcll(j & pp.z[t]) & 1;
+            f[t].lo = __fadd_rn(f[t].lo, neg ? -v.lo : v.lo);
+            f[t].add(neg ? -v.hi : v.hi);
+          }
+      } else {
+        double v;
+        if (pp.part == 0)
+          v = __fma_rn(x.x, x.x, __dmul_rn(x.y, x.y));
+        else if (pp.part == 1)
+          v = __fma_rn(y.x, x.x, __dmul_rn(y.y, x.y));
+        else
+          v = __fma_rn(y.x, x.y, -__dmul_rn(y.y, x.x));
+#pragma unroll
+        for (int t = 0; t < kPauliTerms; ++t)
+          if (t < pp.nterms) acc[t] += (__popcll(j & pp.z[t]) & 1) ? -v : v;
+      }
+    }
+    if constexpr (sizeof(V) == 8) {
+#pragma unroll
+      for (int t = 0; t < kPauliTerms; ++t) acc[t] += f[t].value();
+    }
+  }
+  __shared__ double sh[kPauliTerms][kRedThreads];
+#pragma unroll
+  for (int t = 0; t < kPauliTerms; ++t) sh[t][threadIdx.x] = acc[t];
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+#pragma unroll
+      for (int t = 0; t < kPauliTerms; ++t) sh[t][threadIdx.x] += sh[t][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < kPauliTerms) partials[blockIdx.x * kPauliTerms + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// result[t] = sum over blocks of partials[b][t], fixed order.
+__global__ void __launch_bounds__(kRedThreads)
+    k_finish_terms(const double* __restrict__ partials, int nblocks, double* __restrict__ result) {
+  __shared__ double sh[kPauliTerms][kRedThreads];
+  double acc[kPauliTerms] = {};
+  for (int b = threadIdx.x; b < nblocks; b += kRedThreads)
+#pragma unroll
+    for (int t = 0; t < kPauliTerms; ++t) acc[t] += partials[b * kPauliTerms + t];
+#pragma unroll
+  for (int t = 0; t < kPauliTerms; ++t) sh[t][threadIdx.x] = acc[t];
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+#pragma unroll
+      for (int t = 0; t < kPauliTerms; ++t) sh[t][threadIdx.x] += sh[t][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < kPauliTerms) result[threadIdx.x] = sh[threadIdx.x][0];
+}
+
+extern "C" int ev_pauli_expectation(const ev_state* s, const uint64_t* x_masks,
+                                    const uint64_t* z_masks, const uint8_t* negative,
+                                    uint64_t count, double* out) {
+  clear_error();
+  if (!s || (count && (!x_masks || !z_masks || !out)))
+    return fail(EV_ERR_INVALID_ARGUMENT, "ev_pauli_expectation: null argument");
+  const uint64_t valid = s->n >= 64 ? ~uint64_t(0) : (uint64_t(1) << s->n) - 1;
+  for (uint64_t t = 0; t < count; ++t)
+    if ((x_masks[t] | z_masks[t]) & ~valid)
+      return fail(EV_ERR_QUBIT_OUT_OF_RANGE,
+                  "Pauli string %llu acts on a qubit outside the %llu-qubit register",
+                  (unsigned long long)t, (unsigned long long)s->n);
+  if (count == 0) return EV_OK;
+  EV_CUDA(cudaSetDevice(s->device));
+  // group terms by (X mask, parity of the Y count), first appearance first:
+  // one group shares its pairs and whether Re w or Im w is summed
+  auto key_par = [&](uint64_t t) {
+    return x_masks[t] ? (__builtin_popcountll(x_masks[t] & z_masks[t]) & 1) : 0;
+  };
+  std::vector<uint64_t> order;
+  order.reserve(count);
+  std::vector<char> used(count, 0);
+  for (uint64_t t = 0; t < count; ++t) {
+    if (used[t]) continue;
+    for (uint64_t u = t; u < count; ++u)
+      if (!used[u] && x_masks[u] == x_masks[t] && key_par(u) == key_par(t)) {
+        used[u] = 1;
+        order.push_back(u);
+      }
+  }
+  size_t at = 0;
+  while (at < order.size()) {
+    const uint64_t first = order[at];
+    const uint64_t x = x_masks[first];
+    const int par = key_par(first);
+    PauliPass pp{};
+    uint64_t terms[kPauliTerms];
+    while (at < order.size() && pp.nterms < kPauliTerms && x_masks[order[at]] == x &&
+           key_par(order[at]) == par) {
+      terms[pp.nterms] = order[at];
+      pp.z[pp.nterms] = z_masks[order[at]];
+      ++pp.nterms;
+      ++at;
+    }
+    pp.part = x == 0 ? 0 : (par ? 2 : 1);
+    const int hbit = x == 0 ? -1 : 63 - __builtin_clzll(x);
+    const uint64_t work = x == 0 ? s->len() : s->len() / 2;
+    int nb = 0;
+    uint64_t chunk = 0;
+    red_grid(work, s->num_sms, kMaxRedBlocks * 4 / kPauliTerms, &nb, &chunk);
+    if (s->dtype == EV_C128)
+      k_pauli<double2><<<nb, kRedThreads, 0, s->stream>>>(static_cast<const double2*>(s->amps), work,
+                                                           chunk, x, hbit, pp, s->scratch.partials);
+    else
+      k_pauli<float2><<<nb, kRedThreads, 0, s->stream>>>(static_cast<const float2*>(s->amps), work,
+                                                         chunk, x, hbit, pp, s->scratch.partials);
+    k_finish_terms<<<1, kRedThreads, 0, s->stream>>>(s->scratch.partials, nb, s->scratch.result);
+    s->launches += 2;
+    EV_CUDA(cudaGetLastError());
+    double r[kPauliTerms];
+    EV_TRY(fetch_result(s, r, kPauliTerms));
+    for (int t = 0; t < pp.nterms; ++t) {
+      const uint64_t id = terms[t];
+      const double sign = (negative && negative[id]) ? -1.0 : 1.0;
+      if (x == 0) {
+        out[id] = sign * r[t];
+      } else {
+        const int y = __builtin_popcountll(x & pp.z[t]);
+        const double f = (y & 1) ? ((y % 4 == 1) ? -1.0 : 1.0) : ((y % 4 == 0) ? 1.0 : -1.0);
+        out[id] = sign * f * 2.0 * r[t];
+      }
+    }
+  }
+  return EV_OK;
+}
+
 extern "C" int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* out) {
   clear_error();
   if (!s || (shots && !out)) return fail(EV_ERR_INVALID_ARGUMENT, "ev_sample: null argument");

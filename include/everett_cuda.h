@@ -205,6 +205,16 @@ int ev_run_seeded(const ev_circuit* c, uint64_t seed, const ev_run_options* opts
 int ev_state_run(ev_state* s, const ev_circuit* c, uint64_t seed,
                  const ev_run_options* opts, uint8_t* classical_out);
 
+/* <psi|P|psi> for Pauli strings (PauliString::expectation,
+ * src/backend/stabilizer.rs:79-125): term t is (-1)^negative[t] times the
+ * product over qubits q of X (bit q set in x_masks[t] only), Z (z_masks[t]
+ * only) or Y (both).  negative may be NULL (all +).  Terms sharing an X mask
+ * and the parity of their Y count are evaluated in one pass over the state
+ * (up to 8 per pass).  EV_ERR_QUBIT_OUT_OF_RANGE if a mask names a qubit
+ * outside the register. */
+int ev_pauli_expectation(const ev_state* s, const uint64_t* x_masks, const uint64_t* z_masks,
+                         const uint8_t* negative, uint64_t count, double* out);
+
 /* ---- shot sampling (no reference counterpart) ---------------------------
  * Shot j measures qubits 0..n-1 in order, each exactly as measure_qubit
  * would on the collapsed copy, with the uniforms of Rng::seed_from_u64(seed)

@@ -46,6 +46,7 @@ def lib(parallel: bool = False) -> C.CDLL:
         "oracle_normalize": ([P, U], None),
         "oracle_overlap": ([P, P, U, P], None),
         "oracle_bloch_vector": ([P, U, U, P], None),
+        "oracle_pauli_expectation": ([P, U, U, U, C.c_int], C.c_double),
         "oracle_rng_u64": ([U, U, P], None),
         "oracle_rng_f64": ([U, U, P], None),
         "oracle_validate": ([P], C.c_int),
@@ -110,6 +111,11 @@ def bloch_vector(amps: np.ndarray, q: int) -> list:
     out = np.zeros(3)
     lib().oracle_bloch_vector(amps.ctypes.data, amps.shape[0], q, out.ctypes.data)
     return out.tolist()
+
+
+def pauli_expectation(amps: np.ndarray, x_mask: int, z_mask: int, negative: bool = False) -> float:
+    n = amps.shape[0].bit_length() - 1
+    return lib().oracle_pauli_expectation(amps.ctypes.data, n, x_mask, z_mask, int(negative))
 
 
 def rng_u64(seed: int, count: int) -> np.ndarray:

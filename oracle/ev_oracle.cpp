@@ -374,6 +374,39 @@ void oracle_overlap(const double* self, const double* other, uint64_t len, doubl
   out[0] = acc.re;
   out[1] = acc.im;
 }
+// PauliString::expectation (backend/stabilizer.rs:79-125): P applied to a
+// copy (phase i^(#Y) times the sign, X flips, Z signs), then
+// Re <P psi | psi> by State::overlap.
+double oracle_pauli_expectation(const double* amps, uint64_t n, uint64_t xmask, uint64_t zmask,
+                                int negative) {
+  const C* a = reinterpret_cast<const C*>(amps);
+  const uint64_t dim = uint64_t(1) << n;
+  uint64_t ycount = 0;
+  for (uint64_t q = 0; q < n; ++q)
+    if (((xmask >> q) & 1) && ((zmask >> q) & 1)) ++ycount;
+  C phase{1.0, 0.0};
+  switch (ycount % 4) {
+    case 1: phase = C{0.0, 1.0}; break;
+    case 2: phase = C{-1.0, 0.0}; break;
+    case 3: phase = C{0.0, -1.0}; break;
+    default: break;
+  }
+  const double sign = negative ? -1.0 : 1.0;
+  const C factor = cscale(phase, sign);
+  std::vector<C> out(dim, C{0.0, 0.0});
+  for (uint64_t j = 0; j < dim; ++j) {
+    uint64_t target = j;
+    double zsign = 1.0;
+    for (uint64_t q = 0; q < n; ++q) {
+      if ((xmask >> q) & 1) target ^= uint64_t(1) << q;
+      if (((zmask >> q) & 1) && ((j >> q) & 1)) zsign = -zsign;
+    }
+    out[target] = cadd(out[target], cscale(cmul(a[j], factor), zsign));
+  }
+  double ov[2];
+  oracle_overlap(amps, reinterpret_cast<const double*>(out.data()), dim, ov);
+  return ov[0];
+}
 void oracle_bloch_vector(const double* amps, uint64_t len, uint64_t qubit, double* out) {
   const C* a = reinterpret_cast<const C*>(amps);
   const uint64_t bit = uint64_t(1) << qubit;

@@ -328,3 +328,23 @@ def test_sample_tree_matches_literal():
     amps, _, _ = O.run_seeded(algorithms.ghz(5))
     assert np.array_equal(O.sample_literal(amps, 2, 300), O.sample_tree(amps, 2, 300))
     assert set(O.sample_tree(amps, 2, 300).tolist()) <= {0, 31}
+
+
+def test_oracle_pauli_expectation_pins():
+    """PauliString::expectation (backend/stabilizer.rs:79-125): eigenstates of
+    X, Y and Z give +1, the wrong basis 0, a negative sign flips the value;
+    GHZ(3) is stabilised by XXX, ZZI and IZZ (tests/stabilizer.rs:13-25)."""
+    s2 = 1 / np.sqrt(2)
+    plus = np.array([s2, s2], dtype=complex)
+    y_plus = np.array([s2, 1j * s2], dtype=complex)
+    zero = np.array([1, 0], dtype=complex)
+    assert abs(O.pauli_expectation(plus, 1, 0) - 1) < 1e-15
+    assert abs(O.pauli_expectation(y_plus, 1, 1) - 1) < 1e-15
+    assert abs(O.pauli_expectation(zero, 0, 1) - 1) < 1e-15
+    assert abs(O.pauli_expectation(zero, 1, 0)) < 1e-15
+    assert abs(O.pauli_expectation(zero, 0, 1, True) + 1) < 1e-15
+    ghz = np.zeros(8, dtype=complex)
+    ghz[0] = ghz[7] = s2
+    for x, z in ((0b111, 0), (0, 0b011), (0, 0b110)):
+        assert abs(O.pauli_expectation(ghz, x, z) - 1) < 1e-15
+    assert abs(O.pauli_expectation(ghz, 0b111, 0b001)) < 1e-15  # <YXX> = 0 on GHZ(3)
