@@ -91,6 +91,18 @@ _SIGS = {
     "ev_state_profile": [_P, _I32],
     "ev_state_profile_read": [_P, _P, _I32, C.POINTER(_I32)],
     "ev_batch_run": [_P, _U64, _P, _P],
+    "ev_dm_create": [_U64, C.POINTER(_P)],
+    "ev_dm_destroy": [_P],
+    "ev_dm_num_qubits": [_P, C.POINTER(_U64)],
+    "ev_dm_from_amplitudes": [_P, _U64, C.POINTER(_P)],
+    "ev_dm_download": [_P, _P, _U64],
+    "ev_dm_get": [_P, _U64, _U64, _P],
+    "ev_dm_trace": [_P, _DP],
+    "ev_dm_purity": [_P, _DP],
+    "ev_dm_probability": [_P, _U64, _DP],
+    "ev_dm_expectation_pauli": [_P, _U64, C.c_char, _DP],
+    "ev_dm_partial_trace_1q": [_P, _U64, _P],
+    "ev_dm_run": [C.POINTER(EvCircuit), _P, _U64, C.POINTER(_P), _P],
     "ev_pauli_expectation": [_P, _P, _P, _P, _U64, _P],
     "ev_qasm_parse": [C.c_char_p, _U64, C.POINTER(_P), C.POINTER(_U64), C.POINTER(_U64)],
     "ev_program_circuit": [_P, C.POINTER(EvCircuit)],

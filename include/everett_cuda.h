@@ -263,6 +263,58 @@ typedef struct ev_batch_stats {
 int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const ev_batch_options* opts,
                  ev_batch_stats* stats);
 
+/* ---- density matrices (src/density.rs, src/noise.rs,
+ *      src/backend/density_matrix.rs) ------------------------------------------
+ * A 2^n x 2^n complex128 matrix resident in HBM, row-major (element (i, j) at
+ * i * 2^n + j).  Gates act as rho -> U rho U^dagger, channels as
+ * rho -> sum_k K_k rho K_k^dagger, with the reference's operation order, so
+ * results equal DensityMatrixBackend's bit for bit (signed zeros aside) until
+ * a measurement, whose probability sums agree to rounding.
+ *
+ * NoiseModel (noise.rs): after_1q follows every 1-qubit gate and, on the
+ * target then each control, every controlled gate; after_2q follows every
+ * 2-qubit gate on operand a, then b; readout_error flips a reported
+ * measurement bit with that probability (one more uniform per measurement
+ * when it is > 0).  A channel with nops == 0 is absent. */
+#define EV_MAX_KRAUS 16
+typedef struct ev_channel {
+  uint32_t nops;                  /* Kraus operators in k[0 .. nops)             */
+  uint32_t reserved;
+  double k[EV_MAX_KRAUS][8];      /* each a row-major 2x2, interleaved re, im     */
+} ev_channel;
+
+typedef struct ev_noise_model {
+  ev_channel after_1q;
+  ev_channel after_2q;
+  double readout_error;
+} ev_noise_model;
+
+typedef struct ev_dm ev_dm;
+
+/* |0...0><0...0| (DensityMatrix::zero, density.rs:46-58); EV_ERR_OOM when
+ * the 4^n elements cannot be stored. */
+int ev_dm_create(uint64_t n, ev_dm** out);
+int ev_dm_destroy(ev_dm* d);
+int ev_dm_num_qubits(const ev_dm* d, uint64_t* out);
+/* |psi><psi| (DensityMatrix::from_statevector, density.rs:66-82);
+ * EV_ERR_DIMENSION_MISMATCH unless len is a power of two. */
+int ev_dm_from_amplitudes(const double* amps, uint64_t len, ev_dm** out);
+int ev_dm_download(const ev_dm* d, double* data, uint64_t len); /* len = 4^n elements */
+int ev_dm_get(const ev_dm* d, uint64_t i, uint64_t j, double out[2]);
+int ev_dm_trace(const ev_dm* d, double* out);
+int ev_dm_purity(const ev_dm* d, double* out);
+int ev_dm_probability(const ev_dm* d, uint64_t basis, double* out);
+/* Tr(P rho) for P one of 'I', 'X', 'Y', 'Z' on one qubit (density.rs:236-266). */
+int ev_dm_expectation_pauli(const ev_dm* d, uint64_t qubit, char observable, double* out);
+/* The reduced 2x2 matrix of one qubit, [r00, r01, r10, r11] interleaved
+ * (density.rs:275-295). */
+int ev_dm_partial_trace_1q(const ev_dm* d, uint64_t qubit, double out[8]);
+/* DensityMatrixBackend::run_with_noise_seeded (density_matrix.rs:60-79):
+ * validate, |0..0><0..0|, Rng::seed_from_u64(seed), walk the ops; noise may
+ * be NULL (ideal). */
+int ev_dm_run(const ev_circuit* c, const ev_noise_model* noise, uint64_t seed, ev_dm** out,
+              uint8_t* classical_out);
+
 /* ---- prepared runs (no reference counterpart) ------------------------------
  * A circuit planned once for one state and recorded as a CUDA graph.  Each
  * launch replays the whole run with one graph launch: reset to |0...0>, the

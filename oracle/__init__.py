@@ -47,6 +47,9 @@ def lib(parallel: bool = False) -> C.CDLL:
         "oracle_overlap": ([P, P, U, P], None),
         "oracle_bloch_vector": ([P, U, U, P], None),
         "oracle_pauli_expectation": ([P, U, U, U, C.c_int], C.c_double),
+        "oracle_dm_run": ([P, P, U, P, P], C.c_int),
+        "oracle_dm_from_amplitudes": ([P, U, P], None),
+        "oracle_dm_observables": ([P, U, U, P], None),
         "oracle_rng_u64": ([U, U, P], None),
         "oracle_rng_f64": ([U, U, P], None),
         "oracle_validate": ([P], C.c_int),
@@ -116,6 +119,38 @@ def bloch_vector(amps: np.ndarray, q: int) -> list:
 def pauli_expectation(amps: np.ndarray, x_mask: int, z_mask: int, negative: bool = False) -> float:
     n = amps.shape[0].bit_length() - 1
     return lib().oracle_pauli_expectation(amps.ctypes.data, n, x_mask, z_mask, int(negative))
+
+
+def dm_run(circuit, noise=None, seed: int = 0):
+    """DensityMatrixBackend::run_with_noise_seeded: (rho [dim x dim], classical)."""
+    import ctypes as C_
+    c = circuit.ev_struct()
+    n = circuit.num_qubits()
+    dim = 1 << n
+    rho = np.zeros((dim, dim), dtype=np.complex128)
+    cl = np.zeros(max(1, circuit.num_classical()), dtype=np.uint8)
+    nz = C_.byref(noise) if noise is not None else None
+    rc = lib().oracle_dm_run(C_.addressof(c), nz, seed, rho.ctypes.data, cl.ctypes.data)
+    if rc:
+        raise ValueError(f"oracle validation error {rc}")
+    return rho, [bool(b) for b in cl[:circuit.num_classical()]]
+
+
+def dm_from_amplitudes(amps: np.ndarray) -> np.ndarray:
+    dim = amps.shape[0]
+    rho = np.zeros((dim, dim), dtype=np.complex128)
+    lib().oracle_dm_from_amplitudes(np.ascontiguousarray(amps).ctypes.data, dim, rho.ctypes.data)
+    return rho
+
+
+def dm_observables(rho: np.ndarray, qubit: int) -> dict:
+    """trace, purity, <I>, <X>, <Y>, <Z> on qubit, and its reduced 2x2 matrix."""
+    n = rho.shape[0].bit_length() - 1
+    out = np.zeros(14)
+    lib().oracle_dm_observables(np.ascontiguousarray(rho).ctypes.data, n, qubit, out.ctypes.data)
+    red = out[6:14].view(np.complex128)
+    return {"trace": out[0], "purity": out[1], "I": out[2], "X": out[3], "Y": out[4],
+            "Z": out[5], "reduced": red.copy()}
 
 
 def rng_u64(seed: int, count: int) -> np.ndarray:

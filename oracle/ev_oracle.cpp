@@ -22,6 +22,7 @@
 // iteration), so the parallel build produces bit-identical results.
 #include <cmath>
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
 #include <vector>
 
@@ -518,6 +519,251 @@ void oracle_sample_tree(const double* amps, uint64_t n, uint64_t seed, uint64_t 
       if (u < p1) r |= uint64_t(1) << q;
     }
     out[s] = r;
+  }
+}
+
+
+// ---- density matrices (src/density.rs, src/backend/density_matrix.rs) -------------
+// Row-major 2^n x 2^n; every loop below follows the reference's order.
+
+// index_group (density.rs:426-454): the 2^m indices whose non-target bits
+// encode g; target bits inserted in sorted order, combinations in `targets`
+// order.
+static std::vector<uint64_t> dm_index_group(const std::vector<uint64_t>& targets, uint64_t g) {
+  std::vector<uint64_t> sorted = targets;
+  std::sort(sorted.begin(), sorted.end());
+  uint64_t base = g;
+  for (uint64_t t : sorted) {
+    const uint64_t low = (uint64_t(1) << t) - 1;
+    base = ((base >> t) << (t + 1)) | (base & low);
+  }
+  const uint64_t gd = uint64_t(1) << targets.size();
+  std::vector<uint64_t> idx(gd);
+  for (uint64_t k = 0; k < gd; ++k) {
+    uint64_t v = base;
+    for (size_t b = 0; b < targets.size(); ++b)
+      if ((k >> b) & 1) v |= uint64_t(1) << targets[b];
+    idx[k] = v;
+  }
+  return idx;
+}
+
+// left_multiply (density.rs:348-378): out = U rho.
+static void dm_left(const std::vector<C>& rho, std::vector<C>& out, const std::vector<C>& u,
+                    const std::vector<uint64_t>& targets, uint64_t n) {
+  const uint64_t dim = uint64_t(1) << n, gd = uint64_t(1) << targets.size();
+  for (uint64_t col = 0; col < dim; ++col)
+    for (uint64_t g = 0; g < dim / gd; ++g) {
+      const std::vector<uint64_t> rows = dm_index_group(targets, g);
+      std::vector<C> in(gd);
+      for (uint64_t c = 0; c < gd; ++c) in[c] = rho[rows[c] * dim + col];
+      for (uint64_t r = 0; r < gd; ++r) {
+        C acc{0.0, 0.0};
+        for (uint64_t c = 0; c < gd; ++c) acc = cadd(acc, cmul(u[r * gd + c], in[c]));
+        out[rows[r] * dim + col] = acc;
+      }
+    }
+}
+
+// right_multiply_adjoint[_add] (density.rs:381-421): out (+)= tmp U^dagger.
+static void dm_right(const std::vector<C>& tmp, std::vector<C>& out, const std::vector<C>& u,
+                     const std::vector<uint64_t>& targets, uint64_t n, bool add) {
+  const uint64_t dim = uint64_t(1) << n, gd = uint64_t(1) << targets.size();
+  for (uint64_t row = 0; row < dim; ++row)
+    for (uint64_t g = 0; g < dim / gd; ++g) {
+      const std::vector<uint64_t> cols = dm_index_group(targets, g);
+      std::vector<C> in(gd);
+      for (uint64_t c = 0; c < gd; ++c) in[c] = tmp[row * dim + cols[c]];
+      for (uint64_t ci = 0; ci < gd; ++ci) {
+        C acc{0.0, 0.0};
+        for (uint64_t k = 0; k < gd; ++k) acc = cadd(acc, cmul(in[k], conj(u[ci * gd + k])));
+        C& dst = out[row * dim + cols[ci]];
+        dst = add ? cadd(dst, acc) : acc;
+      }
+    }
+}
+
+static void dm_unitary(std::vector<C>& rho, const std::vector<C>& u,
+                       const std::vector<uint64_t>& targets, uint64_t n) {
+  std::vector<C> out(rho.size(), C{0.0, 0.0});
+  dm_left(rho, out, u, targets, n);
+  dm_right(out, rho, u, targets, n, false);
+}
+
+// apply_channel (density.rs:195-215).
+static void dm_channel(std::vector<C>& rho, const ev_channel& ch, uint64_t target, uint64_t n) {
+  std::vector<C> acc(rho.size(), C{0.0, 0.0});
+  for (uint32_t k = 0; k < ch.nops; ++k) {
+    std::vector<C> u(4);
+    for (int e = 0; e < 4; ++e) u[e] = C{ch.k[k][2 * e], ch.k[k][2 * e + 1]};
+    std::vector<C> tmp(rho.size(), C{0.0, 0.0});
+    dm_left(rho, tmp, u, {target}, n);
+    dm_right(tmp, acc, u, {target}, n, true);
+  }
+  rho = acc;
+}
+
+static double dm_trace(const std::vector<C>& rho, uint64_t dim) {
+  double t = 0.0;
+  for (uint64_t i = 0; i < dim; ++i) t += rho[i * dim + i].re;
+  return t;
+}
+
+struct DmRun {
+  std::vector<C> rho;
+  uint64_t n;
+  const ev_noise_model* noise;
+  Rng rng;
+  uint8_t* classical;
+};
+
+// Backend for DensityMatrixBackend (density_matrix.rs:101-160).
+static void dm_apply_op(const ev_circuit* c, uint64_t* pos, DmRun* r) {
+  const ev_op& op = c->ops[*pos];
+  *pos += 1;
+  const uint64_t n = r->n, dim = uint64_t(1) << n;
+  const ev_noise_model* nz = r->noise;
+  switch (op.kind) {
+    case EV_OP_APPLY1: {
+      std::vector<C> u(4);
+      for (int e = 0; e < 4; ++e) u[e] = ld(op.m, e);
+      dm_unitary(r->rho, u, {op.q0}, n);
+      if (nz && nz->after_1q.nops) dm_channel(r->rho, nz->after_1q, op.q0, n);
+      return;
+    }
+    case EV_OP_APPLY2: {
+      std::vector<C> u(16);
+      for (int e = 0; e < 16; ++e) u[e] = ld(op.m, e);
+      dm_unitary(r->rho, u, {op.q1, op.q0}, n);
+      if (nz && nz->after_2q.nops) {
+        dm_channel(r->rho, nz->after_2q, op.q0, n);
+        dm_channel(r->rho, nz->after_2q, op.q1, n);
+      }
+      return;
+    }
+    case EV_OP_CONTROLLED: {
+      // controlled_unitary (density_matrix.rs:195-228): the full 2^n x 2^n matrix
+      uint64_t mask = 0;
+      for (uint32_t j = 0; j < op.nctrl; ++j) mask |= uint64_t(1) << c->ctrl_pool[op.ctrl_off + j];
+      std::vector<C> u(dim * dim, C{0.0, 0.0});
+      const uint64_t t = op.q0;
+      for (uint64_t col = 0; col < dim; ++col) {
+        if ((col & mask) == mask) {
+          const uint64_t partner = col ^ (uint64_t(1) << t);
+          if (((col >> t) & 1) == 0) {
+            u[col * dim + col] = ld(op.m, 0);
+            u[partner * dim + col] = ld(op.m, 2);
+          } else {
+            u[partner * dim + col] = ld(op.m, 1);
+            u[col * dim + col] = ld(op.m, 3);
+          }
+        } else {
+          u[col * dim + col] = C{1.0, 0.0};
+        }
+      }
+      std::vector<uint64_t> all(n);
+      for (uint64_t q = 0; q < n; ++q) all[q] = q;
+      dm_unitary(r->rho, u, all, n);
+      if (nz && nz->after_1q.nops) {
+        dm_channel(r->rho, nz->after_1q, t, n);
+        for (uint32_t j = 0; j < op.nctrl; ++j)
+          dm_channel(r->rho, nz->after_1q, c->ctrl_pool[op.ctrl_off + j], n);
+      }
+      return;
+    }
+    case EV_OP_MEASURE: {
+      const uint64_t bit = uint64_t(1) << op.q0;
+      double p1 = 0.0;  // measure_probability (density_matrix.rs:165-176)
+      for (uint64_t j = 0; j < dim; ++j)
+        if (j & bit) p1 += r->rho[j * dim + j].re;
+      const bool raw = r->rng.next_f64() < p1;
+      for (uint64_t i = 0; i < dim; ++i)  // collapse (density_matrix.rs:178-193)
+        for (uint64_t j = 0; j < dim; ++j) {
+          const bool im = ((i & bit) != 0) == raw, jm = ((j & bit) != 0) == raw;
+          if (!im || !jm) r->rho[i * dim + j] = C{0.0, 0.0};
+        }
+      const double t = dm_trace(r->rho, dim);  // renormalize (density.rs:218-226)
+      if (t > 0.0) {
+        const double inv = 1.0 / t;
+        for (C& x : r->rho) x = cscale(x, inv);
+      }
+      bool out = raw;
+      if (nz && nz->readout_error > 0.0 && r->rng.next_f64() < nz->readout_error) out = !raw;
+      r->classical[op.q1] = out ? 1 : 0;
+      return;
+    }
+    case EV_OP_IF: {
+      const bool take = r->classical[op.q0] != 0;
+      if (take) {
+        dm_apply_op(c, pos, r);
+      } else {  // skip the inner record (and any nested IF prefixes)
+        while (c->ops[*pos].kind == EV_OP_IF) *pos += 1;
+        *pos += 1;
+      }
+      return;
+    }
+  }
+}
+
+int oracle_dm_run(const ev_circuit* c, const ev_noise_model* noise, uint64_t seed, double* rho_out,
+                  uint8_t* classical_out) {
+  const int rc = oracle_validate(c);
+  if (rc) return rc;
+  const uint64_t n = c->num_qubits, dim = uint64_t(1) << n;
+  DmRun r{std::vector<C>(dim * dim, C{0.0, 0.0}), n, noise, Rng(seed), classical_out};
+  r.rho[0] = C{1.0, 0.0};
+  for (uint64_t j = 0; j < c->num_classical; ++j) classical_out[j] = 0;
+  uint64_t pos = 0;
+  while (pos < c->nops) dm_apply_op(c, &pos, &r);
+  std::memcpy(rho_out, r.rho.data(), dim * dim * sizeof(C));
+  return EV_OK;
+}
+
+void oracle_dm_from_amplitudes(const double* amps, uint64_t dim, double* rho_out) {
+  const C* a = reinterpret_cast<const C*>(amps);
+  C* rho = reinterpret_cast<C*>(rho_out);
+  for (uint64_t i = 0; i < dim; ++i)
+    for (uint64_t j = 0; j < dim; ++j) rho[i * dim + j] = cmul(a[i], conj(a[j]));
+}
+
+// trace, purity, expectation_pauli, partial_trace_1q (density.rs:117-295).
+void oracle_dm_observables(const double* rho_in, uint64_t n, uint64_t qubit, double* out) {
+  const C* rho = reinterpret_cast<const C*>(rho_in);
+  const uint64_t dim = uint64_t(1) << n, bit = uint64_t(1) << qubit;
+  std::vector<C> v(rho, rho + dim * dim);
+  out[0] = dm_trace(v, dim);
+  double pur = 0.0;
+  for (uint64_t i = 0; i < dim; ++i)
+    for (uint64_t j = 0; j < dim; ++j) pur += norm_sqr(rho[i * dim + j]);
+  out[1] = pur;
+  const char ops[4] = {'I', 'X', 'Y', 'Z'};
+  for (int o = 0; o < 4; ++o) {
+    C res{0.0, 0.0};
+    for (uint64_t i = 0; i < dim; ++i)
+      for (uint64_t j = 0; j < dim; ++j) {
+        if ((i & ~bit) != (j & ~bit)) continue;
+        const uint64_t iq = (i & bit) >> qubit, jq = (j & bit) >> qubit;
+        C p{0.0, 0.0};
+        switch (ops[o]) {
+          case 'I': p = iq == jq ? C{1.0, 0.0} : C{0.0, 0.0}; break;
+          case 'X': p = iq == jq ? C{0.0, 0.0} : C{1.0, 0.0}; break;
+          case 'Y': p = (iq == 0 && jq == 1) ? C{0.0, -1.0} : (iq == 1 && jq == 0) ? C{0.0, 1.0} : C{0.0, 0.0}; break;
+          default: p = (iq == 0 && jq == 0) ? C{1.0, 0.0} : (iq == 1 && jq == 1) ? C{-1.0, 0.0} : C{0.0, 0.0}; break;
+        }
+        if (p.re != 0.0 || p.im != 0.0) res = cadd(res, cmul(p, rho[j * dim + i]));
+      }
+    out[2 + o] = res.re;
+  }
+  C red[4] = {C{0, 0}, C{0, 0}, C{0, 0}, C{0, 0}};
+  for (uint64_t i = 0; i < dim; ++i)
+    for (uint64_t j = 0; j < dim; ++j) {
+      if ((i & ~bit) != (j & ~bit)) continue;
+      const uint64_t iq = (i & bit) >> qubit, jq = (j & bit) >> qubit;
+      red[iq * 2 + jq] = cadd(red[iq * 2 + jq], rho[i * dim + j]);
+    }
+  for (int e = 0; e < 4; ++e) {
+    out[6 + 2 * e] = red[e].re;
+    out[7 + 2 * e] = red[e].im;
   }
 }
 

@@ -348,3 +348,30 @@ def test_oracle_pauli_expectation_pins():
     for x, z in ((0b111, 0), (0, 0b011), (0, 0b110)):
         assert abs(O.pauli_expectation(ghz, x, z) - 1) < 1e-15
     assert abs(O.pauli_expectation(ghz, 0b111, 0b001)) < 1e-15  # <YXX> = 0 on GHZ(3)
+
+
+def test_oracle_density_matrix_pins():
+    """density.rs / density_matrix.rs / noise.rs tests, re-expressed: |0><0|
+    has trace 1 and purity 1; X flips it; the Bell state's diagonal matches
+    the statevector probabilities; noise keeps the trace at 1 and lowers the
+    purity; Kraus sets are complete."""
+    from everett_gb300 import Circuit
+    from everett_gb300.density import Channel, NoiseModel
+    c = Circuit(2)
+    c.h(0).cnot(0, 1)
+    rho, _ = O.dm_run(c)
+    ob = O.dm_observables(rho, 0)
+    assert abs(ob["trace"] - 1) < 1e-12 and abs(ob["purity"] - 1) < 1e-12
+    amps, _, _ = O.run_seeded(c)
+    assert np.max(np.abs(np.diag(rho).real - np.abs(amps) ** 2)) < 1e-12
+    x = Circuit(1)
+    x.x(0)
+    rx, _ = O.dm_run(x)
+    assert rx[1, 1] == 1 and rx[0, 0] == 0
+    noisy, _ = O.dm_run(c, NoiseModel.uniform_depolarizing(0.1).ev_struct())
+    ob = O.dm_observables(noisy, 1)
+    assert abs(ob["trace"] - 1) < 1e-10 and ob["purity"] < 1
+    for ch in (Channel.depolarizing(0.3), Channel.amplitude_damping(0.5),
+               Channel.phase_damping(0.9), Channel.bit_flip(0.2), Channel.dephasing(0.4)):
+        s = sum(np.conj(k.m.reshape(2, 2)).T @ k.m.reshape(2, 2) for k in ch.kraus_ops())
+        assert np.max(np.abs(s - np.eye(2))) < 1e-12
