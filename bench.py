@@ -66,9 +66,11 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--fuse-bits", type=int, default=5,
+                    help="qubits per fused unitary for --case fused (5 or 6)")
     ap.add_argument("--case", default="headline",
                     choices=["headline", "fused", "tiled64", "batch", "serve", "prepared",
-                             "kernels"],
+                             "kernels", "density"],
                     help="run one section alone (for profiling): the complex64 fused or tiled "
                          "path on the random-layer circuit, the TFIM batch, the serving mix, "
                          "prepared-graph replay, or each streaming kernel class alone")
@@ -520,6 +522,43 @@ def extras_kernels(n: int, peak: float):
     return out
 
 
+def extras_density():
+    """Noisy density-matrix runs (DensityMatrixBackend with uniform
+    depolarizing noise) on the GPU, against the oracle on the same circuit
+    structure at a size it finishes quickly; both as matrix-element updates
+    per second (ops x 4^n / time)."""
+    import ctypes as C
+
+    from everett_gb300 import _native as N, workloads
+    from everett_gb300.density import DensityMatrixBackend, NoiseModel
+    import oracle as O
+    nm = NoiseModel.uniform_depolarizing(0.001)
+    out = {}
+    for n in (12, 14):
+        c = workloads.random_layers(n, 4, seed=n)
+        DensityMatrixBackend.run_with_noise(c, nm)  # warm-up
+        t0 = time.perf_counter()
+        ex = DensityMatrixBackend.run_with_noise(c, nm)
+        ms = (time.perf_counter() - t0) * 1e3
+        rho = ex.density_matrix()
+        out[f"{n}q"] = {"ms_per_run": round(ms, 2), "ops": len(c),
+                        "element_updates_per_s": float(f"{len(c) * 4.0 ** n / (ms / 1e3):.4g}"),
+                        "trace": rho.trace(), "purity": rho.purity()}
+        del ex, rho
+    n = 7
+    c = workloads.random_layers(n, 4, seed=n)
+    t0 = time.perf_counter()
+    O.dm_run(c, nm.ev_struct())
+    cpu_s = time.perf_counter() - t0
+    out["oracle_cpu"] = {"qubits": n, "ms_per_run": round(cpu_s * 1e3, 2), "cores": 1,
+                         "element_updates_per_s": float(f"{len(c) * 4.0 ** n / cpu_s:.4g}"),
+                         "note": "the reference's loops restated (index groups, scratch "
+                                 "matrices); 1 core"}
+    out["workload"] = ("random-layer circuit depth 4 (Rz Ry Rz per qubit + CNOT bricks), "
+                       "depolarizing p=0.001 after every gate, complex128")
+    return out
+
+
 def run_ours(args, dist: Dist):
     import numpy as np
 
@@ -609,7 +648,8 @@ def run_ours(args, dist: Dist):
                             ("haar28_depth40", lambda: extras_haar(L, N)),
                             ("batch_tfim4096", extras_batch),
                             ("serve_mix", extras_serve),
-                            ("prepared_graph", extras_prepared)):
+                            ("prepared_graph", extras_prepared),
+                            ("density_noisy", extras_density)):
                 try:
                     extras[key] = fn()
                 except Exception as exc:  # report, do not hide
@@ -646,14 +686,16 @@ def run_case(args):
         peak, _ = measured_peaks()
         print(json.dumps({"case": "kernels", **extras_kernels(args.qubits, peak)}))
         return
-    if args.case in ("batch", "serve", "prepared"):
-        fn = {"batch": extras_batch, "serve": extras_serve, "prepared": extras_prepared}[args.case]
+    if args.case in ("batch", "serve", "prepared", "density"):
+        fn = {"batch": extras_batch, "serve": extras_serve, "prepared": extras_prepared,
+              "density": extras_density}[args.case]
         print(json.dumps({"case": args.case, **fn()}))
         return
     L = N.lib()
     c = workloads.random_layers(args.qubits, args.depth, seed=1)
     st = State.zero(args.qubits, "complex64")
-    kw = dict(mode="fused", variant=args.variant, tile_bits=5) if args.case == "fused" else dict(mode="tiled")
+    kw = (dict(mode="fused", variant=args.variant, tile_bits=args.fuse_bits) if args.case == "fused"
+          else dict(mode="tiled"))
     for _ in range(args.warmup):
         timed_runs(L, N, st, c, 1, **kw)
     ms, prof = timed_runs(L, N, st, c, args.steps, **kw)
