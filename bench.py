@@ -69,8 +69,8 @@ def parse_args():
     ap.add_argument("--fuse-bits", type=int, default=5,
                     help="qubits per fused unitary for --case fused (5 or 6)")
     ap.add_argument("--case", default="headline",
-                    choices=["headline", "fused", "tiled64", "batch", "serve", "prepared",
-                             "kernels", "density"],
+                    choices=["headline", "fused", "tiled64", "batch", "serve", "serve_small",
+                             "prepared", "kernels", "density"],
                     help="run one section alone (for profiling): the complex64 fused or tiled "
                          "path on the random-layer circuit, the TFIM batch, the serving mix, "
                          "prepared-graph replay, or each streaming kernel class alone")
@@ -291,6 +291,8 @@ def extras_c64(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, peak_kin
             "ms_per_run": round(ms, 2), "speedup_vs_complex128": round(c128_ms / ms, 1),
             "gate_GBps_complex128_equivalent": round(bytes_per_step / (ms / 1e3) / 1e9, 1),
             "fidelity_vs_complex128": fidelity(ref_state, st),
+            "max_abs_err_vs_complex128": ref_state.max_abs_diff(st),
+            "amplitude_updates_per_s": float(f"{len(circuit) * (1 << n) / (ms / 1e3):.4g}"),
             "roofline": roofline_of(prof, "fused_unitary", 2.0 * (1 << n) * 8, peak, peak_kind,
                                     f"k_fused_tc<5,{variant}> (fused 5-qubit unitary, tcgen05)",
                                     ncu_figure("k_fused_tc_bf16x3", "traffic_bytes_per_launch_full_size")
@@ -340,6 +342,7 @@ def extras_haar(L, N):
         ms, prof = timed_runs(L, N, st, c, 2, **kw)
         out[variant] = {"ms_per_run": round(ms, 1), "speedup_vs_complex128": round(ms128 / ms, 1),
                         "fidelity_vs_complex128": fidelity(ref, st),
+                        "max_abs_err_vs_complex128": ref.max_abs_diff(st),
                         "blocks": prof.get("fused_unitary", {}).get("launches", 0) // 2}
     return out
 
@@ -394,6 +397,58 @@ def extras_serve():
         srv.close()
         key = "saturated_all_at_once" if rate > 1e5 else f"poisson_{int(rate)}_per_s"
         out[key] = serve.latency_summary(res, wall)
+    return out
+
+
+def extras_serve_small():
+    """Continuous batching of small circuits: 2000 TFIM requests of 8-13
+    qubits (complex64, 1000 shots each) through the server, which runs the
+    small gate-only requests admitted together as one persistent batched
+    launch, against serving them one request at a time with one launch
+    sequence per circuit (run + sample)."""
+    import numpy as np
+
+    from everett_gb300 import CudaStateVectorBackend, Rng, State, serve, workloads
+    rng = Rng.seed_from_u64(99)
+    cs = [workloads.tfim_raw(rng, nmin=8, nmax=13) for _ in range(2000)]
+    requests = [(c, i, 1000) for i, c in enumerate(cs)]
+    states = {}
+    sample = cs[::8]
+    for c in sample[:8]:
+        n = c.num_qubits()
+        states.setdefault(n, State.zero(n, "complex64"))
+        CudaStateVectorBackend.run_into(states[n], c, 0, mode="tiled")
+    t0 = time.perf_counter()
+    lat = []
+    for c in sample:
+        n = c.num_qubits()
+        if n not in states:
+            states[n] = State.zero(n, "complex64")
+        t1 = time.perf_counter()
+        CudaStateVectorBackend.run_into(states[n], c, 0, mode="tiled")
+        states[n].sample(1000, seed=1)
+        lat.append((time.perf_counter() - t1) * 1e3)
+    base = len(sample) / (time.perf_counter() - t0)
+    out = {"workload": "2000 TFIM Trotter requests, 8-13 qubits, 10-50 steps, complex64, "
+                       "1000 shots each",
+           "one_request_at_a_time_one_launch_sequence_each": {
+               "circuits_per_s": round(base, 1),
+               "p50_ms_service": round(float(np.percentile(lat, 50)), 3),
+               "p99_ms_service": round(float(np.percentile(lat, 99)), 3)}}
+    srv = serve.Server(dtype="complex64", workers=4, mode="tiled")
+    try:
+        srv.run_all(requests[:64])
+        for rate in (2000.0, 1e6):
+            res, wall = serve.poisson_run(srv, requests, rate=rate, seed=int(rate) % 997)
+            key = "saturated_all_at_once" if rate > 1e5 else f"poisson_{int(rate)}_per_s"
+            summ = serve.latency_summary(res, wall)
+            summ["speedup_vs_one_at_a_time"] = round(summ["circuits_per_s"] / base, 1)
+            out[key] = summ
+        st = srv.stats()
+        out["batched_launches"] = st["batched_launches"]
+        out["batched_requests"] = st["batched_requests"]
+    finally:
+        srv.close()
     return out
 
 
@@ -648,6 +703,7 @@ def run_ours(args, dist: Dist):
                             ("haar28_depth40", lambda: extras_haar(L, N)),
                             ("batch_tfim4096", extras_batch),
                             ("serve_mix", extras_serve),
+                            ("serve_small_batched", extras_serve_small),
                             ("prepared_graph", extras_prepared),
                             ("density_noisy", extras_density)):
                 try:
@@ -669,6 +725,7 @@ def run_ours(args, dist: Dist):
                        "l2": f"inputs larger than L2 ({(1 << n) * 16 / 2**30:.1f} GiB state), "
                              f"no flush"},
             "pct_hbm_peak": round(100 * value / peak, 1),
+            "amplitude_updates_per_s": float(f"{len(circuit) * (1 << n) / (worst_ms / args.steps / 1e3):.4g}"),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(lc1.value - lc0.value),
             "clocks": clk.summary(),
@@ -686,9 +743,9 @@ def run_case(args):
         peak, _ = measured_peaks()
         print(json.dumps({"case": "kernels", **extras_kernels(args.qubits, peak)}))
         return
-    if args.case in ("batch", "serve", "prepared", "density"):
-        fn = {"batch": extras_batch, "serve": extras_serve, "prepared": extras_prepared,
-              "density": extras_density}[args.case]
+    if args.case in ("batch", "serve", "serve_small", "prepared", "density"):
+        fn = {"batch": extras_batch, "serve": extras_serve, "serve_small": extras_serve_small,
+              "prepared": extras_prepared, "density": extras_density}[args.case]
         print(json.dumps({"case": args.case, **fn()}))
         return
     L = N.lib()

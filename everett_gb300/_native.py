@@ -121,6 +121,7 @@ _SIGS = {
     "ev_server_stats_get": [_P, _P],
     "ev_server_destroy": [_P],
     "ev_probe_fp64": [_DP],
+    "ev_max_abs_diff": [_P, _P, _DP],
     "ev_host_alloc": [_U64, C.POINTER(_P)],
     "ev_host_free": [_P],
 }

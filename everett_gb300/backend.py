@@ -116,6 +116,12 @@ class State:
         N.check(N.lib().ev_overlap(self._h, other._h, out))
         return complex(out[0], out[1])
 
+    def max_abs_diff(self, other: "State") -> float:
+        """max_j |self_j - other_j| (either amplitude type), on the device."""
+        out = C.c_double()
+        N.check(N.lib().ev_max_abs_diff(self._h, other._h, C.byref(out)))
+        return out.value
+
     def fidelity(self, other: "State") -> float:
         out = C.c_double()
         N.check(N.lib().ev_fidelity(self._h, other._h, C.byref(out)))

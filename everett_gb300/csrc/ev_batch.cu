@@ -284,7 +284,39 @@ struct Arena {
   cudaStream_t stream = nullptr;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
 };
-Arena g_arena;
+// Arenas are leased one per concurrent call, so batched launches from
+// different host threads (the serving workers) run side by side on their own
+// streams instead of queueing on one arena.  Queue items wait only on earlier
+// items, which CTAs already running have taken, so kernels sharing the GPU
+// always drain.
+struct ArenaPool {
+  std::mutex mu;
+  std::vector<Arena*> free_list;
+};
+ArenaPool g_pool;
+
+Arena* acquire_arena(int dev) {
+  std::lock_guard<std::mutex> lock(g_pool.mu);
+  for (size_t i = 0; i < g_pool.free_list.size(); ++i)
+    if (g_pool.free_list[i]->device == dev) {
+      Arena* a = g_pool.free_list[i];
+      g_pool.free_list.erase(g_pool.free_list.begin() + long(i));
+      return a;
+    }
+  Arena* a = new Arena();
+  a->device = dev;
+  return a;
+}
+
+struct ArenaLease {
+  Arena* a;
+  ~ArenaLease() {
+    std::lock_guard<std::mutex> lock(g_pool.mu);
+    g_pool.free_list.push_back(a);
+  }
+};
+
+std::mutex g_cache_mu;  // the tuning cache file
 
 int grow_dev(void** p, size_t* cap, size_t need) {
   if (*cap >= need) return EV_OK;
@@ -455,20 +487,15 @@ int max_tile_bits(int dtype) { return dtype == EV_C128 ? 13 : 14; }
 }  // namespace
 
 // Runs one configuration; fills stats (device_ms, host_ms, items).
-static int batch_once(const ev_batch_circuit* items, uint64_t count, int dtype, int kmax,
+static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, int dtype, int kmax,
                       int threads, ev_batch_stats* st, bool stall = false) {
   using clk = std::chrono::steady_clock;
   const auto t0 = clk::now();
-  Arena& A = g_arena;
-  int dev = 0;
-  EV_CUDA(cudaGetDevice(&dev));
-  if (A.device != dev) {
-    A.device = dev;
-    if (!A.stream) {
-      EV_CUDA(cudaStreamCreateWithFlags(&A.stream, cudaStreamNonBlocking));
-      EV_CUDA(cudaEventCreate(&A.e0));
-      EV_CUDA(cudaEventCreate(&A.e1));
-    }
+  const int dev = A.device;
+  if (!A.stream) {
+    EV_CUDA(cudaStreamCreateWithFlags(&A.stream, cudaStreamNonBlocking));
+    EV_CUDA(cudaEventCreate(&A.e0));
+    EV_CUDA(cudaEventCreate(&A.e1));
   }
   int sms = 0;
   EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -688,14 +715,22 @@ extern "C" int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const
       return fail(EV_ERR_INVALID_ARGUMENT, "batch circuit %llu: shots requested without an output",
                   (unsigned long long)i);
   }
-  std::lock_guard<std::mutex> lock(g_arena.mu);
+  int dev = 0;
+  EV_CUDA(cudaGetDevice(&dev));
+  ArenaLease lease{acquire_arena(dev)};
+  Arena& A = *lease.a;
   int kbits = opts ? opts->tile_bits : 0, threads = opts ? opts->threads : 0;
   const int kcap = max_tile_bits(dtype);
   int from_cache = 0;
   if (kbits <= 0 || threads <= 0) {
     const std::string key = batch_key(items, count, dtype);
     int ck = 0, ct = 0;
-    if (cache_lookup(key, &ck, &ct)) {
+    bool cached;
+    {
+      std::lock_guard<std::mutex> cl(g_cache_mu);
+      cached = cache_lookup(key, &ck, &ct);
+    }
+    if (cached) {
       if (kbits <= 0) kbits = ck;
       if (threads <= 0) threads = ct;
       from_cache = 1;
@@ -718,8 +753,8 @@ extern "C" int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const
           if (kbits > 0 && kc != kbits) continue;
           if (threads > 0 && tc != threads) continue;
           ev_batch_stats s{};
-          int rc = batch_once(sample.data(), sample.size(), dtype, kc, tc, &s);
-          if (rc == EV_OK) rc = batch_once(sample.data(), sample.size(), dtype, kc, tc, &s);
+          int rc = batch_once(A, sample.data(), sample.size(), dtype, kc, tc, &s);
+          if (rc == EV_OK) rc = batch_once(A, sample.data(), sample.size(), dtype, kc, tc, &s);
           if (rc != EV_OK) {
             clear_error();
             continue;
@@ -730,7 +765,10 @@ extern "C" int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const
             bt = tc;
           }
         }
-      cache_store(key, bk, bt);
+      {
+        std::lock_guard<std::mutex> cl(g_cache_mu);
+        cache_store(key, bk, bt);
+      }
       if (kbits <= 0) kbits = bk;
       if (threads <= 0) threads = bt;
     }
@@ -741,7 +779,7 @@ extern "C" int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const
   if (kbits < 4) kbits = 4;
   if (threads != 256 && threads != 512)
     return fail(EV_ERR_INVALID_ARGUMENT, "batch: threads must be 256 or 512");
-  const int rc = batch_once(items, count, dtype, kbits, threads, stats,
+  const int rc = batch_once(A, items, count, dtype, kbits, threads, stats,
                             opts != nullptr && opts->test_stall != 0);
   if (rc == EV_OK && stats) stats->from_cache = from_cache;
   return rc;

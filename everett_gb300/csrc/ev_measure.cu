@@ -715,6 +715,78 @@ extern "C" int ev_fidelity(const ev_state* self, const ev_state* other, double* 
   return EV_OK;
 }
 
+// max_j |self_j - other_j| (modulus in f64; a max, so the order of the
+// reduction does not change the result).  The two states may hold different
+// amplitude types: the error of a complex64 run against complex128.
+template <typename VA, typename VB>
+__global__ void __launch_bounds__(kRedThreads)
+    k_maxdiff(const VA* __restrict__ a, const VB* __restrict__ b, uint64_t count, uint64_t chunk,
+              double* __restrict__ partials) {
+  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
+  const uint64_t hi = lo + chunk < count ? lo + chunk : count;
+  double m = 0.0;
+  for (uint64_t i = lo + threadIdx.x; i < hi; i += kRedThreads) {
+    const double dx = double(a[i].x) - double(b[i].x), dy = double(a[i].y) - double(b[i].y);
+    m = fmax(m, hypot(dx, dy));
+  }
+  __shared__ double sh[kRedThreads];
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partials[blockIdx.x] = sh[0];
+}
+
+__global__ void k_finish_max(const double* __restrict__ partials, int nblocks, double* result) {
+  __shared__ double sh[kRedThreads];
+  double m = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += kRedThreads) m = fmax(m, partials[b]);
+  sh[threadIdx.x] = m;
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + w]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) result[0] = sh[0];
+}
+
+extern "C" int ev_max_abs_diff(const ev_state* self, const ev_state* other, double* out) {
+  clear_error();
+  if (!self || !other || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_max_abs_diff: null argument");
+  if (self->n != other->n)
+    return fail(EV_ERR_DIMENSION_MISMATCH, "states must have equal qubit counts (%llu vs %llu)",
+                (unsigned long long)self->n, (unsigned long long)other->n);
+  EV_CUDA(cudaSetDevice(self->device));
+  EV_CUDA(cudaStreamSynchronize(other->stream));
+  int nb = 0;
+  uint64_t chunk = 0;
+  red_grid(self->len(), self->num_sms, kMaxRedBlocks, &nb, &chunk);
+  const bool a128 = self->dtype == EV_C128, b128 = other->dtype == EV_C128;
+  double* part = self->scratch.partials;
+  if (a128 && b128)
+    k_maxdiff<double2, double2><<<nb, kRedThreads, 0, self->stream>>>(
+        static_cast<const double2*>(self->amps), static_cast<const double2*>(other->amps),
+        self->len(), chunk, part);
+  else if (a128)
+    k_maxdiff<double2, float2><<<nb, kRedThreads, 0, self->stream>>>(
+        static_cast<const double2*>(self->amps), static_cast<const float2*>(other->amps),
+        self->len(), chunk, part);
+  else if (b128)
+    k_maxdiff<float2, double2><<<nb, kRedThreads, 0, self->stream>>>(
+        static_cast<const float2*>(self->amps), static_cast<const double2*>(other->amps),
+        self->len(), chunk, part);
+  else
+    k_maxdiff<float2, float2><<<nb, kRedThreads, 0, self->stream>>>(
+        static_cast<const float2*>(self->amps), static_cast<const float2*>(other->amps),
+        self->len(), chunk, part);
+  k_finish_max<<<1, kRedThreads, 0, self->stream>>>(part, nb, self->scratch.result);
+  self->launches += 2;
+  EV_CUDA(cudaGetLastError());
+  return fetch_result(self, out, 1);
+}
+
 extern "C" int ev_bloch_vector(const ev_state* s, uint64_t qubit, double out[3]) {
   clear_error();
   if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_bloch_vector: null argument");

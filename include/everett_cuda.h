@@ -430,6 +430,9 @@ int ev_state_profile_read(ev_state* s, ev_kernel_stat* out, int32_t max, int32_t
  * second, from independent FMA chains on every SM): the roofline of the
  * complex128 kernels, whose arithmetic is FP64. */
 int ev_probe_fp64(double* fma_per_s);
+/* max_j |self_j - other_j| over two states of equal size, either amplitude
+ * type (the max amplitude error of a complex64 run against complex128). */
+int ev_max_abs_diff(const ev_state* self, const ev_state* other, double* out);
 
 int ev_host_alloc(uint64_t bytes, void** out); /* page-locked host memory */
 int ev_host_free(void* p);

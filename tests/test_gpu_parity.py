@@ -168,6 +168,24 @@ def test_complex64_reductions_match_oracle(gpu):
     assert abs(st.norm_sqr() - want) < 1e-14
 
 
+def test_max_abs_diff_matches_host(gpu):
+    """ev_max_abs_diff (either amplitude type) equals the host maximum to
+    1e-15 relative (the device and host hypot may differ in the last bit)."""
+    def close(x, y):
+        return abs(x - y) <= 1e-15 * max(abs(y), 1e-300)
+
+    for n in (1, 5, 13):
+        amps, _, _ = O.run_seeded(workloads.random_layers(n, 3, seed=n))
+        other, _, _ = O.run_seeded(workloads.random_layers(n, 3, seed=n + 1))
+        a, b = State.from_amplitudes(amps), State.from_amplitudes(other)
+        assert close(a.max_abs_diff(b), np.max(np.abs(amps - other)))
+        c = State.from_amplitudes(amps, dtype="complex64")
+        c32 = c.amplitudes()
+        assert close(a.max_abs_diff(c), np.max(np.abs(amps - c32)))
+        assert close(c.max_abs_diff(a), np.max(np.abs(c32 - amps)))
+        assert a.max_abs_diff(a) == 0.0
+
+
 def test_complex64_shots_match_tree(gpu):
     """complex64 sampling: the tree's leaves are double-float sums rounded to
     f64 once, so shots equal the oracle's tree on the same amplitudes except
