@@ -682,6 +682,20 @@ def run_ours(args, dist: Dist):
     roofline = roofline_of(prof, "tile_pass", 2.0 * (1 << n) * 16, peak, peak_kind,
                            "k_tile<double2> (shared-memory tile pass, complex128)",
                            ncu_figure("k_tile_c128", "traffic_bytes_per_launch_full_size"))
+    fp64 = None
+    if roofline is not None:
+        rate = C.c_double()
+        N.check(L.ev_probe_fp64(C.byref(rate)))
+        instr = workloads.fp64_instructions(circuit)
+        tile_ms = prof.get("tile_pass", {}).get("ms", 0.0) / max(1, args.steps)
+        if tile_ms > 0:
+            achieved = instr / (tile_ms / 1e3)
+            fp64 = {"instructions_per_step": float(f"{instr:.4g}"),
+                    "achieved_per_s": float(f"{achieved:.4g}"),
+                    "peak_per_s": float(f"{rate.value:.4g}"),
+                    "peak_source": "measured (ev_probe_fp64: sustained FP64 FMA issue rate)",
+                    "frac": round(achieved / rate.value, 3)}
+            roofline["fp64"] = fp64
     if roofline is not None:
         roofline["note"] = ("compute-bound on the FP64 pipe (GB300 issues FP64 at 1/64 of the "
                             "FP32 rate); ncu: fp64 pipe busy "

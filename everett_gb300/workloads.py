@@ -169,6 +169,53 @@ def gate_bytes(circuit: Circuit, amp_bytes: int = 16) -> int:
     return sum(op_bytes(op, n, amp_bytes) for op in circuit.ops())
 
 
+def _kind1(m) -> str:
+    """The engine's 1-qubit classification (exact 0/1 tests, as classify1)."""
+    off0 = m[1] == 0 and m[2] == 0
+    if off0:
+        if m[0] == 1 and m[3] == 1:
+            return "ident"
+        return "phase" if m[0] == 1 else "diag"
+    if m[0] == 0 and m[3] == 0:
+        return "anti"
+    if all(complex(z).imag == 0 for z in m):
+        return "real"
+    return "dense"
+
+
+# FP64 instructions per amplitude the op touches, from the kernels' source:
+# a complex product in the reference's FMA form is 4 (2 mul + 2 fma), a
+# complex add 2, a real-times-complex product 2.
+_FP64_1Q = {"dense": 10, "real": 6, "diag": 4, "phase": 4, "anti": 4, "ident": 0}
+
+
+def fp64_instructions(circuit: Circuit) -> float:
+    """FP64 instructions a complex128 run of the circuit issues, summed over
+    its gates (measurements excluded): the roofline of the exact path."""
+    from .circuit import Apply1, Apply2, Controlled, IfClassic
+    n = circuit.num_qubits()
+    dim = float(1 << n)
+    total = 0.0
+    for op in circuit.ops():
+        while isinstance(op, IfClassic):
+            op = op.then
+        if isinstance(op, Apply1):
+            k = _kind1(op.gate.m)
+            total += _FP64_1Q[k] * (dim / 2 if k == "phase" else dim)
+        elif isinstance(op, Controlled):
+            k = _kind1(op.gate.m)
+            frac = dim / (1 << len(set(op.controls)))
+            total += _FP64_1Q[k] * (frac / 2 if k == "phase" else frac)
+        elif isinstance(op, Apply2):
+            m = op.gate.m.reshape(4, 4)
+            off = m - np.diag(np.diag(m))
+            perm = bool(np.all((m == 0) | (m == 1) | (m == -1)))
+            if perm:
+                continue
+            total += (4 if not np.any(off) else 22) * dim
+    return total
+
+
 class RawCircuit:
     """A gate-only circuit held directly as C ABI op records (for large
     generated workloads where building Python op objects would dominate)."""
