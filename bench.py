@@ -70,7 +70,7 @@ def parse_args():
                     help="qubits per fused unitary for --case fused (5 or 6)")
     ap.add_argument("--case", default="headline",
                     choices=["headline", "fused", "tiled64", "batch", "serve", "serve_small",
-                             "prepared", "kernels", "density"],
+                             "prepared", "kernels", "density", "stabilizer"],
                     help="run one section alone (for profiling): the complex64 fused or tiled "
                          "path on the random-layer circuit, the TFIM batch, the serving mix, "
                          "prepared-graph replay, or each streaming kernel class alone")
@@ -614,6 +614,46 @@ def extras_density():
     return out
 
 
+def extras_stabilizer():
+    """Random Clifford circuits with mid-circuit measurements on the GPU
+    tableau, against the oracle (the reference's tableau loops) on the same
+    circuit."""
+    from everett_gb300 import Circuit, Rng
+    from everett_gb300.stabilizer import StabilizerBackend
+    import oracle as O
+
+    def circuit(n, gates, meas, seed):
+        rng = Rng.seed_from_u64(seed)
+        c = Circuit.with_classical(n, n)
+        every = max(1, gates // max(1, meas))
+        for k in range(gates):
+            a = int(rng.next_u64() % n)
+            b = (a + 1 + int(rng.next_u64() % (n - 1))) % n
+            [lambda: c.h(a), lambda: c.s(a), lambda: c.cnot(a, b), lambda: c.cz(a, b)][k % 4]()
+            if k % every == every - 1:
+                c.measure(a, a)
+        return c
+
+    out = {"workload": "random H / S / CNOT / CZ circuit with a measurement every gates/meas gates"}
+    for n, gates, meas in ((1000, 20000, 200), (4000, 40000, 100)):
+        c = circuit(n, gates, meas, n)
+        c.to_ev()  # the op records are encoded once, outside the timed region
+        StabilizerBackend.run_seeded(circuit(64, 200, 4, 1), 0)
+        t0 = time.perf_counter()
+        ex = StabilizerBackend.run_seeded(c, 7)
+        ms = (time.perf_counter() - t0) * 1e3
+        row = {"gpu_ms": round(ms, 1), "gates": gates, "measurements": meas}
+        if n <= 1000:
+            t0 = time.perf_counter()
+            want = O.stab_run(c, 7)
+            cpu_ms = (time.perf_counter() - t0) * 1e3
+            row["oracle_cpu_ms_1_core"] = round(cpu_ms, 1)
+            row["speedup"] = round(cpu_ms / ms, 1)
+            row["classical_equal"] = ex.classical() == want[3]
+        out[f"{n}q"] = row
+    return out
+
+
 def run_ours(args, dist: Dist):
     import numpy as np
 
@@ -719,7 +759,8 @@ def run_ours(args, dist: Dist):
                             ("serve_mix", extras_serve),
                             ("serve_small_batched", extras_serve_small),
                             ("prepared_graph", extras_prepared),
-                            ("density_noisy", extras_density)):
+                            ("density_noisy", extras_density),
+                            ("stabilizer", extras_stabilizer)):
                 try:
                     extras[key] = fn()
                 except Exception as exc:  # report, do not hide
@@ -757,9 +798,10 @@ def run_case(args):
         peak, _ = measured_peaks()
         print(json.dumps({"case": "kernels", **extras_kernels(args.qubits, peak)}))
         return
-    if args.case in ("batch", "serve", "serve_small", "prepared", "density"):
+    if args.case in ("batch", "serve", "serve_small", "prepared", "density", "stabilizer"):
         fn = {"batch": extras_batch, "serve": extras_serve, "serve_small": extras_serve_small,
-              "prepared": extras_prepared, "density": extras_density}[args.case]
+              "prepared": extras_prepared, "density": extras_density,
+              "stabilizer": extras_stabilizer}[args.case]
         print(json.dumps({"case": args.case, **fn()}))
         return
     L = N.lib()

@@ -32,6 +32,7 @@ ERR_QUBIT_OUT_OF_RANGE = 1
 ERR_CLASSICAL_BIT_OUT_OF_RANGE = 2
 ERR_DUPLICATE_QUBIT = 3
 ERR_DIMENSION_MISMATCH = 4
+ERR_NON_CLIFFORD = 5
 ERR_QASM = 6
 ERR_INVALID_ARGUMENT = 16
 ERR_OOM = 17
@@ -91,6 +92,10 @@ _SIGS = {
     "ev_state_profile": [_P, _I32],
     "ev_state_profile_read": [_P, _P, _I32, C.POINTER(_I32)],
     "ev_batch_run": [_P, _U64, _P, _P],
+    "ev_stab_run": [C.POINTER(EvCircuit), _U64, C.POINTER(_P), _P],
+    "ev_stab_num_qubits": [_P, C.POINTER(_U64)],
+    "ev_stab_generators": [_P, _P, _P, _P],
+    "ev_stab_destroy": [_P],
     "ev_dm_create": [_U64, C.POINTER(_P)],
     "ev_dm_destroy": [_P],
     "ev_dm_num_qubits": [_P, C.POINTER(_U64)],

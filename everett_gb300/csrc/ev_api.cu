@@ -512,8 +512,9 @@ extern "C" int ev_state_create(uint64_t n, int32_t dtype, ev_state** out) {
   return create_state(n, dtype, out);
 }
 
+// Destroying never fails and leaves the last error message in place (a run
+// that fails frees its own state before returning the error).
 extern "C" int ev_state_destroy(ev_state* s) {
-  clear_error();
   if (!s) return EV_OK;
   cudaSetDevice(s->device);
   cudaStreamSynchronize(s->stream);

@@ -609,8 +609,9 @@ extern "C" int ev_dm_create(uint64_t n, ev_dm** out) {
   return rc;
 }
 
+// Destroying never fails and leaves the last error message in place (a run
+// that fails frees its own state before returning the error).
 extern "C" int ev_dm_destroy(ev_dm* d) {
-  clear_error();
   if (!d) return EV_OK;
   cudaSetDevice(d->device);
   cudaStreamSynchronize(d->stream);

@@ -31,6 +31,13 @@ class DimensionMismatch(EverettError):
     code = N.ERR_DIMENSION_MISMATCH
 
 
+class NonClifford(EverettError):
+    """Error::NonClifford (src/error.rs:38-43): the stabilizer backend met a
+    gate outside the Clifford group."""
+
+    code = N.ERR_NON_CLIFFORD
+
+
 class QasmError(EverettError):
     """Error::Qasm { line, col, message } (src/error.rs:45-52); str() reads
     "OpenQASM 3 error at L:C: message" as the reference's Display does."""
@@ -74,7 +81,8 @@ class Cancelled(EverettError):
 
 
 _BY_CODE = {cls.code: cls for cls in (
-    QubitOutOfRange, ClassicalBitOutOfRange, DuplicateQubit, DimensionMismatch, QasmError,
+    QubitOutOfRange, ClassicalBitOutOfRange, DuplicateQubit, DimensionMismatch, NonClifford,
+    QasmError,
     InvalidArgument,
     DeviceOutOfMemory, CudaError, DeviceTimeout, AdmissionRefused, Cancelled)}
 

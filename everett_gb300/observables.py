@@ -23,8 +23,8 @@ class PauliString:
     def __init__(self, x, z, neg: bool = False):
         if len(x) != len(z):
             raise ValueError("x and z must have one bit per qubit")
-        self.x = [bool(b) for b in x]
-        self.z = [bool(b) for b in z]
+        self.x = np.asarray(x, dtype=bool).copy()
+        self.z = np.asarray(z, dtype=bool).copy()
         self.neg = bool(neg)
 
     @classmethod
@@ -45,23 +45,23 @@ class PauliString:
         return self.neg
 
     def pauli(self, q: int) -> str:
-        return {(False, False): "I", (True, False): "X", (False, True): "Z",
-                (True, True): "Y"}[(self.x[q], self.z[q])]
+        return "IZXY"[2 * int(self.x[q]) + int(self.z[q])]
 
     def masks(self) -> tuple:
-        xm = sum(1 << q for q, b in enumerate(self.x) if b)
-        zm = sum(1 << q for q, b in enumerate(self.z) if b)
+        xm = sum(1 << int(q) for q in np.flatnonzero(self.x))
+        zm = sum(1 << int(q) for q in np.flatnonzero(self.z))
         return xm, zm
 
     def __str__(self):
-        return ("-" if self.neg else "+") + "".join(self.pauli(q) for q in range(len(self.x)))
+        codes = np.array(list("IZXY"))[2 * self.x.astype(int) + self.z.astype(int)]
+        return ("-" if self.neg else "+") + "".join(codes.tolist())
 
     def __repr__(self):
         return f"PauliString({str(self)!r})"
 
     def __eq__(self, other):
-        return (isinstance(other, PauliString) and self.x == other.x and self.z == other.z
-                and self.neg == other.neg)
+        return (isinstance(other, PauliString) and np.array_equal(self.x, other.x)
+                and np.array_equal(self.z, other.z) and self.neg == other.neg)
 
     def expectation(self, state) -> float:
         if state.num_qubits() != self.num_qubits():

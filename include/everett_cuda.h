@@ -40,6 +40,7 @@ enum {
   EV_ERR_CLASSICAL_BIT_OUT_OF_RANGE = 2, /* Error::ClassicalBitOutOfRange */
   EV_ERR_DUPLICATE_QUBIT = 3,            /* Error::DuplicateQubit         */
   EV_ERR_DIMENSION_MISMATCH = 4,         /* Error::DimensionMismatch      */
+  EV_ERR_NON_CLIFFORD = 5,               /* Error::NonClifford            */
   EV_ERR_QASM = 6,                       /* Error::Qasm (line:col in the message) */
   EV_ERR_INVALID_ARGUMENT = 16, /* null pointer, bad dtype, malformed op list */
   EV_ERR_OOM = 17,              /* device allocation refused              */
@@ -314,6 +315,22 @@ int ev_dm_partial_trace_1q(const ev_dm* d, uint64_t qubit, double out[8]);
  * be NULL (ideal). */
 int ev_dm_run(const ev_circuit* c, const ev_noise_model* noise, uint64_t seed, ev_dm** out,
               uint8_t* classical_out);
+
+/* ---- stabilizer tableau (src/backend/stabilizer.rs) -------------------------
+ * StabilizerBackend::run_seeded: a Clifford circuit on an Aaronson-Gottesman
+ * tableau held bit-packed in HBM.  Gates are recognised up to global phase as
+ * the reference does (H, S, S^dagger, X, Y, Z; CNOT, CZ, SWAP; singly
+ * controlled X and Z); any other gate makes the run fail with
+ * EV_ERR_NON_CLIFFORD after the op walk, as the reference's poisoned backend
+ * does.  A random measurement outcome is next_u64() & 1 of the seeded Rng. */
+typedef struct ev_stab ev_stab;
+
+int ev_stab_run(const ev_circuit* c, uint64_t seed, ev_stab** out, uint8_t* classical_out);
+int ev_stab_num_qubits(const ev_stab* t, uint64_t* out);
+/* The n stabilizer generators (StabilizerExecution::generators): x and z are
+ * n x n bytes, row i = generator i, column q = qubit q; neg[i] = 1 for sign -1. */
+int ev_stab_generators(const ev_stab* t, uint8_t* x, uint8_t* z, uint8_t* neg);
+int ev_stab_destroy(ev_stab* t);
 
 /* ---- prepared runs (no reference counterpart) ------------------------------
  * A circuit planned once for one state and recorded as a CUDA graph.  Each

@@ -50,6 +50,7 @@ def lib(parallel: bool = False) -> C.CDLL:
         "oracle_dm_run": ([P, P, U, P, P], C.c_int),
         "oracle_dm_from_amplitudes": ([P, U, P], None),
         "oracle_dm_observables": ([P, U, U, P], None),
+        "oracle_stab_run": ([P, U, P, P, P, P], C.c_int),
         "oracle_rng_u64": ([U, U, P], None),
         "oracle_rng_f64": ([U, U, P], None),
         "oracle_validate": ([P], C.c_int),
@@ -151,6 +152,23 @@ def dm_observables(rho: np.ndarray, qubit: int) -> dict:
     red = out[6:14].view(np.complex128)
     return {"trace": out[0], "purity": out[1], "I": out[2], "X": out[3], "Y": out[4],
             "Z": out[5], "reduced": red.copy()}
+
+
+def stab_run(circuit, seed: int = 0):
+    """StabilizerBackend::run_seeded: (x [n x n], z [n x n], neg [n], classical),
+    or the error code (EV_ERR_NON_CLIFFORD = 5) as an int."""
+    import ctypes as C_
+    c = circuit.ev_struct()
+    n = circuit.num_qubits()
+    x = np.zeros((max(1, n), max(1, n)), dtype=np.uint8)
+    z = np.zeros_like(x)
+    neg = np.zeros(max(1, n), dtype=np.uint8)
+    cl = np.zeros(max(1, circuit.num_classical()), dtype=np.uint8)
+    rc = lib().oracle_stab_run(C_.addressof(c), seed, x.ctypes.data, z.ctypes.data,
+                               neg.ctypes.data, cl.ctypes.data)
+    if rc:
+        return rc
+    return x[:n, :n], z[:n, :n], neg[:n], [bool(b) for b in cl[:circuit.num_classical()]]
 
 
 def rng_u64(seed: int, count: int) -> np.ndarray:

@@ -767,4 +767,270 @@ void oracle_dm_observables(const double* rho_in, uint64_t n, uint64_t qubit, dou
   }
 }
 
+
+// ---- stabilizer tableau (src/backend/stabilizer.rs) ---------------------------
+
+enum StPrim { SP_H, SP_S, SP_SDG, SP_X, SP_Y, SP_Z, SP_CNOT };
+struct StOp {
+  StPrim k;
+  uint64_t a, b;
+};
+
+struct Tableau {
+  uint64_t n;
+  std::vector<std::vector<uint8_t>> x, z;
+  std::vector<uint8_t> r;
+  Rng rng;
+  int error = 0;
+  Tableau(uint64_t n_, uint64_t seed) : n(n_), rng(seed) {  // identity (stabilizer.rs:231-250)
+    const uint64_t rows = 2 * n + 1;
+    x.assign(rows, std::vector<uint8_t>(n, 0));
+    z.assign(rows, std::vector<uint8_t>(n, 0));
+    r.assign(rows, 0);
+    for (uint64_t i = 0; i < n; ++i) {
+      x[i][i] = 1;
+      z[n + i][i] = 1;
+    }
+  }
+  void prim(const StOp& p) {  // stabilizer.rs:254-320
+    const uint64_t a = p.a, b = p.b;
+    for (uint64_t i = 0; i < 2 * n; ++i) {
+      switch (p.k) {
+        case SP_H: {
+          r[i] ^= x[i][a] & z[i][a];
+          std::swap(x[i][a], z[i][a]);
+          break;
+        }
+        case SP_S:
+          r[i] ^= x[i][a] & z[i][a];
+          z[i][a] ^= x[i][a];
+          break;
+        case SP_SDG:
+          r[i] ^= x[i][a] & z[i][a];
+          z[i][a] ^= x[i][a];
+          r[i] ^= x[i][a];
+          break;
+        case SP_X: r[i] ^= z[i][a]; break;
+        case SP_Y: r[i] ^= x[i][a] ^ z[i][a]; break;
+        case SP_Z: r[i] ^= x[i][a]; break;
+        case SP_CNOT:
+          r[i] ^= x[i][a] & z[i][b] & (x[i][b] ^ z[i][a] ^ 1);
+          x[i][b] ^= x[i][a];
+          z[i][a] ^= z[i][b];
+          break;
+      }
+    }
+  }
+  static int g(int x1, int z1, int x2, int z2) {  // stabilizer.rs:381-390
+    if (!x1 && !z1) return 0;
+    if (x1 && z1) return z2 - x2;
+    if (x1) return z2 * (2 * x2 - 1);
+    return x2 * (1 - 2 * z2);
+  }
+  void rowsum(uint64_t h, uint64_t j) {  // stabilizer.rs:366-378
+    int sum = 2 * r[h] + 2 * r[j];
+    for (uint64_t q = 0; q < n; ++q) sum += g(x[j][q], z[j][q], x[h][q], z[h][q]);
+    r[h] = (((sum % 4) + 4) % 4) == 2;
+    for (uint64_t q = 0; q < n; ++q) {
+      x[h][q] ^= x[j][q];
+      z[h][q] ^= z[j][q];
+    }
+  }
+  bool measure(uint64_t q) {  // stabilizer.rs:322-364
+    uint64_t p = 2 * n;
+    for (uint64_t i = n; i < 2 * n; ++i)
+      if (x[i][q]) {
+        p = i;
+        break;
+      }
+    if (p < 2 * n) {
+      for (uint64_t i = 0; i < 2 * n; ++i)
+        if (i != p && x[i][q]) rowsum(i, p);
+      x[p - n] = x[p];
+      z[p - n] = z[p];
+      r[p - n] = r[p];
+      std::fill(x[p].begin(), x[p].end(), 0);
+      std::fill(z[p].begin(), z[p].end(), 0);
+      const bool outcome = (rng.next_u64() & 1) == 1;
+      r[p] = outcome;
+      z[p][q] = 1;
+      return outcome;
+    }
+    const uint64_t s = 2 * n;
+    std::fill(x[s].begin(), x[s].end(), 0);
+    std::fill(z[s].begin(), z[s].end(), 0);
+    r[s] = 0;
+    for (uint64_t i = 0; i < n; ++i)
+      if (x[i][q]) rowsum(s, n + i);
+    return r[s] != 0;
+  }
+};
+
+// up to global phase (stabilizer.rs:540-563), EPS = 1e-9
+static bool st_phase_aligned(const C* a, const C* b, int len) {
+  const double eps = 1e-9;
+  int p = -1;
+  for (int i = 0; i < len; ++i)
+    if (std::hypot(b[i].re, b[i].im) > eps) {
+      p = i;
+      break;
+    }
+  if (p < 0) {
+    for (int i = 0; i < len; ++i)
+      if (std::hypot(a[i].re, a[i].im) > eps) return false;
+    return true;
+  }
+  if (std::hypot(a[p].re, a[p].im) <= eps) return false;
+  const double ns = norm_sqr(b[p]);
+  const C num = cmul(a[p], conj(b[p]));
+  const C phase{num.re / ns, num.im / ns};
+  if (std::fabs(std::hypot(phase.re, phase.im) - 1.0) > eps) return false;
+  for (int i = 0; i < len; ++i) {
+    const C pb = cmul(phase, b[i]);
+    if (std::hypot(a[i].re - pb.re, a[i].im - pb.im) > eps) return false;
+  }
+  return true;
+}
+
+static bool st_is1(const double* m, const double* ref) {
+  C a[4], b[4];
+  for (int e = 0; e < 4; ++e) {
+    a[e] = ld(m, e);
+    b[e] = ld(ref, e);
+  }
+  return st_phase_aligned(a, b, 4);
+}
+
+void oracle_gate_h(double* m);
+static const double kStI[8] = {1, 0, 0, 0, 0, 0, 1, 0}, kStX[8] = {0, 0, 1, 0, 1, 0, 0, 0},
+                    kStY[8] = {0, 0, 0, -1, 0, 1, 0, 0}, kStZ[8] = {1, 0, 0, 0, 0, 0, -1, 0},
+                    kStS[8] = {1, 0, 0, 0, 0, 0, 0, 1}, kStSdg[8] = {1, 0, 0, 0, 0, 0, 0, -1};
+
+// clifford1 (stabilizer.rs:497-515); returns false if not Clifford
+static bool st_clifford1(const double* m, uint64_t t, std::vector<StOp>* out) {
+  double h[8];
+  oracle_gate_h(h);
+  if (st_is1(m, kStI)) return true;
+  if (st_is1(m, h)) return out->push_back({SP_H, t, 0}), true;
+  if (st_is1(m, kStS)) return out->push_back({SP_S, t, 0}), true;
+  if (st_is1(m, kStSdg)) return out->push_back({SP_SDG, t, 0}), true;
+  if (st_is1(m, kStX)) return out->push_back({SP_X, t, 0}), true;
+  if (st_is1(m, kStY)) return out->push_back({SP_Y, t, 0}), true;
+  if (st_is1(m, kStZ)) return out->push_back({SP_Z, t, 0}), true;
+  return false;
+}
+
+static bool st_clifford2(const double* m, uint64_t a, uint64_t b, std::vector<StOp>* out) {
+  static const double cnot[32] = {1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0,
+                                  0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 1, 0, 0, 0};
+  static const double cz[32] = {1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0, 0, 0,
+                                0, 0, 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, -1, 0};
+  static const double swp[32] = {1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0, 0, 0,
+                                 0, 0, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 0};
+  C g[16], ref[16];
+  for (int e = 0; e < 16; ++e) g[e] = ld(m, e);
+  auto eq = [&](const double* r) {
+    for (int e = 0; e < 16; ++e) ref[e] = ld(r, e);
+    return st_phase_aligned(g, ref, 16);
+  };
+  if (eq(cnot)) return out->push_back({SP_CNOT, a, b}), true;
+  if (eq(cz)) {
+    out->push_back({SP_H, b, 0});
+    out->push_back({SP_CNOT, a, b});
+    out->push_back({SP_H, b, 0});
+    return true;
+  }
+  if (eq(swp)) {
+    out->push_back({SP_CNOT, a, b});
+    out->push_back({SP_CNOT, b, a});
+    out->push_back({SP_CNOT, a, b});
+    return true;
+  }
+  return false;
+}
+
+struct StRun {
+  Tableau t;
+  uint8_t* classical;
+  const char* poison = nullptr;
+};
+
+static void st_apply(const ev_circuit* c, uint64_t* pos, StRun* s) {
+  const ev_op& op = c->ops[*pos];
+  *pos += 1;
+  std::vector<StOp> prims;
+  switch (op.kind) {
+    case EV_OP_APPLY1:
+      if (s->poison) return;
+      if (st_clifford1(op.m, op.q0, &prims))
+        for (const StOp& p : prims) s->t.prim(p);
+      else
+        s->poison = "non-Clifford 1-qubit gate";
+      return;
+    case EV_OP_APPLY2:
+      if (s->poison) return;
+      if (st_clifford2(op.m, op.q0, op.q1, &prims))
+        for (const StOp& p : prims) s->t.prim(p);
+      else
+        s->poison = "non-Clifford 2-qubit gate";
+      return;
+    case EV_OP_CONTROLLED: {
+      if (s->poison) return;
+      bool ok = false;
+      if (op.nctrl == 1) {  // controlled_clifford (stabilizer.rs:529-546)
+        const uint64_t ctl = c->ctrl_pool[op.ctrl_off], t = op.q0;
+        if (st_is1(op.m, kStX)) {
+          prims.push_back({SP_CNOT, ctl, t});
+          ok = true;
+        } else if (st_is1(op.m, kStZ)) {
+          prims.push_back({SP_H, t, 0});
+          prims.push_back({SP_CNOT, ctl, t});
+          prims.push_back({SP_H, t, 0});
+          ok = true;
+        } else if (st_is1(op.m, kStI)) {
+          ok = true;
+        }
+      }
+      if (ok)
+        for (const StOp& p : prims) s->t.prim(p);
+      else
+        s->poison = "non-Clifford controlled gate";
+      return;
+    }
+    case EV_OP_MEASURE:
+      s->classical[op.q1] = s->poison ? 0 : (s->t.measure(op.q0) ? 1 : 0);
+      return;
+    case EV_OP_IF:
+      if (s->classical[op.q0]) {
+        st_apply(c, pos, s);
+      } else {
+        while (c->ops[*pos].kind == EV_OP_IF) *pos += 1;
+        *pos += 1;
+      }
+      return;
+  }
+}
+
+// StabilizerBackend::run_seeded (stabilizer.rs:207-229): returns
+// EV_ERR_NON_CLIFFORD if any gate was outside the Clifford set.
+int oracle_stab_run(const ev_circuit* c, uint64_t seed, uint8_t* x_out, uint8_t* z_out,
+                    uint8_t* neg_out, uint8_t* classical_out) {
+  const int rc = oracle_validate(c);
+  if (rc) return rc;
+  const uint64_t n = c->num_qubits;
+  StRun s{Tableau(n, seed), classical_out};
+  for (uint64_t j = 0; j < c->num_classical; ++j) classical_out[j] = 0;
+  uint64_t pos = 0;
+  while (pos < c->nops) st_apply(c, &pos, &s);
+  if (s.poison) return EV_ERR_NON_CLIFFORD;
+  for (uint64_t i = 0; i < n; ++i) {
+    for (uint64_t q = 0; q < n; ++q) {
+      x_out[i * n + q] = s.t.x[n + i][q];
+      z_out[i * n + q] = s.t.z[n + i][q];
+    }
+    neg_out[i] = s.t.r[n + i];
+  }
+  return EV_OK;
+}
+
 }  // extern "C"
