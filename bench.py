@@ -707,16 +707,25 @@ def run_ours(args, dist: Dist):
         opts = N.EvRunOptions(N.C128, 1 if args.mode == "tiled" else 0, 0, 0)
         cl = np.zeros(1, dtype=np.uint8)
         dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            N.check(L.ev_state_run(h, C.byref(circ), 0, C.byref(opts), cl.ctypes.data))
-            N.check(L.ev_state_download(h, out, 1 << n))
-        e2e_s = dist.max(time.perf_counter() - t0)
+        run_s = dl_s = 0.0
+        with Clocks(gpu_index if dist.world == 1 else 0) as clk_e2e:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                t1 = time.perf_counter()
+                N.check(L.ev_state_run(h, C.byref(circ), 0, C.byref(opts), cl.ctypes.data))
+                t2 = time.perf_counter()
+                N.check(L.ev_state_download(h, out, 1 << n))
+                run_s += t2 - t1
+                dl_s += time.perf_counter() - t2
+            e2e_s = dist.max(time.perf_counter() - t0)
         L.ev_host_free(pinned_ops)
         L.ev_host_free(out)
         e2e = {"value": round(dist.world * bytes_per_step * args.steps / e2e_s / 1e9, 2),
                "unit": "GB/s", "h2d_bytes_per_step": int(ops.nbytes),
-               "d2h_bytes_per_step": int(out_bytes)}
+               "d2h_bytes_per_step": int(out_bytes),
+               "ms_per_step_run": round(1e3 * run_s / args.steps, 1),
+               "ms_per_step_download": round(1e3 * dl_s / args.steps, 1),
+               "clocks": clk_e2e.summary()}
 
     peak, peak_kind = measured_peaks()
     roofline = roofline_of(prof, "tile_pass", 2.0 * (1 << n) * 16, peak, peak_kind,
