@@ -66,6 +66,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--kernel-reps", type=int, default=3,
+                    help="timed calls per case for --case kernels (0: one untimed call each)")
     ap.add_argument("--fuse-bits", type=int, default=5,
                     help="qubits per fused unitary for --case fused (5 or 6)")
     ap.add_argument("--case", default="headline",
@@ -483,7 +485,7 @@ def extras_prepared():
     return out
 
 
-def extras_kernels(n: int, peak: float):
+def extras_kernels(n: int, peak: float, reps: int = 3):
     """Each streaming kernel class alone on an n-qubit state, timed with CUDA
     events on the state's stream, against the measured copy bandwidth.
     Bytes are the algorithmic bytes the engine's kernel moves (2 * N_t * B for
@@ -548,7 +550,8 @@ def extras_kernels(n: int, peak: float):
         res = {}
         for name, fn, nbytes, fp64 in cases:
             fn()
-            reps = 3
+            if reps == 0:  # one call per case (a profiling target)
+                continue
             N.check(L.ev_state_record_event(h, 0))
             for _ in range(reps):
                 fn()
@@ -805,7 +808,7 @@ def run_case(args):
     build.build()
     if args.case == "kernels":
         peak, _ = measured_peaks()
-        print(json.dumps({"case": "kernels", **extras_kernels(args.qubits, peak)}))
+        print(json.dumps({"case": "kernels", **extras_kernels(args.qubits, peak, args.kernel_reps)}))
         return
     if args.case in ("batch", "serve", "serve_small", "prepared", "density", "stabilizer"):
         fn = {"batch": extras_batch, "serve": extras_serve, "serve_small": extras_serve_small,

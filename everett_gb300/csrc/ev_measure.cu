@@ -824,6 +824,7 @@ template <typename V>
 __global__ void __launch_bounds__(kRedThreads)
     k_pauli(const V* __restrict__ a, uint64_t count, uint64_t chunk, uint64_t xmask, int hbit,
             PauliPass pp, double* __restrict__ partials) {
+  constexpr int kPG = 4;  // iterations whose loads are in flight together
   const uint64_t lo = uint64_t(blockIdx.x) * chunk;
   const uint64_t hi = lo + chunk < count ? lo + chunk : count;
   double acc[kPauliTerms];
@@ -831,44 +832,54 @@ __global__ void __launch_bounds__(kRedThreads)
   for (int t = 0; t < kPauliTerms; ++t) acc[t] = 0.0;
   for (uint64_t base = lo + threadIdx.x; base < hi; base += uint64_t(kFlush) * kRedThreads) {
     FF f[kPauliTerms];
-#pragma unroll 2
-    for (int r = 0; r < kFlush; ++r) {
-      const uint64_t i = base + uint64_t(r) * kRedThreads;
-      if (i >= hi) break;
-      const uint64_t j = pp.part == 0 ? i : insert0(i, hbit);
-      const V x = a[j];
-      V y = x;
-      if (pp.part != 0) y = a[j ^ xmask];
-      if constexpr (sizeof(V) == 8) {
-        FF v;  // the term, exactly split: hi + lo
-        if (pp.part == 0) {
-          v.add_prod(x.x, x.x);
-          v.add_prod(x.y, x.y);
-        } else if (pp.part == 1) {
-          v.add_prod(y.x, x.x);
-          v.add_prod(y.y, x.y);
-        } else {
-          v.add_prod(y.x, x.y);
-          v.add_prod(-y.y, x.x);
+    for (int g0 = 0; g0 < kFlush; g0 += kPG) {
+      V xs[kPG], ys[kPG];
+      uint64_t js[kPG];
+#pragma unroll
+      for (int r = 0; r < kPG; ++r) {
+        const uint64_t i = base + uint64_t(g0 + r) * kRedThreads;
+        js[r] = pp.part == 0 ? i : insert0(i, hbit);
+        if (i < hi) {
+          xs[r] = a[js[r]];
+          ys[r] = pp.part != 0 ? a[js[r] ^ xmask] : xs[r];
         }
+      }
 #pragma unroll
-        for (int t = 0; t < kPauliTerms; ++t)
-          if (t < pp.nterms) {
-            const bool neg = __popcll(j & pp.z[t]) & 1;
-            f[t].lo = __fadd_rn(f[t].lo, neg ? -v.lo : v.lo);
-            f[t].add(neg ? -v.hi : v.hi);
+      for (int r = 0; r < kPG; ++r) {
+        if (base + uint64_t(g0 + r) * kRedThreads >= hi) break;
+        const uint64_t j = js[r];
+        const V x = xs[r], y = ys[r];
+        if constexpr (sizeof(V) == 8) {
+          FF v;  // the term, exactly split: hi + lo
+          if (pp.part == 0) {
+            v.add_prod(x.x, x.x);
+            v.add_prod(x.y, x.y);
+          } else if (pp.part == 1) {
+            v.add_prod(y.x, x.x);
+            v.add_prod(y.y, x.y);
+          } else {
+            v.add_prod(y.x, x.y);
+            v.add_prod(-y.y, x.x);
           }
-      } else {
-        double v;
-        if (pp.part == 0)
-          v = __fma_rn(x.x, x.x, __dmul_rn(x.y, x.y));
-        else if (pp.part == 1)
-          v = __fma_rn(y.x, x.x, __dmul_rn(y.y, x.y));
-        else
-          v = __fma_rn(y.x, x.y, -__dmul_rn(y.y, x.x));
 #pragma unroll
-        for (int t = 0; t < kPauliTerms; ++t)
-          if (t < pp.nterms) acc[t] += (__popcll(j & pp.z[t]) & 1) ? -v : v;
+          for (int t = 0; t < kPauliTerms; ++t)
+            if (t < pp.nterms) {
+              const bool neg = __popcll(j & pp.z[t]) & 1;
+              f[t].lo = __fadd_rn(f[t].lo, neg ? -v.lo : v.lo);
+              f[t].add(neg ? -v.hi : v.hi);
+            }
+        } else {
+          double v;
+          if (pp.part == 0)
+            v = __fma_rn(x.x, x.x, __dmul_rn(x.y, x.y));
+          else if (pp.part == 1)
+            v = __fma_rn(y.x, x.x, __dmul_rn(y.y, x.y));
+          else
+            v = __fma_rn(y.x, x.y, -__dmul_rn(y.y, x.x));
+#pragma unroll
+          for (int t = 0; t < kPauliTerms; ++t)
+            if (t < pp.nterms) acc[t] += (__popcll(j & pp.z[t]) & 1) ? -v : v;
+        }
       }
     }
     if constexpr (sizeof(V) == 8) {
