@@ -323,15 +323,18 @@ __global__ void k_decide(const double* __restrict__ result, double u_host,
 }
 
 // Rescaling by an f64 factor: complex128 multiplies in f64 (Complex64 * f64,
-// complex.rs:127-133); complex64 applies the f64-computed factor rounded to
-// f32, which changes a result by at most one f32 rounding.
+// complex.rs:127-133).  complex64 applies the factor as a float pair
+// s ~ sh + sl: x*sh is taken exactly inside an FMA with x*sl added, so each
+// amplitude is rounded once from (nearly) x*s -- no systematic bias from a
+// rounded factor, and the FP64 pipe stays idle.
 template <typename V>
 __device__ __forceinline__ V scale_amp(V a, double s) {
   if constexpr (sizeof(V) == 16) {
     return make_double2(__dmul_rn(a.x, s), __dmul_rn(a.y, s));
   } else {
-    const float f = float(s);
-    return make_float2(__fmul_rn(a.x, f), __fmul_rn(a.y, f));
+    const float sh = float(s);
+    const float sl = float(s - double(sh));
+    return make_float2(__fmaf_rn(a.x, sh, __fmul_rn(a.x, sl)), __fmaf_rn(a.y, sh, __fmul_rn(a.y, sl)));
   }
 }
 
