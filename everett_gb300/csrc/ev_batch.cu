@@ -42,7 +42,7 @@
 namespace ev {
 
 struct BatchOp {
-  uint8_t kind, k1, p0, p1, lo, hi, nins, pad;
+  uint8_t kind, k1, p0, p1, lo, hi, nins, soft;  // soft: as TileOp::soft
   uint32_t lmask;
   uint32_t mat;  // offset of the matrix in the pool (doubles)
   uint64_t emask;
@@ -403,7 +403,7 @@ void plan_circuit(const ev_circuit* c, int kmax, bool reorder, CircPlan* out) {
       b.lo = tmp.lo;
       b.hi = tmp.hi;
       b.nins = tmp.nins;
-      b.pad = 0;
+      b.soft = 0;
       b.lmask = tmp.lmask;
       b.emask = tmp.emask;
       b.ins = tmp.ins;

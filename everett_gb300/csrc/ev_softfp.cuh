@@ -1,0 +1,133 @@
+// ev_softfp.cuh -- IEEE-754 binary64 multiplication, round to nearest even,
+// computed on the integer pipes.
+//
+// GB300's FP64 pipe retires about 0.53e12 fused multiply-adds per second,
+// far below its integer and FP32 pipes, and the complex128 gate passes are
+// bound by it.  A correctly rounded product is a fixed function of its
+// operands, so a product formed here from the 106-bit integer product of the
+// significands is bit-identical to the hardware's: the tile passes send part
+// of their products through this path and the rest through the FP64 pipe,
+// with unchanged results.
+//
+// The fast path covers operands that are normal with biased exponents in
+// [512, 1534], where a product can neither underflow nor lose its exponent
+// range; it reports every other operand (zero, subnormal, infinite, NaN, or
+// far from 1) so the caller computes that product with the FP64 pipe.  The
+// rounding follows the standard's definition: keep the top 53 bits of the
+// exact product, round up when the discarded part exceeds half an ulp, or
+// equals it and the kept part is odd.
+//
+// The header compiles for the host too (g++), where the CPU tests compare it
+// with the host's own multiplication.
+#pragma once
+
+#include <stdint.h>
+#ifndef __CUDACC__
+#include <string.h>
+#endif
+
+#ifdef __CUDACC__
+#define EV_SOFT_FN __host__ __device__ __forceinline__
+#else
+#define EV_SOFT_FN static inline
+#endif
+
+namespace ev {
+namespace softfp {
+
+EV_SOFT_FN uint64_t to_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return (uint64_t)__double_as_longlong(x);
+#else
+  uint64_t u;
+  memcpy(&u, &x, sizeof(u));
+  return u;
+#endif
+}
+
+EV_SOFT_FN double from_bits(uint64_t u) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  memcpy(&x, &u, sizeof(x));
+  return x;
+#endif
+}
+
+// The 128-bit product of two 64-bit integers: *hi gets the top 64 bits,
+// the return value is nonzero when the low 64 bits are.
+EV_SOFT_FN uint32_t mul_128(uint64_t a, uint64_t b, uint64_t* hi) {
+#ifdef __CUDA_ARCH__
+  const uint32_t al = (uint32_t)a, ah = (uint32_t)(a >> 32);
+  const uint32_t bl = (uint32_t)b, bh = (uint32_t)(b >> 32);
+  uint32_t r0, r1, r2, r3;
+  // schoolbook product of 32-bit limbs, carries chained through the .cc flag
+  asm("mul.lo.u32 %0, %4, %6;\n\t"
+      "mul.hi.u32 %1, %4, %6;\n\t"
+      "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
+      "madc.hi.u32 %2, %4, %7, 0;\n\t"
+      "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
+      "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
+      "madc.hi.u32 %3, %5, %7, 0;\n\t"
+      "mad.lo.cc.u32 %2, %5, %7, %2;\n\t"
+      "addc.u32 %3, %3, 0;"
+      : "=&r"(r0), "=&r"(r1), "=&r"(r2), "=&r"(r3)
+      : "r"(al), "r"(ah), "r"(bl), "r"(bh));
+  *hi = ((uint64_t)r3 << 32) | r2;
+  return r0 | r1;
+#else
+  const unsigned __int128 p = (unsigned __int128)a * b;
+  *hi = (uint64_t)(p >> 64);
+  return (uint64_t)p != 0;
+#endif
+}
+
+// An operand unpacked once and used in several products: the significand
+// with its leading 1 at bit 63, the sign bit (bit 31), and the biased
+// exponent minus 512 in the exponent field's place (bits 20..30), so that the
+// sum of two such fields plus the normalisation bit is the product's biased
+// exponent minus one, in place.
+struct Unpacked {
+  uint64_t sig;
+  uint32_t ex;
+  uint32_t sg;
+  uint32_t ok;  // normal, biased exponent in [512, 1534]
+};
+
+EV_SOFT_FN Unpacked unpack(double x) {
+  const uint64_t u = to_bits(x);
+  const uint32_t w = (uint32_t)(u >> 32);
+  Unpacked r;
+  r.sig = (u << 11) | (1ull << 63);
+  r.ex = (w & 0x7FF00000u) - (512u << 20);  // wraps outside the domain
+  r.sg = w & 0x80000000u;
+  r.ok = r.ex <= (1022u << 20);
+  return r;
+}
+
+// RN(a * b) for a.ok && b.ok; any value otherwise.
+EV_SOFT_FN double mul(const Unpacked& a, const Unpacked& b) {
+  // a.sig * b.sig = P * 2^22 with P the 106-bit product of the 53-bit
+  // significands; hi holds its top 64 bits, in [2^62, 2^64).
+  uint64_t hi;
+  const uint32_t sticky = mul_128(a.sig, b.sig, &hi);
+  const uint32_t top = (uint32_t)(hi >> 63);  // P >= 2^105
+  // The 53 kept bits are hi >> sh.  Fold the bits below hi into bit 0
+  // (below the half-ulp bit sh - 1 in both cases), then add half an ulp
+  // minus one plus the kept part's lowest bit: the sum carries into bit sh
+  // exactly when the discarded part exceeds half an ulp, or equals it and
+  // the kept part is odd.  hi <= 2^64 - 2^12, so the sum cannot overflow.
+  const uint32_t sh = 10u + top;
+  const uint64_t h = hi | (uint64_t)(sticky != 0);
+  const uint32_t lsb = ((uint32_t)h >> sh) & 1u;
+  const uint64_t m = (h + ((1ull << (sh - 1)) - 1u + lsb)) >> sh;  // in [2^52, 2^53]
+  // Sign, and the biased exponent minus one in place (in [0, 2045]): adding
+  // the significand with its leading 1 at bit 52 completes the exponent, and
+  // a significand that rounded up to 2^53 carries into it.
+  const uint32_t word = (a.sg ^ b.sg) | (a.ex + b.ex + (top << 20));
+  return from_bits(((uint64_t)word << 32) + m);
+}
+
+}  // namespace softfp
+}  // namespace ev

@@ -15,12 +15,28 @@
 // must lie in T.  Controls need not: a control outside T is a fixed bit of
 // the tile's base index, so the whole tile either takes the gate or skips
 // it, and a control inside T becomes a local mask.
+#include <cstdlib>
+
 #include "ev_tile.cuh"
 
 namespace ev {
 
 constexpr int kTileThreads = 512;
 constexpr int kMaxPassOps = 48;  // op records per pass (staged in shared memory)
+
+// How many amplitudes of each pair have their complex128 products formed on
+// the integer pipes (TileOp::soft), for real-matrix records and for the
+// others.  EV_TILE_SOFT="rd" (two digits 0-2) overrides both.
+struct SoftLevels {
+  int real, other;
+};
+constexpr SoftLevels kDefaultSoft{2, 2};
+static SoftLevels tile_soft_levels() {
+  const char* e = getenv("EV_TILE_SOFT");
+  if (e == nullptr || e[0] < '0' || e[0] > '2' || e[1] < '0' || e[1] > '2' || e[2] != 0)
+    return kDefaultSoft;
+  return SoftLevels{e[0] - '0', e[1] - '0'};
+}
 
 // One persistent block per resident slot; tiles strided over the grid.  The
 // pass's op records and index tables are staged in shared memory once per
@@ -115,6 +131,7 @@ int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, 
   std::vector<Pass> passes =
       plan_passes(c, first, last, n, k, L, uint64_t(kMaxPassOps), s->dtype == EV_C64);
   const uint64_t ntiles = uint64_t(1) << (n - k);
+  const SoftLevels soft = tile_soft_levels();
   std::vector<TileOp> ops;
   for (const Pass& p : passes) {
     TilePlan plan{};
@@ -132,7 +149,11 @@ int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, 
         plan.comp[plan.ncomp++] = uint8_t(q);
       }
     ops.assign(p.ops.size(), TileOp{});
-    for (size_t j = 0; j < p.ops.size(); ++j) encode_op(c, c->ops[p.ops[j]], p.tset, local, &ops[j]);
+    for (size_t j = 0; j < p.ops.size(); ++j) {
+      encode_op(c, c->ops[p.ops[j]], p.tset, local, &ops[j]);
+      if (s->dtype == EV_C128 && ops[j].kind == T_1Q)
+        ops[j].soft = uint8_t(ops[j].k1 == K1_REAL ? soft.real : soft.other);
+    }
     SegStep st;
     st.fused = 0;
     st.off0 = blob->add(&plan, sizeof(plan));
@@ -156,4 +177,78 @@ int launch_tile_step(ev_state* s, const SegStep& st, const unsigned char* dblob)
   return launch_tile<float2>(s, st.count, plan, dplan, dops, st.nops, nullptr);
 }
 
+// ---- device check of the integer-pipe product ------------------------------------
+// Operands drawn from five families that reach every rounding case (full
+// random significands, short significands with exact products and ties,
+// significands next to 1 and 2, the edges of the fast-path exponent range,
+// amplitude-like magnitudes), all inside the fast path's domain.
+
+__device__ __forceinline__ uint64_t check_next(uint64_t& st) {  // SplitMix64
+  uint64_t z = (st += 0x9E3779B97F4A7C15ULL);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+  return z ^ (z >> 31);
+}
+
+__device__ double check_operand(uint64_t& st, int family) {
+  const uint64_t sign = check_next(st) & 1, r = check_next(st), r2 = check_next(st);
+  const uint64_t fmask = (1ull << 52) - 1;
+  uint64_t exp = 512 + r2 % 1023, frac = r;
+  if (family == 1) {
+    const int k = 1 + int(r2 % 30);
+    frac = (r >> (64 - k)) << (52 - k);
+    exp = 512 + (r2 >> 8) % 1023;
+  } else if (family == 2) {
+    const uint64_t small = r >> (12 + (r2 >> 20) % 52);
+    frac = (r2 & 1) ? small : (fmask - small);
+    exp = 512 + (r2 >> 8) % 1023;
+  } else if (family == 3) {
+    const uint64_t edges[4] = {512, 513, 1533, 1534};
+    exp = edges[r2 & 3];
+    frac = (r2 & 4) ? r : fmask;
+  } else if (family == 4) {
+    exp = 1023 - r2 % 41;
+  }
+  return __longlong_as_double((long long)((sign << 63) | (exp << 52) | (frac & fmask)));
+}
+
+__global__ void k_softfp_check(uint64_t seed, uint64_t per_thread, unsigned long long* bad) {
+  const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  uint64_t st = seed ^ (gid * 0xD1B54A32D192ED03ULL);
+  unsigned long long mine = 0;
+  for (uint64_t i = 0; i < per_thread; ++i) {
+    const int fam = int((gid + i) % 25);
+    const double a = check_operand(st, fam % 5), b = check_operand(st, fam / 5);
+    const softfp::Unpacked ua = softfp::unpack(a), ub = softfp::unpack(b);
+    const double got = softfp::mul(ua, ub), want = __dmul_rn(a, b);
+    mine += (!(ua.ok & ub.ok)) || __double_as_longlong(got) != __double_as_longlong(want);
+  }
+  if (mine) atomicAdd(bad, mine);
+}
+
 }  // namespace ev
+
+extern "C" int ev_softfp_check(uint64_t seed, uint64_t count, uint64_t* mismatches) {
+  using namespace ev;
+  clear_error();
+  if (!mismatches) return fail(EV_ERR_INVALID_ARGUMENT, "ev_softfp_check: null output");
+  int dev = 0, sms = 0;
+  EV_CUDA(cudaGetDevice(&dev));
+  EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint64_t threads = uint64_t(sms) * 4 * 256;
+  const uint64_t per = (count + threads - 1) / threads;
+  unsigned long long* d = nullptr;
+  EV_CUDA(cudaMalloc(reinterpret_cast<void**>(&d), sizeof(*d)));
+  int rc = EV_OK;
+  unsigned long long h = 0;
+  if (cudaMemset(d, 0, sizeof(*d)) != cudaSuccess) {
+    rc = fail(EV_ERR_CUDA, "ev_softfp_check: memset failed");
+  } else {
+    k_softfp_check<<<unsigned(sms * 4), 256>>>(seed, per, d);
+    if (cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = fail(EV_ERR_CUDA, "ev_softfp_check: kernel failed");
+  }
+  cudaFree(d);
+  if (rc == EV_OK) *mismatches = h;
+  return rc;
+}

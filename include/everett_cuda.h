@@ -447,6 +447,11 @@ int ev_state_profile_read(ev_state* s, ev_kernel_stat* out, int32_t max, int32_t
  * second, from independent FMA chains on every SM): the roofline of the
  * complex128 kernels, whose arithmetic is FP64. */
 int ev_probe_fp64(double* fma_per_s);
+/* Checks the integer-pipe double product of the complex128 tile passes
+ * against the FP64 pipe's on `count` operand pairs drawn from `seed`
+ * (families that reach every rounding case); *mismatches = pairs whose bits
+ * differ.  A check of the build, for tests. */
+int ev_softfp_check(uint64_t seed, uint64_t count, uint64_t* mismatches);
 /* max_j |self_j - other_j| over two states of equal size, either amplitude
  * type (the max amplitude error of a complex64 run against complex128). */
 int ev_max_abs_diff(const ev_state* self, const ev_state* other, double* out);

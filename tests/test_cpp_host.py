@@ -33,3 +33,24 @@ def test_cpp_rng_matches_oracle(program, seed):
     f64 = [float.fromhex(v) for v in lines[64:]]
     assert u64 == [int(v) for v in oracle.rng_u64(seed, 64)]
     assert f64 == [float(v) for v in oracle.rng_f64(seed, 64)]
+
+
+def test_integer_pipe_product_host(tmp_path):
+    """The integer-pipe double product (everett_gb300/csrc/ev_softfp.cuh),
+    compiled for the host, equals the host's IEEE multiplication on 2*10^7
+    operand pairs from families that reach every rounding case."""
+    import shutil
+    from pathlib import Path
+    root = Path(__file__).resolve().parents[1]
+    gxx = shutil.which("g++")
+    assert gxx, "g++ is required"
+    exe = tmp_path / "test_softfp"
+    subprocess.run([gxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror",
+                    "-I", str(root / "everett_gb300" / "csrc"),
+                    str(root / "tests" / "cpp" / "test_softfp.cpp"), "-o", str(exe)],
+                   check=True, capture_output=True, text=True)
+    for seed in ("3", "4"):
+        r = subprocess.run([str(exe), "10000000", seed], capture_output=True, text=True,
+                           timeout=300)
+        assert r.returncode == 0, r.stdout + r.stderr
+        assert ", 0 mismatches" in r.stdout, r.stdout

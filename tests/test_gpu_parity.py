@@ -328,3 +328,44 @@ def test_edge_sizes(gpu):
     ex = CudaStateVectorBackend.run(Circuit(10))
     assert ex.state().probability(0) == 1.0
     assert ex.state().sample(0).shape == (0,)
+
+
+def test_integer_pipe_product_matches_fp64_pipe(gpu):
+    """The tile passes' integer-pipe double product is bit-identical to the
+    FP64 pipe's on 2^30 operand pairs per seed, drawn to reach every
+    rounding case (exact products, exact ties, carries into the exponent,
+    the edges of the fast path's exponent range)."""
+    import ctypes as C
+    from everett_gb300 import _native as N
+    for seed in (1, 2):
+        bad = C.c_uint64(7)
+        N.check(N.lib().ev_softfp_check(seed, 1 << 30, C.byref(bad)))
+        assert bad.value == 0, (seed, bad.value)
+
+
+@pytest.mark.parametrize("level", ["00", "11", "22", "21", "12"])
+def test_tiled_integer_pipe_levels_bit_exact(gpu, monkeypatch, level):
+    """Every level of the complex128 tile passes' integer-pipe products
+    (none, one amplitude per pair, both) gives the oracle's bits, including
+    pairs that leave the fast path: zeros of the initial state, gate entries
+    and amplitudes below 2^-511."""
+    monkeypatch.setenv("EV_TILE_SOFT", level)
+    rng = np.random.default_rng(17)
+    n = 13
+    c = Circuit(n)
+    tiny = Gate1.ry(1e-160)  # entries and amplitudes far below the fast path's range
+    for layer in range(6):
+        for q in range(n):
+            c.gate1(GATES_1Q[int(rng.integers(0, len(GATES_1Q)))], q)
+            c.rz(q, float(rng.uniform(0, 6.3)))
+        c.gate1(tiny, layer % n)
+        c.controlled([int((layer + 3) % n)], Gate1.ry(float(rng.uniform(0, 6.3))), layer % n)
+        for i in range(layer % 2, n - 1, 2):
+            c.cnot(i, i + 1)
+    want, _, _ = O.run_seeded(c, 0)
+    for tb in (6, 10):
+        got = CudaStateVectorBackend.run(c, mode="tiled", tile_bits=tb).state().amplitudes()
+        assert exact(got, want), (level, tb)
+    rl = workloads.random_layers(14, 6, 5)
+    want, _, _ = O.run_seeded(rl, 0, parallel=True)
+    assert exact(CudaStateVectorBackend.run(rl, mode="tiled").state().amplitudes(), want), level
