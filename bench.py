@@ -746,12 +746,18 @@ def run_ours(args, dist: Dist):
                     "achieved_per_s": float(f"{achieved:.4g}"),
                     "peak_per_s": float(f"{rate.value:.4g}"),
                     "peak_source": "measured (ev_probe_fp64: sustained FP64 FMA issue rate)",
-                    "frac": round(achieved / rate.value, 3)}
+                    "frac": round(achieved / rate.value, 3),
+                    "note": ("the reference's FP64 operations counted from the source, per "
+                             "second of tile pass; above 1 because the pass forms part of its "
+                             "products on the integer pipes (bit-identical)")}
             roofline["fp64"] = fp64
     if roofline is not None:
-        roofline["note"] = ("compute-bound on the FP64 pipe (GB300 issues FP64 at 1/64 of the "
-                            "FP32 rate); ncu: fp64 pipe busy "
-                            f"{ncu_figure('k_tile_c128', 'fp64_pipe_pct')}% in rotation passes")
+        roofline["note"] = (
+            "compute-bound: GB300 issues FP64 at 1/64 of the FP32 rate, so the pass splits its "
+            "products between the FP64 pipe and an exact integer-pipe multiply; ncu in rotation "
+            f"passes: alu pipe {ncu_figure('k_tile_c128', 'alu_pipe_pct')}%, fp64 pipe "
+            f"{ncu_figure('k_tile_c128', 'fp64_pipe_pct')}%, fma-heavy pipe "
+            f"{ncu_figure('k_tile_c128', 'fmaheavy_pipe_pct')}% busy")
 
     cpu = None
     extras = {}
