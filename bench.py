@@ -496,9 +496,12 @@ def extras_kernels(n: int, peak: float, reps: int = 3):
 
     complex128 arithmetic is FP64, which GB300 issues at a small fraction of
     its FP32 rate, so each complex128 case also carries its FP64 floor: the
-    FP64 instructions its kernel issues per state amplitude (dmul, dadd, dfma
-    counted from the source: a complex product in the reference's FMA form is
-    4, a complex add 2) times 2^n, over the measured FMA issue rate."""
+    FP64-pipe instructions its kernel issues per state amplitude (dadd, dfma
+    and the dmul left on that pipe, counted from the source: a complex
+    product in the reference's FMA form is 2 FMAs there plus 2 products
+    formed on the integer pipes, a complex add 2) times 2^n, over the
+    measured FMA issue rate.  The state is dense (a depth-2 random-layer
+    circuit), as a circuit leaves it."""
     import ctypes as C
 
     import numpy as np
@@ -518,26 +521,33 @@ def extras_kernels(n: int, peak: float, reps: int = 3):
     xshared = ["+" + "".join(("XY"[int(y)] if xb else "IZ"[int(b)])
                              for xb, y, b in zip(xpart, ypart, prng.integers(0, 2, n)))
                for _ in range(8)]
+    from everett_gb300 import CudaStateVectorBackend
+    dense = workloads.random_layers(n, 2, seed=11)
     for dtype, B in (("complex128", 16), ("complex64", 8)):
+        # dense states, as a circuit leaves them: every amplitude nonzero and
+        # complex (the complex128 gates form their products on the integer
+        # pipes only for operands in a normal range; zeros take the FP64 pipe)
         st = State.zero(n, dtype)
         other = State.zero(n, dtype)
-        N.check(L.ev_normalize(st.handle))
+        CudaStateVectorBackend.run_into(st, dense, 0, mode="tiled")
+        CudaStateVectorBackend.run_into(other, dense, 1, mode="tiled")
         h = st.handle
         Nn = 1 << n
         hi, lo = n - 1, 0
-        # name, call, algorithmic bytes, FP64 instructions per amplitude (complex128)
+        # name, call, algorithmic bytes, FP64-pipe instructions per amplitude
+        # (complex128, with the plain products on the integer pipes)
         cases = [
-            ("1q_dense_high", lambda: st.apply_1q(hi, g_dense), 2 * Nn * B, 10),
-            ("1q_dense_low", lambda: st.apply_1q(lo, g_dense), 2 * Nn * B, 10),
-            ("1q_real_h", lambda: st.apply_1q(hi - 3, Gate1.h()), 2 * Nn * B, 6),
-            ("1q_diag_rz", lambda: st.apply_1q(hi - 1, Gate1.rz(0.3)), 2 * Nn * B, 4),
-            ("1q_phase", lambda: st.apply_1q(hi - 2, Gate1.phase(0.3)), Nn * B, 2),
+            ("1q_dense_high", lambda: st.apply_1q(hi, g_dense), 2 * Nn * B, 6),
+            ("1q_dense_low", lambda: st.apply_1q(lo, g_dense), 2 * Nn * B, 6),
+            ("1q_real_h", lambda: st.apply_1q(hi - 3, Gate1.h()), 2 * Nn * B, 2),
+            ("1q_diag_rz", lambda: st.apply_1q(hi - 1, Gate1.rz(0.3)), 2 * Nn * B, 2),
+            ("1q_phase", lambda: st.apply_1q(hi - 2, Gate1.phase(0.3)), Nn * B, 1),
             ("1q_anti_x", lambda: st.apply_1q(7, Gate1.x()), 2 * Nn * B, 4),
             ("cnot", lambda: st.apply_2q(hi, 3, Gate2.cnot()), Nn * B, 0),
             ("cz", lambda: st.apply_2q(hi, 3, Gate2.cz()), Nn * B // 2, 0),
             ("swap", lambda: st.apply_2q(hi, 3, Gate2.swap()), Nn * B, 0),
             ("2q_dense", lambda: st.apply_2q(hi, 3, g2), 2 * Nn * B, 22),
-            ("controlled_1q_1ctrl", lambda: st.apply_controlled_1q([hi], 5, g_dense), Nn * B, 5),
+            ("controlled_1q_1ctrl", lambda: st.apply_controlled_1q([hi], 5, g_dense), Nn * B, 3),
             ("measure_high", lambda: st.measure_qubit(hi, 0.25), 2 * Nn * B, 2),
             ("measure_low", lambda: st.measure_qubit(lo, 0.25), 2 * Nn * B, 2),
             ("norm_sqr", lambda: st.norm_sqr(), Nn * B, 2),

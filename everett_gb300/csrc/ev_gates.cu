@@ -17,8 +17,11 @@
 // terms changes no value (only, at most, the sign of a zero).
 #include <cstdio>
 
+#include <type_traits>
+
 #include "ev_device.cuh"
 #include "ev_internal.h"
+#include "ev_softpair.cuh"
 
 namespace ev {
 
@@ -75,6 +78,23 @@ __device__ __forceinline__ void pair_update(V* __restrict__ s, uint64_t i0, uint
   }
 }
 
+// pair_update with the complex128 products of both outputs on the integer
+// pipes (ev_softpair.cuh); same results.
+template <int KIND>
+__device__ __forceinline__ void pair_update_soft(double2* __restrict__ s, uint64_t i0, uint64_t i1,
+                                                 const SoftM1& f) {
+  if constexpr (KIND == K1_PHASE) {
+    double2 a0 = make_double2(0.0, 0.0), a1 = s[i1];
+    soft_pair<KIND>(a0, a1, f, true);
+    s[i1] = a1;
+  } else {
+    double2 a0 = s[i0], a1 = s[i1];
+    soft_pair<KIND>(a0, a1, f, true);
+    s[i0] = a0;
+    s[i1] = a1;
+  }
+}
+
 // apply_1q over all 2^(n-1) pairs (kernel.rs:100-119).
 template <int KIND, typename V>
 __global__ void __launch_bounds__(256) k_pair(V* __restrict__ s, uint64_t npairs, int k, M1<V> m,
@@ -82,6 +102,16 @@ __global__ void __launch_bounds__(256) k_pair(V* __restrict__ s, uint64_t npairs
   if (skip(pred)) return;
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   const uint64_t bit = uint64_t(1) << k;
+  if constexpr (std::is_same<V, double2>::value) {
+    const SoftM1 f = soft_matrix<KIND>(m.m0, m.m1, m.m2, m.m3);
+    if (f.ok) {
+      for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < npairs; i += stride) {
+        const uint64_t i0 = insert0(i, k);
+        pair_update_soft<KIND>(s, i0, i0 | bit, f);
+      }
+      return;
+    }
+  }
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < npairs; i += stride) {
     const uint64_t i0 = insert0(i, k);
     pair_update<KIND>(s, i0, i0 | bit, m);
@@ -95,6 +125,16 @@ __global__ void __launch_bounds__(256) k_diag(V* __restrict__ s, uint64_t len, i
                                               const uint8_t* pred) {
   if (skip(pred)) return;
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  if constexpr (std::is_same<V, double2>::value) {
+    const softfp::Unpacked u0 = softfp::unpack(d0.y), u1 = softfp::unpack(d1.y);
+    if (u0.ok & u1.ok) {  // products on the integer pipes, as ev_softpair.cuh
+      for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < len; j += stride) {
+        const bool one = (j >> k) & 1;
+        s[j] = soft_diag(one ? d1 : d0, one ? u1 : u0, s[j]);
+      }
+      return;
+    }
+  }
   for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < len; j += stride)
     s[j] = cmul(((j >> k) & 1) ? d1 : d0, s[j]);
 }
@@ -108,6 +148,18 @@ __global__ void __launch_bounds__(256) k_ctrl(V* __restrict__ s, uint64_t count,
   if (skip(pred)) return;
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   const uint64_t tbit = uint64_t(1) << target;
+  if constexpr (std::is_same<V, double2>::value) {
+    const SoftM1 f = soft_matrix<KIND>(m.m0, m.m1, m.m2, m.m3);
+    if (f.ok) {
+      for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += stride) {
+        uint64_t j = i;
+        for (int q = 0; q < pos.np; ++q) j = insert0(j, pos.p[q]);
+        const uint64_t i0 = j | ctrl_mask;
+        pair_update_soft<KIND>(s, i0, i0 | tbit, f);
+      }
+      return;
+    }
+  }
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += stride) {
     uint64_t j = i;
     for (int q = 0; q < pos.np; ++q) j = insert0(j, pos.p[q]);

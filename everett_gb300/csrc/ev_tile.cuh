@@ -14,7 +14,7 @@
 
 #include "ev_device.cuh"
 #include "ev_internal.h"
-#include "ev_softfp.cuh"
+#include "ev_softpair.cuh"
 
 namespace ev {
 
@@ -65,50 +65,17 @@ __device__ __forceinline__ uint32_t ins0(uint32_t i, int p) {
   return ((i >> p) << (p + 1)) | (i & ((1u << p) - 1));
 }
 
-// ---- complex128 products on the integer pipes --------------------------------
-// The FP64 pipe bounds the complex128 passes; each product computed by
-// softfp::mul instead is bit-identical, so a record may send the products of
-// one or both amplitudes of a pair there.  A pair whose amplitudes fall
-// outside the fast path's domain (a zero, say) takes the FP64 pipe alone.
-
-struct SoftAmp {
-  softfp::Unpacked x, y;
-};
-__device__ __forceinline__ SoftAmp sunpack(double2 a) {
-  return SoftAmp{softfp::unpack(a.x), softfp::unpack(a.y)};
-}
-// r * a for a real r, as rmul
-__device__ __forceinline__ double2 srmul(const softfp::Unpacked& r, const SoftAmp& a) {
-  return make_double2(softfp::mul(r, a.x), softfp::mul(r, a.y));
-}
-// m * a in FMA form, as cmul; my is m.y unpacked
-__device__ __forceinline__ double2 scmul(double2 m, const softfp::Unpacked& my, double2 a,
-                                         const SoftAmp& ua) {
-  return make_double2(__fma_rn(m.x, a.x, -softfp::mul(my, ua.y)),
-                      __fma_rn(m.x, a.y, softfp::mul(my, ua.x)));
-}
-
 template <int K1, typename V, typename Op>
 __device__ __forceinline__ void tile_1q_fp64(V* t, uint32_t count, const Op& op, const double* mm);
 
-// The pair loop of tile_1q with the products of one (op.soft == 1) or both
-// amplitudes of each pair on the integer pipes.
+// The pair loop of tile_1q with the complex128 products of one (op.soft ==
+// 1) or both amplitudes of each pair on the integer pipes (ev_softpair.cuh).
 template <int K1, typename Op>
 __device__ __forceinline__ void tile_1q_soft(double2* t, uint32_t count, const Op& op,
                                              const double* mm) {
-  const double2 m0 = ldm<double2>(mm, 0), m1 = ldm<double2>(mm, 1), m2 = ldm<double2>(mm, 2),
-                m3 = ldm<double2>(mm, 3);
-  // REAL gates multiply by the real parts, the others by the imaginary ones
-  constexpr bool kReal = K1 == K1_REAL;
-  const softfp::Unpacked u0 = softfp::unpack(kReal ? m0.x : m0.y),
-                         u1 = softfp::unpack(kReal ? m1.x : m1.y),
-                         u2 = softfp::unpack(kReal ? m2.x : m2.y),
-                         u3 = softfp::unpack(kReal ? m3.x : m3.y);
-  uint32_t mok;
-  if constexpr (K1 == K1_DIAG) mok = u0.ok & u3.ok;
-  else if constexpr (K1 == K1_PHASE) mok = u3.ok;
-  else mok = u0.ok & u1.ok & u2.ok & u3.ok;
-  if (!mok) {  // uniform across the block
+  const SoftM1 f = soft_matrix<K1>(ldm<double2>(mm, 0), ldm<double2>(mm, 1), ldm<double2>(mm, 2),
+                                   ldm<double2>(mm, 3));
+  if (!f.ok) {  // uniform across the block
     tile_1q_fp64<K1>(t, count, op, mm);
     return;
   }
@@ -121,40 +88,15 @@ __device__ __forceinline__ void tile_1q_soft(double2* t, uint32_t count, const O
     uint32_t j = ins0(i, ins_first);
     for (int q = 1; q < nins; ++q) j = ins0(j, int((ins >> (4 * q)) & 15));
     const uint32_t i0 = j | lmask, i1 = i0 | tbit;
-    if constexpr (K1 == K1_REAL || K1 == K1_DENSE) {
-      const double2 a0 = t[i0], a1 = t[i1];
-      const SoftAmp s0 = sunpack(a0), s1 = sunpack(a1);
-      if (s0.x.ok & s0.y.ok & s1.x.ok & s1.y.ok) {
-        if constexpr (kReal) {
-          t[i0] = cadd(srmul(u0, s0), srmul(u1, s1));
-          t[i1] = both ? cadd(srmul(u2, s0), srmul(u3, s1))
-                       : cadd(rmul(m2.x, a0), rmul(m3.x, a1));
-        } else {
-          t[i0] = cadd(scmul(m0, u0, a0, s0), scmul(m1, u1, a1, s1));
-          t[i1] = both ? cadd(scmul(m2, u2, a0, s0), scmul(m3, u3, a1, s1))
-                       : cadd(cmul(m2, a0), cmul(m3, a1));
-        }
-      } else if constexpr (kReal) {
-        t[i0] = cadd(rmul(m0.x, a0), rmul(m1.x, a1));
-        t[i1] = cadd(rmul(m2.x, a0), rmul(m3.x, a1));
-      } else {
-        t[i0] = cadd(cmul(m0, a0), cmul(m1, a1));
-        t[i1] = cadd(cmul(m2, a0), cmul(m3, a1));
-      }
-    } else if constexpr (K1 == K1_DIAG) {
-      const double2 a0 = t[i0], a1 = t[i1];
-      const SoftAmp s0 = sunpack(a0);
-      t[i0] = (s0.x.ok & s0.y.ok) ? scmul(m0, u0, a0, s0) : cmul(m0, a0);
-      if (both) {
-        const SoftAmp s1 = sunpack(a1);
-        t[i1] = (s1.x.ok & s1.y.ok) ? scmul(m3, u3, a1, s1) : cmul(m3, a1);
-      } else {
-        t[i1] = cmul(m3, a1);
-      }
-    } else if constexpr (K1 == K1_PHASE) {
-      const double2 a1 = t[i1];
-      const SoftAmp s1 = sunpack(a1);
-      t[i1] = (s1.x.ok & s1.y.ok) ? scmul(m3, u3, a1, s1) : cmul(m3, a1);
+    if constexpr (K1 == K1_PHASE) {
+      double2 a0 = make_double2(0.0, 0.0), a1 = t[i1];
+      soft_pair<K1>(a0, a1, f, both);
+      t[i1] = a1;
+    } else {
+      double2 a0 = t[i0], a1 = t[i1];
+      soft_pair<K1>(a0, a1, f, both);
+      t[i0] = a0;
+      t[i1] = a1;
     }
   }
 }
