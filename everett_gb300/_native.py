@@ -126,6 +126,7 @@ _SIGS = {
     "ev_server_stats_get": [_P, _P],
     "ev_server_destroy": [_P],
     "ev_probe_fp64": [_DP],
+    "ev_marginal_low": [_P, _U64, _DP],
     "ev_softfp_check": [_U64, _U64, C.POINTER(_U64)],
     "ev_max_abs_diff": [_P, _P, _DP],
     "ev_host_alloc": [_U64, C.POINTER(_P)],

@@ -1,7 +1,8 @@
 """Circuit generators of the reference (src/algorithms/*.rs) that build the
 workloads of this engine: QFT (qft.rs:54-118), Trotterised TFIM
-(hamiltonian.rs:91-118), Bell/GHZ preparation (prep.rs:51-59) and
-teleportation (teleport.rs:45-85)."""
+(hamiltonian.rs:91-118), Bell/GHZ preparation (prep.rs:51-59),
+teleportation (teleport.rs:45-85), superdense coding (superdense.rs:35-50)
+and phase estimation (phase_estimation.rs:55-121)."""
 from __future__ import annotations
 
 import math
@@ -96,3 +97,48 @@ def teleport_state(alpha: complex, beta: complex) -> Circuit:
     c.gate1(prep, 0)
     c.compose(teleport_circuit())
     return c
+
+
+def superdense_circuit(bit0: bool, bit1: bool) -> Circuit:
+    """Encode two bits on one half of a Bell pair and decode them into
+    classical bits 0 and 1 (superdense.rs:35-50)."""
+    c = Circuit.with_classical(2, 2)
+    c.h(0).cnot(0, 1)
+    if bit1:
+        c.x(0)
+    if bit0:
+        c.z(0)
+    c.cnot(0, 1).h(0)
+    c.measure(0, 0).measure(1, 1)
+    return c
+
+
+def phase_estimation(counting_qubits: int, phi: float) -> Circuit:
+    """m counting qubits 0..m-1 and the eigenstate qubit m of phase(2*pi*phi)
+    (phase_estimation.rs:55-87): X on the target, H on the counting register,
+    controlled phase(2*pi*phi*2^j) from counting qubit j, then iqft(m)."""
+    m = counting_qubits
+    c = Circuit(m + 1)
+    c.x(m)
+    for j in range(m):
+        c.h(j)
+    for j in range(m):
+        c.controlled([j], Gate1.phase(math.tau * phi * float(1 << j)), m)
+    c.compose(iqft(m))
+    return c
+
+
+def most_probable_phase(state, counting_qubits: int) -> float:
+    """The most probable counting-register value over 2^m
+    (phase_estimation.rs:97-121). The marginal over the other qubits is a
+    device reduction summed in the reference's basis order; among equal
+    maxima the last index wins, as Rust's Iterator::max_by returns it."""
+    m = counting_qubits
+    if m > state.num_qubits():
+        raise ValueError("most_probable_phase: more counting qubits than the state has")
+    marg = state.marginal_low(m)
+    best = 0
+    for i in range(1, marg.shape[0]):
+        if not marg[best] > marg[i]:
+            best = i
+    return best / float(1 << m)

@@ -127,6 +127,14 @@ class State:
         N.check(N.lib().ev_fidelity(self._h, other._h, C.byref(out)))
         return out.value
 
+    def marginal_low(self, m: int) -> np.ndarray:
+        """Probabilities of the low m qubits summed over the others
+        (most_probable_phase's marginal, phase_estimation.rs:97-110), reduced
+        on the device; 2^m doubles come back."""
+        out = np.empty(1 << m, dtype=np.float64)
+        N.check(N.lib().ev_marginal_low(self._h, m, out.ctypes.data_as(C.POINTER(C.c_double))))
+        return out
+
     def bloch_vector(self, qubit: int) -> list:
         out = (C.c_double * 3)()
         N.check(N.lib().ev_bloch_vector(self._h, qubit, out))

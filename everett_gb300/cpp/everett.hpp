@@ -450,6 +450,13 @@ class State {
     check(ev_bloch_vector(h_.get(), qubit, b.data()));
     return b;
   }
+  // probabilities of the low m qubits summed over the others, in basis order
+  // (the marginal of phase_estimation.rs:97-110)
+  std::vector<double> marginal_low(size_t m) const {
+    std::vector<double> out(size_t(1) << m);
+    check(ev_marginal_low(h_.get(), m, out.data()));
+    return out;
+  }
   // full-register shots (bit q of a shot = qubit q); no reference counterpart
   std::vector<uint64_t> sample(uint64_t shots, uint64_t seed) {
     std::vector<uint64_t> out(shots);
@@ -565,6 +572,36 @@ inline Circuit teleport_state(Complex64 alpha, Complex64 beta) {  // teleport.rs
   c.gate1(prep, 0);
   c.compose(teleport_circuit());
   return c;
+}
+
+inline Circuit superdense_circuit(bool bit0, bool bit1) {  // superdense.rs:35-50
+  Circuit c = Circuit::with_classical(2, 2);
+  c.h(0).cnot(0, 1);
+  if (bit1) c.x(0);
+  if (bit0) c.z(0);
+  c.cnot(0, 1).h(0);
+  c.measure(0, 0).measure(1, 1);
+  return c;
+}
+
+inline Circuit phase_estimation(size_t m, double phi) {  // phase_estimation.rs:55-87
+  Circuit c(m + 1);
+  c.x(m);
+  for (size_t j = 0; j < m; ++j) c.h(j);
+  for (size_t j = 0; j < m; ++j)
+    c.controlled({j}, Gate1::phase(6.283185307179586 * phi * double(uint32_t(1) << j)), m);
+  c.compose(iqft(m));
+  return c;
+}
+
+// phase_estimation.rs:97-121; among equal maxima the last index wins, as
+// Rust's Iterator::max_by returns it
+inline double most_probable_phase(const State& state, size_t m) {
+  const std::vector<double> marg = state.marginal_low(m);
+  size_t best = 0;
+  for (size_t i = 1; i < marg.size(); ++i)
+    if (!(marg[best] > marg[i])) best = i;
+  return double(best) / double(marg.size());
 }
 
 }  // namespace algorithms

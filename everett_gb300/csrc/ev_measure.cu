@@ -622,6 +622,50 @@ extern "C" int ev_normalize(ev_state* s) {
   return EV_OK;
 }
 
+// Marginal distribution of the low m qubits: out[c] = sum over the high bits
+// t of norm_sqr(a[t * 2^m + c]), each sum taken in increasing t from 0.0 --
+// the order of the basis loop in phase_estimation.rs:97-110
+// (most_probable_phase).  One thread per c; the loads of a warp are
+// consecutive amplitudes.
+template <typename V>
+__global__ void __launch_bounds__(256)
+    k_marginal_low(const V* __restrict__ s, uint32_t m, uint64_t iters, double* __restrict__ out) {
+  const uint64_t c = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (c >= (uint64_t(1) << m)) return;
+  double acc = 0.0;
+  for (uint64_t t = 0; t < iters; ++t) acc = __dadd_rn(acc, nsq(s[(t << m) | c]));
+  out[c] = acc;
+}
+
+extern "C" int ev_marginal_low(const ev_state* s, uint64_t m, double* out) {
+  clear_error();
+  if (!s || !out) return fail(EV_ERR_INVALID_ARGUMENT, "ev_marginal_low: null argument");
+  if (m > s->n || m > 28)
+    return fail(EV_ERR_INVALID_ARGUMENT, "ev_marginal_low: %llu low qubits of a %llu-qubit state",
+                (unsigned long long)m, (unsigned long long)s->n);
+  EV_CUDA(cudaSetDevice(s->device));
+  const uint64_t count = uint64_t(1) << m;
+  double* d = nullptr;
+  EV_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d), count * sizeof(double), s->stream));
+  const unsigned grid = unsigned((count + 255) / 256);
+  const uint64_t iters = s->len() >> m;
+  if (s->dtype == EV_C128)
+    k_marginal_low<<<grid, 256, 0, s->stream>>>(static_cast<const double2*>(s->amps), uint32_t(m),
+                                                iters, d);
+  else
+    k_marginal_low<<<grid, 256, 0, s->stream>>>(static_cast<const float2*>(s->amps), uint32_t(m),
+                                                iters, d);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out, d, count * sizeof(double), cudaMemcpyDeviceToHost, s->stream);
+  cudaFreeAsync(d, s->stream);
+  const cudaError_t e2 = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess || e2 != cudaSuccess)
+    return fail(EV_ERR_CUDA, "ev_marginal_low: %s",
+                cudaGetErrorString(e != cudaSuccess ? e : e2));
+  return EV_OK;
+}
+
 // State::probability: one amplitude, norm_sqr on the host with std::fma
 // (state.rs:119-122).
 extern "C" int ev_probability(const ev_state* s, uint64_t basis, double* out) {

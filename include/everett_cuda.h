@@ -184,6 +184,10 @@ int ev_amplitude(const ev_state* s, uint64_t basis, double out[2]);
  * (both are promoted to f64). */
 int ev_overlap(const ev_state* self, const ev_state* other, double out[2]);
 int ev_fidelity(const ev_state* self, const ev_state* other, double* out);
+/* Marginal distribution of the low m qubits (m <= 28): out[c] (2^m
+ * doubles) = sum over the other qubits of |a[t * 2^m + c]|^2, summed in
+ * basis order as most_probable_phase does (phase_estimation.rs:97-110). */
+int ev_marginal_low(const ev_state* s, uint64_t m, double* out);
 /* [<X>, <Y>, <Z>] of one qubit (State::bloch_vector). */
 int ev_bloch_vector(const ev_state* s, uint64_t qubit, double out[3]);
 

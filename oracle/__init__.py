@@ -46,6 +46,7 @@ def lib(parallel: bool = False) -> C.CDLL:
         "oracle_normalize": ([P, U], None),
         "oracle_overlap": ([P, P, U, P], None),
         "oracle_bloch_vector": ([P, U, U, P], None),
+        "oracle_marginal_low": ([P, U, U, P], None),
         "oracle_pauli_expectation": ([P, U, U, U, C.c_int], C.c_double),
         "oracle_dm_run": ([P, P, U, P, P], C.c_int),
         "oracle_dm_from_amplitudes": ([P, U, P], None),
@@ -115,6 +116,23 @@ def bloch_vector(amps: np.ndarray, q: int) -> list:
     out = np.zeros(3)
     lib().oracle_bloch_vector(amps.ctypes.data, amps.shape[0], q, out.ctypes.data)
     return out.tolist()
+
+
+def marginal_low(amps: np.ndarray, m: int) -> np.ndarray:
+    out = np.zeros(1 << m)
+    lib().oracle_marginal_low(amps.ctypes.data, amps.shape[0], m, out.ctypes.data)
+    return out
+
+
+def most_probable_phase(amps: np.ndarray, m: int) -> float:
+    """phase_estimation.rs:97-121: the LAST index among equal maxima (Rust's
+    Iterator::max_by keeps the later of two equal elements)."""
+    marg = marginal_low(amps, m)
+    best = 0
+    for i in range(1, marg.shape[0]):
+        if not marg[i] < marg[best]:
+            best = i
+    return best / float(1 << m)
 
 
 def pauli_expectation(amps: np.ndarray, x_mask: int, z_mask: int, negative: bool = False) -> float:

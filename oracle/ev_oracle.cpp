@@ -366,6 +366,15 @@ void oracle_normalize(double* amps, uint64_t len) {  // state.rs:103-111
     for (uint64_t j = 0; j < len; ++j) a[j] = cscale(a[j], inv);
   }
 }
+// most_probable_phase's marginal (phase_estimation.rs:97-110): one pass over
+// the basis in increasing order, marginal[basis & (2^m - 1)] += norm_sqr, each
+// entry starting from 0.0.
+void oracle_marginal_low(const double* amps, uint64_t len, uint64_t m, double* out) {
+  const C* a = reinterpret_cast<const C*>(amps);
+  const uint64_t count = uint64_t(1) << m;
+  for (uint64_t c = 0; c < count; ++c) out[c] = 0.0;
+  for (uint64_t j = 0; j < len; ++j) out[j & (count - 1)] += norm_sqr(a[j]);
+}
 // <other|self> = sum conj(other_j) * self_j, accumulated from ZERO (state.rs:130-138).
 void oracle_overlap(const double* self, const double* other, uint64_t len, double* out) {
   const C* a = reinterpret_cast<const C*>(self);

@@ -1,7 +1,8 @@
 // Tests of the C++ host surface (everett_gb300/cpp/everett.hpp), written as
 // the reference's own Rust tests are (src/circuit.rs:331-384,
 // src/state.rs:188-240, src/rng.rs:61-90, tests/algorithms_prep.rs,
-// tests/algorithms_qft.rs, tests/algorithms_teleport.rs), plus checks that
+// tests/algorithms_qft.rs, tests/algorithms_teleport.rs,
+// tests/algorithms_phase_estimation.rs, tests/algorithms_superdense.rs), plus checks that
 // the C++ builder encodes what the engine's own circuit records hold.
 //
 // Usage: test_everett host|gpu   (host cases need no GPU)
@@ -325,6 +326,28 @@ static void teleport_is_seed_independent() {
   REQUIRE(seen[0] + seen[1] + seen[2] + seen[3] >= 2);
 }
 
+// tests/algorithms_phase_estimation.rs:12-36
+static void phase_estimation_recovers_phases() {
+  const std::vector<std::pair<size_t, double>> dyadic = {
+      {1, 0.5}, {2, 0.25}, {2, 0.75}, {3, 0.125}, {3, 0.875}, {4, 0.0}};
+  for (const auto& mp : dyadic) {
+    Execution ex = StateVectorBackend::run(algorithms::phase_estimation(mp.first, mp.second));
+    REQUIRE(std::fabs(algorithms::most_probable_phase(ex.state(), mp.first) - mp.second) < 1e-10);
+  }
+  Execution ex = StateVectorBackend::run(algorithms::phase_estimation(4, 0.3));
+  REQUIRE(std::fabs(algorithms::most_probable_phase(ex.state(), 4) - 0.3) <= 1.0 / 16.0 + 1e-10);
+}
+
+// tests/algorithms_superdense.rs:5-36
+static void superdense_decodes_both_bits() {
+  for (int b = 0; b < 4; ++b) {
+    const bool bit0 = b & 1, bit1 = b & 2;
+    Execution ex = StateVectorBackend::run(algorithms::superdense_circuit(bit0, bit1));
+    REQUIRE(ex.classical()[0] == bit0);
+    REQUIRE(ex.classical()[1] == bit1);
+  }
+}
+
 static void measurement_uses_the_seeded_uniforms() {
   // One measurement of |+>: the outcome is 1 exactly when the seed's first
   // uniform is below P(1) = |1/sqrt 2|^2 (measure.rs measure_qubit).
@@ -395,6 +418,8 @@ int main(int argc, char** argv) {
       {"qft_of_basis_one_matches_closed_form", qft_of_basis_one_matches_closed_form},
       {"teleport_cases", teleport_cases},
       {"teleport_is_seed_independent", teleport_is_seed_independent},
+      {"phase_estimation_recovers_phases", phase_estimation_recovers_phases},
+      {"superdense_decodes_both_bits", superdense_decodes_both_bits},
       {"measurement_uses_the_seeded_uniforms", measurement_uses_the_seeded_uniforms},
       {"trotter_norm_is_kept", trotter_norm_is_kept},
       {"gpu_run_errors_are_typed", gpu_run_errors_are_typed},

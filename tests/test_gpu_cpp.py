@@ -1,5 +1,5 @@
-"""The C++ host surface on the GPU: the reference's state, preparation, QFT
-and teleportation tests written in C++ against everett.hpp and run through
+"""The C++ host surface on the GPU: the reference's state, preparation, QFT,
+teleportation, phase-estimation and superdense tests written in C++ against everett.hpp and run through
 the engine (tests/cpp/test_everett.cpp, group "gpu")."""
 import subprocess
 
@@ -17,4 +17,4 @@ def test_cpp_gpu_cases(gpu, tmp_path_factory):
         pytest.fail(f"C++ test program failed to build:\n{e.stderr}")
     r = run_group(exe, "gpu")
     assert r.returncode == 0, r.stdout + r.stderr
-    assert "15 run, 0 failed" in r.stdout, r.stdout
+    assert "17 run, 0 failed" in r.stdout, r.stdout

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from everett_gb300 import Circuit, CudaStateVectorBackend, PauliString, State, workloads
+from everett_gb300 import Circuit, algorithms, CudaStateVectorBackend, PauliString, State, workloads
 from everett_gb300.error import QubitOutOfRange
 
 pytestmark = pytest.mark.gpu
@@ -76,3 +76,30 @@ def test_pauli_expectation_rejects_foreign_qubits(gpu):
     rc = N.lib().ev_pauli_expectation(st.handle, xm.ctypes.data, zm.ctypes.data, None, 1,
                                       out.ctypes.data)
     assert rc == N.ERR_QUBIT_OUT_OF_RANGE
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_marginal_low_and_phase_estimation(gpu, dtype):
+    """most_probable_phase's marginal as a device reduction: identical to the
+    oracle's basis-order sums in complex128 (1e-12 in complex64, against the
+    oracle on the same complex64 amplitudes), and the reference's
+    phase-estimation and superdense assertions hold on the GPU
+    (algorithms_phase_estimation.rs:12-36, algorithms_superdense.rs:5-36)."""
+    for n, m in [(1, 0), (6, 3), (12, 12), (17, 5)]:
+        amps = O.sample_state(n) if n > 1 else np.array([0.6, 0.8j])
+        st = State.from_amplitudes(amps, dtype=dtype)
+        got = st.marginal_low(m)
+        want = O.marginal_low(np.ascontiguousarray(st.amplitudes(), dtype=np.complex128), m)
+        if dtype == "complex128":
+            assert np.array_equal(got, want), (n, m)
+        else:
+            assert np.max(np.abs(got - want)) < 1e-12, (n, m)
+    for m, phi in [(1, 0.5), (2, 0.25), (2, 0.75), (3, 0.125), (3, 0.875), (4, 0.0)]:
+        ex = CudaStateVectorBackend.run(algorithms.phase_estimation(m, phi))
+        assert abs(algorithms.most_probable_phase(ex.state(), m) - phi) < 1e-10
+    ex = CudaStateVectorBackend.run(algorithms.phase_estimation(4, 0.3))
+    assert abs(algorithms.most_probable_phase(ex.state(), 4) - 0.3) <= 1.0 / 16.0 + 1e-10
+    for b0 in (False, True):
+        for b1 in (False, True):
+            ex = CudaStateVectorBackend.run(algorithms.superdense_circuit(b0, b1))
+            assert list(ex.classical()) == [b0, b1]

@@ -369,3 +369,34 @@ def test_tiled_integer_pipe_levels_bit_exact(gpu, monkeypatch, level):
     rl = workloads.random_layers(14, 6, 5)
     want, _, _ = O.run_seeded(rl, 0, parallel=True)
     assert exact(CudaStateVectorBackend.run(rl, mode="tiled").state().amplitudes(), want), level
+
+
+def test_gates_on_mixed_range_amplitudes_bit_exact(gpu):
+    """The complex128 gate kernels form plain products on the integer pipes
+    for operands in a normal range and fall back pair by pair otherwise: a
+    state mixing zeros, signed zeros, tiny (1e-200) and huge (1e200) parts and
+    ordinary values gives the oracle's bits for every 1-qubit kind, plain and
+    controlled."""
+    rng = np.random.default_rng(23)
+    n = 9
+    base = O.sample_state(n)
+    pick = rng.integers(0, 6, size=(1 << n, 2))
+    parts = base.view(np.float64).reshape(-1, 2).copy()
+    parts[pick == 1] = 0.0
+    parts[pick == 2] = -0.0
+    parts[pick == 3] *= 1e-200
+    parts[pick == 4] *= 1e200
+    mixed = parts.reshape(-1).view(np.complex128).copy()
+    st = State.from_amplitudes(mixed)
+    for k in range(n):
+        for g in GATES_1Q:
+            st.upload(mixed)
+            st.apply_1q(k, g)
+            want = mixed.copy()
+            O.apply_1q(want, k, g)
+            assert exact(st.amplitudes(), want), (k, g)
+            st.upload(mixed)
+            st.apply_controlled_1q([(k + 1) % n], k, g)
+            want = mixed.copy()
+            O.apply_controlled_1q(want, [(k + 1) % n], k, g)
+            assert exact(st.amplitudes(), want), ("ctrl", k, g)

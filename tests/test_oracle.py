@@ -267,6 +267,34 @@ def test_teleport_bloch(alpha, beta):  # algorithms_teleport.rs:40-91
         assert max(abs(g - w) for g, w in zip(got, want)) < 1e-10
 
 
+@pytest.mark.parametrize("m,phi", [(1, 0.5), (2, 0.25), (2, 0.75), (3, 0.125), (3, 0.875),
+                                   (4, 0.0)])
+def test_phase_estimation_dyadic(m, phi):  # algorithms_phase_estimation.rs:12-36
+    amps, _, rc = O.run_seeded(algorithms.phase_estimation(m, phi), 0)
+    assert rc == 0
+    assert abs(O.most_probable_phase(amps, m) - phi) < 1e-10
+
+
+def test_phase_estimation_non_dyadic():  # algorithms_phase_estimation.rs:22-29
+    amps, _, _ = O.run_seeded(algorithms.phase_estimation(4, 0.3), 0)
+    assert abs(O.most_probable_phase(amps, 4) - 0.3) <= 1.0 / 16.0 + 1e-10
+
+
+def test_most_probable_phase_ties_take_last():
+    """Iterator::max_by keeps the later of equal elements: a uniform
+    marginal gives the last index."""
+    amps = np.full(8, 1 / math.sqrt(8), dtype=np.complex128)
+    assert O.most_probable_phase(amps, 2) == 3 / 4
+
+
+@pytest.mark.parametrize("bit0,bit1", [(False, False), (False, True), (True, False), (True, True)])
+def test_superdense(bit0, bit1):  # algorithms_superdense.rs:5-36
+    for seed in range(4):
+        _, cl, rc = O.run_seeded(algorithms.superdense_circuit(bit0, bit1), seed)
+        assert rc == 0
+        assert list(cl) == [bit0, bit1]
+
+
 # ---- rng.rs:62-95 plus cross-implementation agreement ------------------------
 
 def test_rng_properties_and_agreement():
