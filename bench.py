@@ -76,7 +76,8 @@ def parse_args():
                     help="run one section alone (for profiling): the complex64 fused or tiled "
                          "path on the random-layer circuit, the TFIM batch, the serving mix, "
                          "prepared-graph replay, or each streaming kernel class alone")
-    ap.add_argument("--variant", default="bf16x3", choices=["bf16x3", "tf32x3", "fp32"])
+    ap.add_argument("--variant", default="bf16x3", choices=["bf16x3", "tf32x3", "fp32", "ozaki"],
+                    help="fused arithmetic for --case fused (ozaki: the complex128 one)")
     return ap.parse_args()
 
 
@@ -834,13 +835,14 @@ def run_case(args):
         return
     L = N.lib()
     c = workloads.random_layers(args.qubits, args.depth, seed=1)
-    st = State.zero(args.qubits, "complex64")
+    dtype = "complex128" if args.case == "fused" and args.variant == "ozaki" else "complex64"
+    st = State.zero(args.qubits, dtype)
     kw = (dict(mode="fused", variant=args.variant, tile_bits=args.fuse_bits) if args.case == "fused"
           else dict(mode="tiled"))
     for _ in range(args.warmup):
         timed_runs(L, N, st, c, 1, **kw)
     ms, prof = timed_runs(L, N, st, c, args.steps, **kw)
-    print(json.dumps({"case": args.case, "qubits": args.qubits, "depth": args.depth, **kw,
+    print(json.dumps({"case": args.case, "qubits": args.qubits, "depth": args.depth, "dtype": dtype, **kw,
                       "ms_per_run": round(ms, 3), "kernel_profile": prof}))
 
 

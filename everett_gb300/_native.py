@@ -25,7 +25,7 @@ assert OP_DTYPE.itemsize == 288
 OP_APPLY1, OP_APPLY2, OP_CONTROLLED, OP_MEASURE, OP_IF = 1, 2, 3, 4, 5
 C128, C64 = 0, 1
 MODE_EXACT, MODE_TILED, MODE_FUSED = 0, 1, 2
-FUSED_TF32X3, FUSED_BF16X3, FUSED_FP32 = 0, 1, 2
+FUSED_TF32X3, FUSED_BF16X3, FUSED_FP32, FUSED_OZAKI = 0, 1, 2, 3
 
 OK = 0
 ERR_QUBIT_OUT_OF_RANGE = 1
@@ -85,6 +85,7 @@ _SIGS = {
     "ev_validate": [C.POINTER(EvCircuit)],
     "ev_run_seeded": [C.POINTER(EvCircuit), _U64, C.POINTER(EvRunOptions), C.POINTER(_P), _P],
     "ev_state_run": [_P, C.POINTER(EvCircuit), _U64, C.POINTER(EvRunOptions), _P],
+    "ev_state_drive": [_P, C.POINTER(EvCircuit), _U64, C.POINTER(EvRunOptions), _P],
     "ev_sample": [_P, _U64, _U64, _P],
     "ev_state_record_event": [_P, _I32],
     "ev_state_elapsed_ms": [_P, _I32, _I32, C.POINTER(C.c_float)],
@@ -128,6 +129,7 @@ _SIGS = {
     "ev_probe_fp64": [_DP],
     "ev_marginal_low": [_P, _U64, _DP],
     "ev_softfp_check": [_U64, _U64, C.POINTER(_U64)],
+    "ev_ozaki_gemm_host": [_DP, _U64, _DP, _DP],
     "ev_max_abs_diff": [_P, _P, _DP],
     "ev_host_alloc": [_U64, C.POINTER(_P)],
     "ev_host_free": [_P],

@@ -23,8 +23,9 @@ _DTYPES = {"complex128": N.C128, "c128": N.C128, "complex64": N.C64, "c64": N.C6
 _MODES = {"exact": N.MODE_EXACT, "tiled": N.MODE_TILED, "fused": N.MODE_FUSED,
           N.MODE_EXACT: N.MODE_EXACT, N.MODE_TILED: N.MODE_TILED, N.MODE_FUSED: N.MODE_FUSED}
 _VARIANTS = {"tf32x3": N.FUSED_TF32X3, "bf16x3": N.FUSED_BF16X3, "fp32": N.FUSED_FP32,
+             "ozaki": N.FUSED_OZAKI,
              N.FUSED_TF32X3: N.FUSED_TF32X3, N.FUSED_BF16X3: N.FUSED_BF16X3,
-             N.FUSED_FP32: N.FUSED_FP32}
+             N.FUSED_FP32: N.FUSED_FP32, N.FUSED_OZAKI: N.FUSED_OZAKI}
 
 
 class State:
@@ -202,7 +203,7 @@ class PreparedRun:
     """
 
     def __init__(self, state: State, circuit: Circuit, mode="exact", tile_bits=0,
-                 variant="tf32x3"):
+                 variant=None):
         c = circuit.ev_struct()
         opts = _options(state.dtype(), mode, tile_bits, variant)
         h = C.c_void_p()
@@ -237,11 +238,13 @@ class PreparedRun:
         self.close()
 
 
-def _options(dtype, mode, tile_bits, variant="tf32x3") -> N.EvRunOptions:
+def _options(dtype, mode, tile_bits, variant=None) -> N.EvRunOptions:
     o = N.EvRunOptions()
     o.dtype = _DTYPES[dtype]
     o.mode = _MODES[mode]
     o.tile_bits = int(tile_bits)
+    if variant is None:  # the fused arithmetic of the state's type
+        variant = "ozaki" if o.dtype == N.C128 else "tf32x3"
     o.variant = _VARIANTS[variant]
     return o
 
@@ -260,16 +263,18 @@ class CudaStateVectorBackend:
 
     @classmethod
     def run(cls, circuit: Circuit, dtype="complex128", mode="exact", tile_bits=0,
-            variant="tf32x3") -> Execution:
+            variant=None) -> Execution:
         """mode: "exact" (one kernel per op), "tiled" (runs of ops per
-        shared-memory pass) or "fused" (complex64: dense k-qubit unitaries,
-        k = tile_bits, arithmetic = variant "tf32x3" | "bf16x3" | "fp32")."""
+        shared-memory pass) or "fused" (dense k-qubit unitaries, k =
+        tile_bits; complex64 arithmetic = variant "tf32x3" (default) |
+        "bf16x3" | "fp32", complex128 = "ozaki": 5-qubit unitaries on the
+        tensor cores by 8-bit digit slicing)."""
         return cls.run_seeded(circuit, 0, dtype=dtype, mode=mode, tile_bits=tile_bits,
                               variant=variant)
 
     @classmethod
     def run_seeded(cls, circuit: Circuit, seed: int, dtype="complex128", mode="exact",
-                   tile_bits=0, variant="tf32x3") -> Execution:
+                   tile_bits=0, variant=None) -> Execution:
         c = circuit.ev_struct()
         opts = _options(dtype, mode, tile_bits, variant)
         h = C.c_void_p()
@@ -281,7 +286,7 @@ class CudaStateVectorBackend:
 
     @staticmethod
     def run_into(state: State, circuit: Circuit, seed: int = 0, mode="exact",
-                 tile_bits=0, variant="tf32x3") -> list:
+                 tile_bits=0, variant=None) -> list:
         """Runs a circuit on an existing state (reset to |0...0> first)."""
         c = circuit.ev_struct()
         opts = _options(state.dtype(), mode, tile_bits, variant)
@@ -292,8 +297,21 @@ class CudaStateVectorBackend:
         return [bool(b) for b in classical[:ncl]]
 
     @staticmethod
+    def drive(state: State, circuit: Circuit, seed: int = 0, mode="exact",
+              tile_bits=0, variant=None) -> list:
+        """Applies a circuit's ops to the state as it stands (drive,
+        backend/mod.rs:43-72); returns the classical register."""
+        c = circuit.ev_struct()
+        opts = _options(state.dtype(), mode, tile_bits, variant)
+        ncl = circuit.num_classical()
+        classical = np.zeros(max(1, ncl), dtype=np.uint8)
+        N.check(N.lib().ev_state_drive(state.handle, C.byref(c), seed, C.byref(opts),
+                                       classical.ctypes.data))
+        return [bool(b) for b in classical[:ncl]]
+
+    @staticmethod
     def prepare(state: State, circuit: Circuit, mode="exact", tile_bits=0,
-                variant="tf32x3") -> PreparedRun:
+                variant=None) -> PreparedRun:
         """Plans a circuit for a state once and records it as a CUDA graph;
         each ``launch(seed)`` of the result equals ``run_into`` with that
         seed."""

@@ -266,8 +266,10 @@ static int build_plan(ev_state* s, const ev_circuit* c, const ev_run_options* o,
   const int mode = o ? o->mode : EV_MODE_EXACT;
   const int tile_bits = o ? o->tile_bits : 0;
   const int variant = o ? o->variant : 0;
-  if (mode == EV_MODE_FUSED && s->dtype != EV_C64)
-    return fail(EV_ERR_INVALID_ARGUMENT, "fused mode needs complex64 amplitudes");
+  if (mode == EV_MODE_FUSED && (variant == EV_FUSED_OZAKI) != (s->dtype == EV_C128))
+    return fail(EV_ERR_INVALID_ARGUMENT, variant == EV_FUSED_OZAKI
+                                             ? "the ozaki fused variant needs complex128 amplitudes"
+                                             : "fused mode needs complex64 amplitudes");
   if (mode < EV_MODE_EXACT || mode > EV_MODE_FUSED)
     return fail(EV_ERR_INVALID_ARGUMENT, "unknown run mode %d", mode);
   plan->stream = s->stream;
@@ -658,6 +660,23 @@ extern "C" int ev_state_run(ev_state* s, const ev_circuit* c, uint64_t seed,
     return fail(EV_ERR_INVALID_ARGUMENT, "ev_state_run: null classical output");
   EV_CUDA(cudaSetDevice(s->device));
   EV_TRY(state_zero(s));
+  return run_ops(s, c, seed, opts, classical_out);
+}
+
+// backend/mod.rs:43-72 (drive): the op walk on the state as it stands.
+extern "C" int ev_state_drive(ev_state* s, const ev_circuit* c, uint64_t seed,
+                              const ev_run_options* opts, uint8_t* classical_out) {
+  clear_error();
+  if (!s) return fail(EV_ERR_INVALID_ARGUMENT, "ev_state_drive: null state");
+  EV_TRY(validate(c));
+  if (c->num_qubits != s->n)
+    return fail(EV_ERR_DIMENSION_MISMATCH, "circuit has %llu qubits, state has %llu",
+                (unsigned long long)c->num_qubits, (unsigned long long)s->n);
+  if (opts && opts->dtype != s->dtype)
+    return fail(EV_ERR_INVALID_ARGUMENT, "run options name a different amplitude type");
+  if (c->num_classical && !classical_out)
+    return fail(EV_ERR_INVALID_ARGUMENT, "ev_state_drive: null classical output");
+  EV_CUDA(cudaSetDevice(s->device));
   return run_ops(s, c, seed, opts, classical_out);
 }
 

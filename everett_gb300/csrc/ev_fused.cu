@@ -37,6 +37,7 @@
 
 #include "ev_device.cuh"
 #include "ev_internal.h"
+#include "ev_ozaki.cuh"
 
 namespace ev {
 
@@ -852,6 +853,241 @@ __global__ void __launch_bounds__(kTmaThreads)
   }
 }
 
+// ---- tcgen05 kernel, complex128 by digit slicing (ev_ozaki.cuh) ---------------
+//
+// One CTA per SM: seven A digit slices of 16 KiB, seven B digit slices of
+// 8 KiB and 448 TMEM columns (seven diagonal accumulators of 128 x 64 f32).
+// Thread t owns row t mod 128 and the four groups of four amplitudes
+// g = t/128 + 2 gi, as in k_fused_tc; the two threads of a row exchange their
+// largest exponent through shared memory.  A step: digits of the rows into
+// the seven A slices (one 16-byte chunk per group and slice), then the rows
+// of the next step are loaded into the same registers so that their latency
+// hides behind the MMAs; one thread issues the MMAs of the output half
+// n < 32 (28 digit pairs x 4 K-steps, N = 32) and commits them to bar[0],
+// then those of n >= 32 to bar[1].  Warps 0-3 recombine the first half
+// while the tensor core still computes the second; warps 4-7 the second.
+// Every wait is bounded; on timeout the kernel records an error, frees TMEM
+// and returns.
+
+constexpr int kOzThreads = 256;
+
+struct OzShape {
+  static constexpr int K = oz::kK;
+  static constexpr int A_SLICE = kRows * K * 2;  // 128 rows x 64 BF16
+  static constexpr int B_SLICE = K * K * 2;      // 64 x 64 BF16
+  static constexpr int SMEM = oz::kDigits * (A_SLICE + B_SLICE) + 1024;
+  static constexpr int TMEM_COLS = 512;
+  static constexpr int BLOB = oz::kDigits * B_SLICE + K * 4;  // B slices, column exponents
+};
+
+// f32 bits of (byte - 128) for the byte of w that sel (0x7440 | byte) picks.
+__device__ __forceinline__ uint32_t oz_byte_digit(uint32_t w, uint32_t sel) {
+  return __float_as_uint(
+      __fadd_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, sel)), -8388736.0f));
+}
+
+// The seven BF16 digits of re and im (row exponent E), packed per slice as
+// one 32-bit word [re digit | im digit << 16].
+__device__ __forceinline__ void oz_digits_pair(double re, double im, int E, uint32_t w[7]) {
+  const int64_t m0 = oz::fixed55(uint32_t(__double2hiint(re)), uint32_t(__double2loint(re)), E);
+  const int64_t m1 = oz::fixed55(uint32_t(__double2hiint(im)), uint32_t(__double2loint(im)), E);
+  const uint64_t b0 = uint64_t(m0) + oz::kBias, b1 = uint64_t(m1) + oz::kBias;
+  const uint32_t l0 = uint32_t(b0), h0 = uint32_t(b0 >> 32);
+  const uint32_t l1 = uint32_t(b1), h1 = uint32_t(b1 >> 32);
+  const float t0 = __fadd_rn(__int_as_float(0x4B400000 + (int32_t(h0) >> 16)), -12582912.0f);
+  const float t1 = __fadd_rn(__int_as_float(0x4B400000 + (int32_t(h1) >> 16)), -12582912.0f);
+  w[0] = __byte_perm(__float_as_uint(t0), __float_as_uint(t1), 0x7632);
+  w[1] = __byte_perm(oz_byte_digit(h0, 0x7441), oz_byte_digit(h1, 0x7441), 0x7632);
+  w[2] = __byte_perm(oz_byte_digit(h0, 0x7440), oz_byte_digit(h1, 0x7440), 0x7632);
+  w[3] = __byte_perm(oz_byte_digit(l0, 0x7443), oz_byte_digit(l1, 0x7443), 0x7632);
+  w[4] = __byte_perm(oz_byte_digit(l0, 0x7442), oz_byte_digit(l1, 0x7442), 0x7632);
+  w[5] = __byte_perm(oz_byte_digit(l0, 0x7441), oz_byte_digit(l1, 0x7441), 0x7632);
+  w[6] = __byte_perm(oz_byte_digit(l0, 0x7440), oz_byte_digit(l1, 0x7440), 0x7632);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+template <int d>
+__device__ __forceinline__ void oz_add_diag(uint32_t lane_tmem, int c0, int64_t acc[16]) {
+  uint32_t w[16];
+  tmem_ld16(lane_tmem + uint32_t(d * oz::kK + c0), w);
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int c = 0; c < 16; ++c) oz::accumulate<d>(acc[c], __uint_as_float(w[c]));
+}
+
+__global__ void __launch_bounds__(kOzThreads, 1)
+    k_fused_oz(double2* __restrict__ s, const FusedDesc* __restrict__ gd,
+               const unsigned char* __restrict__ bmat, int* __restrict__ err) {
+  using Sh = OzShape;
+  constexpr int K = Sh::K;
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ FusedDesc d;
+  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int fexp[K];
+  __shared__ int rexp[2][kRows];
+  unsigned char* sm = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  unsigned char* a_sl = sm;
+  unsigned char* b_sl = sm + oz::kDigits * Sh::A_SLICE;
+  const int tid = threadIdx.x, warp = tid >> 5;
+
+  for (int i = tid; i < int(sizeof(FusedDesc) / 8); i += blockDim.x)
+    reinterpret_cast<uint64_t*>(&d)[i] = reinterpret_cast<const uint64_t*>(gd)[i];
+  {
+    const uint16_t* src = reinterpret_cast<const uint16_t*>(bmat);
+    for (int e = tid; e < oz::kDigits * K * K; e += blockDim.x) {
+      const int j = e / (K * K), rem = e % (K * K);
+      *reinterpret_cast<uint16_t*>(b_sl + j * Sh::B_SLICE + sw128_off(rem / K, rem % K, K, 2)) =
+          src[e];
+    }
+    const int* fe = reinterpret_cast<const int*>(bmat + oz::kDigits * Sh::B_SLICE);
+    for (int n = tid; n < K; n += blockDim.x) fexp[n] = fe[n];
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[0])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[1])));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_addr(&tmem_slot)),
+                 "r"(uint32_t(Sh::TMEM_COLS)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_slot;
+  // f32 accumulate, BF16 A and B, K-major, N = 32, M = 128
+  const uint32_t idesc =
+      (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(32 >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
+  uint32_t phase = 0;
+  bool ok = true;
+  const int quarter = warp & 3, half = warp >> 2;
+  const int row = quarter * 32 + (tid & 31);
+  const uint32_t rsw = uint32_t((row >> 3) * 1024 + (row & 7) * 128);
+  const uint32_t rx = uint32_t(row & 7);
+  const uint64_t roff = d.rtab[row];
+  const uint32_t lane_tmem = tmem + (uint32_t(quarter * 32) << 16);
+  double2 x[4][4];
+  uint64_t step = blockIdx.x;
+  if (step < d.nsteps) {
+    const uint64_t rb = step_base(d, step) | roff;
+#pragma unroll
+    for (int gi = 0; gi < 4; ++gi)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) x[gi][i] = __ldcs(s + (rb | d.ftab[4 * (half + 2 * gi) + i]));
+  }
+  for (; step < d.nsteps && ok; step += gridDim.x) {
+    const uint64_t rbase = step_base(d, step) | roff;
+    int em = 0;
+#pragma unroll
+    for (int gi = 0; gi < 4; ++gi)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        em = max(em, oz::exp_of(uint32_t(__double2hiint(x[gi][i].x))));
+        em = max(em, oz::exp_of(uint32_t(__double2hiint(x[gi][i].y))));
+      }
+    rexp[half][row] = em;
+    __syncthreads();
+    em = max(rexp[0][row], rexp[1][row]);
+#pragma unroll
+    for (int gi = 0; gi < 4; ++gi) {
+      const int g = half + 2 * gi;  // reals 8g..8g+7: chunk g of the row's 128-byte line
+      const uint32_t o = rsw + ((uint32_t(g) ^ rx) << 4);
+      uint32_t w[4][7];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) oz_digits_pair(x[gi][i].x, x[gi][i].y, em, w[i]);
+#pragma unroll
+      for (int sl = 0; sl < oz::kDigits; ++sl)
+        *reinterpret_cast<uint4*>(a_sl + sl * Sh::A_SLICE + o) =
+            make_uint4(w[0][sl], w[1][sl], w[2][sl], w[3][sl]);
+    }
+    // the next step's rows, in flight during the MMAs and the recombination
+    const uint64_t nstep = step + gridDim.x;
+    if (nstep < d.nsteps) {
+      const uint64_t nb = step_base(d, nstep) | roff;
+#pragma unroll
+      for (int gi = 0; gi < 4; ++gi)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) x[gi][i] = __ldcs(s + (nb | d.ftab[4 * (half + 2 * gi) + i]));
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (tid == 0) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = smem_addr(a_sl), b0 = smem_addr(b_sl);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+#pragma unroll
+        for (int dg = 0; dg < oz::kDigits; ++dg)
+#pragma unroll
+          for (int i = 0; i <= dg; ++i) {
+            const int j = dg - i;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk)
+              mma_bf16(tmem + uint32_t(dg * K + h * 32),
+                       sw128_desc(a0 + uint32_t(i * Sh::A_SLICE + kk * 32)),
+                       sw128_desc(b0 + uint32_t(j * Sh::B_SLICE + h * 32 * 128 + kk * 32)), idesc,
+                       (i | kk) != 0);
+          }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_addr(&bar[h]))
+            : "memory");
+      }
+    }
+    if (!mbar_wait(&bar[half], phase, kWaitLimit)) {
+      ok = false;
+      atomicExch(err, 1);
+      break;
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 16) {
+      int64_t acc[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) acc[c] = 0;
+      oz_add_diag<0>(lane_tmem, c0, acc);
+      oz_add_diag<1>(lane_tmem, c0, acc);
+      oz_add_diag<2>(lane_tmem, c0, acc);
+      oz_add_diag<3>(lane_tmem, c0, acc);
+      oz_add_diag<4>(lane_tmem, c0, acc);
+      oz_add_diag<5>(lane_tmem, c0, acc);
+      oz_add_diag<6>(lane_tmem, c0, acc);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const int n = c0 + 2 * j;
+        const double re = oz::scaled(acc[2 * j], em + fexp[n] - oz::kPow2Bias);
+        const double im = oz::scaled(acc[2 * j + 1], em + fexp[n + 1] - oz::kPow2Bias);
+        __stcs(s + (rbase | d.ftab[n >> 1]), make_double2(re, im));
+      }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    // the A slices are rewritten next step: every MMA of this one must be done
+    if (half == 0 && !mbar_wait(&bar[1], phase, kWaitLimit)) {
+      ok = false;
+      atomicExch(err, 1);
+      break;
+    }
+    phase ^= 1;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(uint32_t(Sh::TMEM_COLS)));
+  }
+}
+
 // ---- host: launch ---------------------------------------------------------------
 
 static uint32_t tf32_hi_bits(float x) {
@@ -906,6 +1142,70 @@ static void build_bmat(const Block& b, int variant, std::vector<unsigned char>* 
       lo[e] = bf16_rn(float(Wt[e] - double(bf16_f(h))));
     }
   }
+}
+
+// BF16 bits of a small integer (|v| <= 256: exact in BF16).
+static uint16_t bf16_of_int(int v) {
+  const float f = float(v);
+  uint32_t u;
+  std::memcpy(&u, &f, 4);
+  return uint16_t(u >> 16);
+}
+
+// Digit-sliced operand of W^T for the complex128 pass: row n of W^T (column n
+// of W) is scaled by its own largest biased exponent F_n and written as seven
+// BF16 digit slices [N][K] (slice 0 = most significant), followed by the 64
+// exponents F_n (ev_ozaki.cuh).
+static void oz_slice_columns(const double* Wt, std::vector<unsigned char>* out) {
+  constexpr int K = oz::kK;
+  out->assign(OzShape::BLOB, 0);
+  uint16_t* sl = reinterpret_cast<uint16_t*>(out->data());
+  int32_t* fe = reinterpret_cast<int32_t*>(out->data() + oz::kDigits * OzShape::B_SLICE);
+  for (int n = 0; n < K; ++n) {
+    int E = 0;
+    for (int k = 0; k < K; ++k) {
+      uint64_t u;
+      std::memcpy(&u, &Wt[size_t(n) * K + k], 8);
+      E = std::max(E, oz::exp_of(uint32_t(u >> 32)));
+    }
+    fe[n] = E;
+    for (int k = 0; k < K; ++k) {
+      uint64_t u;
+      std::memcpy(&u, &Wt[size_t(n) * K + k], 8);
+      const int64_t M = oz::fixed55(uint32_t(u >> 32), uint32_t(u), E);
+      for (int i = 0; i < oz::kDigits; ++i)
+        sl[size_t(i) * K * K + size_t(n) * K + k] = bf16_of_int(oz::digit(M, i));
+    }
+  }
+}
+
+static void build_bmat_oz(const Block& b, std::vector<unsigned char>* out) {
+  const int D = 1 << b.F.size(), K = 2 * D;
+  std::vector<double> Wt(size_t(K) * K);
+  for (int a = 0; a < D; ++a)
+    for (int f = 0; f < D; ++f) {
+      const cd u = b.U[size_t(a) * D + f];
+      Wt[size_t(2 * a) * K + 2 * f] = u.real();
+      Wt[size_t(2 * a) * K + 2 * f + 1] = -u.imag();
+      Wt[size_t(2 * a + 1) * K + 2 * f] = u.imag();
+      Wt[size_t(2 * a + 1) * K + 2 * f + 1] = u.real();
+    }
+  oz_slice_columns(Wt.data(), out);
+}
+
+static int launch_oz(ev_state* s, const FusedDesc* dd, const unsigned char* db, uint64_t nsteps,
+                     int* derr) {
+  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_fused_oz)));
+  uint64_t grid = uint64_t(s->num_sms);  // one CTA per SM (shared memory and TMEM)
+  if (grid > nsteps) grid = nsteps;
+  s->tc_ctas_per_sm = 1;
+  if (debug_enabled())
+    fprintf(stderr, "[ev] k_fused_oz smem %d per CTA, grid %llu\n", OzShape::SMEM,
+            (unsigned long long)grid);
+  k_fused_oz<<<unsigned(grid), kOzThreads, OzShape::SMEM, s->stream>>>(
+      static_cast<double2*>(s->amps), dd, db, derr);
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
 }
 
 template <int KB, int VAR>
@@ -989,7 +1289,7 @@ int fused_width(int variant, int kbits) {
   int k = kbits > 0 ? kbits : default_fused_bits();
   if (k > 6) k = 6;
   if (k < 1) k = 1;
-  if (variant == EV_FUSED_TF32X3) return 5;
+  if (variant == EV_FUSED_TF32X3 || variant == EV_FUSED_OZAKI) return 5;
   if (variant == EV_FUSED_BF16X3) return k >= 6 ? 6 : 5;
   return k;
 }
@@ -998,9 +1298,12 @@ int fused_width(int variant, int kbits) {
 // images go into the blob.
 static int plan_fused(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int kbits,
                       int variant, PlanBlob* blob, std::vector<SegStep>* out) {
-  if (s->dtype != EV_C64) return fail(EV_ERR_INVALID_ARGUMENT, "fused mode needs a complex64 state");
-  if (variant < EV_FUSED_TF32X3 || variant > EV_FUSED_FP32)
+  if (variant < EV_FUSED_TF32X3 || variant > EV_FUSED_OZAKI)
     return fail(EV_ERR_INVALID_ARGUMENT, "unknown fused variant %d", variant);
+  if ((variant == EV_FUSED_OZAKI) != (s->dtype == EV_C128))
+    return fail(EV_ERR_INVALID_ARGUMENT,
+                variant == EV_FUSED_OZAKI ? "the ozaki fused variant needs a complex128 state"
+                                          : "this fused variant needs a complex64 state");
   const int n = int(s->n);
   const int k = fused_width(variant, kbits);
   // registers too small for 128-row steps run through the tile pass
@@ -1010,11 +1313,14 @@ static int plan_fused(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t
   // the measured comparison in the design notes) or the warp-specialised
   // TMA-staged pipeline (EV_FUSED_STAGING=tma), read when a run is planned.
   const char* staging = getenv("EV_FUSED_STAGING");
-  const bool use_tma = staging != nullptr && std::strcmp(staging, "tma") == 0;
+  const bool use_tma = staging != nullptr && std::strcmp(staging, "tma") == 0 &&
+                       variant != EV_FUSED_OZAKI;
   std::vector<Block> blocks = fuse_ops(c, first, last, n, k);
   std::vector<unsigned char> mat;
   for (const Block& b : blocks) {
-    if (tc) {
+    if (variant == EV_FUSED_OZAKI) {
+      build_bmat_oz(b, &mat);
+    } else if (tc) {
       build_bmat(b, variant, &mat);
     } else {
       const int D = 1 << b.F.size();
@@ -1042,10 +1348,11 @@ int launch_fused_step(ev_state* s, const SegStep& st, const unsigned char* dblob
   const FusedDesc* dd = reinterpret_cast<const FusedDesc*>(dblob + st.off0);
   const unsigned char* dm = dblob + st.off1;
   int* derr = reinterpret_cast<int*>(s->scratch.counter + 1);
-  ProfScope prof(s, P_FUSED, 2.0 * double(s->len()) * 8.0);
+  ProfScope prof(s, P_FUSED, 2.0 * double(s->len()) * (s->dtype == EV_C128 ? 16.0 : 8.0));
   s->launches += 1;
   const uint64_t nsteps = st.count;
   const bool tma = st.tma != 0;
+  if (st.variant == EV_FUSED_OZAKI) return launch_oz(s, dd, dm, nsteps, derr);
   if (st.variant == EV_FUSED_TF32X3)
     return tma ? launch_tma<5, EV_FUSED_TF32X3, 3>(s, dd, dm, nsteps, derr)
                : launch_tc<5, EV_FUSED_TF32X3>(s, dd, dm, nsteps, derr);
@@ -1066,6 +1373,62 @@ int launch_fused_step(ev_state* s, const SegStep& st, const unsigned char* dblob
   }
 }
 
+// Host restatement of the digit-sliced product for checks: the same slicing
+// of W's columns and x's rows, the diagonal sums formed exactly (as the
+// tensor core forms them: every partial sum is an integer below 2^24), held
+// as f32 and recombined with the device's own routines.
+static void oz_gemm_host(const double* x, uint64_t rows, const double* W, double* y) {
+  constexpr int K = oz::kK;
+  std::vector<double> Wt(size_t(K) * K);
+  for (int k = 0; k < K; ++k)
+    for (int n = 0; n < K; ++n) Wt[size_t(n) * K + k] = W[size_t(k) * K + n];
+  std::vector<unsigned char> img;
+  oz_slice_columns(Wt.data(), &img);
+  const uint16_t* sl = reinterpret_cast<const uint16_t*>(img.data());
+  const int32_t* fe = reinterpret_cast<const int32_t*>(img.data() + oz::kDigits * OzShape::B_SLICE);
+  auto bf16_int = [](uint16_t h) {
+    const uint32_t u = uint32_t(h) << 16;
+    float f;
+    std::memcpy(&f, &u, 4);
+    return int64_t(f);
+  };
+  for (uint64_t r = 0; r < rows; ++r) {
+    const double* xr = x + r * K;
+    int E = 0;
+    for (int k = 0; k < K; ++k) {
+      uint64_t u;
+      std::memcpy(&u, &xr[k], 8);
+      E = std::max(E, oz::exp_of(uint32_t(u >> 32)));
+    }
+    int X[K][oz::kDigits];
+    for (int k = 0; k < K; ++k) {
+      uint64_t u;
+      std::memcpy(&u, &xr[k], 8);
+      const int64_t M = oz::fixed55(uint32_t(u >> 32), uint32_t(u), E);
+      for (int i = 0; i < oz::kDigits; ++i) X[k][i] = oz::digit(M, i);
+    }
+    for (int n = 0; n < K; ++n) {
+      float D[oz::kDigits];
+      for (int dg = 0; dg < oz::kDigits; ++dg) {
+        int64_t sum = 0;
+        for (int i = 0; i <= dg; ++i)
+          for (int k = 0; k < K; ++k)
+            sum += int64_t(X[k][i]) * bf16_int(sl[size_t(dg - i) * K * K + size_t(n) * K + k]);
+        D[dg] = float(sum);  // |sum| < 2^24: exact
+      }
+      int64_t acc = 0;
+      oz::accumulate<0>(acc, D[0]);
+      oz::accumulate<1>(acc, D[1]);
+      oz::accumulate<2>(acc, D[2]);
+      oz::accumulate<3>(acc, D[3]);
+      oz::accumulate<4>(acc, D[4]);
+      oz::accumulate<5>(acc, D[5]);
+      oz::accumulate<6>(acc, D[6]);
+      y[r * K + n] = oz::scaled(acc, E + fe[n] - oz::kPow2Bias);
+    }
+  }
+}
+
 int plan_segment(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int mode,
                  int bits, int variant, PlanBlob* blob, std::vector<SegStep>* out) {
   if (mode == EV_MODE_FUSED) return plan_fused(s, c, first, last, bits, variant, blob, out);
@@ -1073,3 +1436,10 @@ int plan_segment(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last
 }
 
 }  // namespace ev
+
+extern "C" int ev_ozaki_gemm_host(const double* x, uint64_t rows, const double* w, double* y) {
+  ev::clear_error();
+  if (!x || !w || !y) return ev::fail(EV_ERR_INVALID_ARGUMENT, "ev_ozaki_gemm_host: null argument");
+  ev::oz_gemm_host(x, rows, w, y);
+  return EV_OK;
+}

@@ -91,14 +91,20 @@ enum {
   EV_MODE_EXACT = 0, /* one kernel per op, the reference's arithmetic order */
   EV_MODE_TILED = 1, /* runs of ops applied to shared-memory tiles, one HBM
                         pass per run; same per-amplitude arithmetic        */
-  EV_MODE_FUSED = 2  /* complex64 only: runs of ops fused on the host (f64)
-                        into dense k-qubit unitaries, one HBM pass each    */
+  EV_MODE_FUSED = 2  /* runs of ops fused on the host (f64) into dense
+                        k-qubit unitaries, one HBM pass each; complex64
+                        with the variants below but EV_FUSED_OZAKI, which
+                        is the complex128 one                             */
 };
 /* Arithmetic of a fused k-qubit unitary (EV_MODE_FUSED). */
 enum {
   EV_FUSED_TF32X3 = 0, /* tensor cores, split TF32 products, f32 accumulate */
   EV_FUSED_BF16X3 = 1, /* tensor cores, split BF16 products, f32 accumulate */
-  EV_FUSED_FP32 = 2    /* CUDA cores, f32 complex multiply-add              */
+  EV_FUSED_FP32 = 2,   /* CUDA cores, f32 complex multiply-add              */
+  EV_FUSED_OZAKI = 3   /* complex128: tensor cores, each f64 as seven 8-bit
+                          digits in BF16 (per-row / per-column scale), digit
+                          products summed exactly in f32, recombined in
+                          int64 (the Ozaki scheme); k = 5                  */
 };
 typedef struct ev_run_options {
   int32_t dtype;     /* EV_C128 or EV_C64                                  */
@@ -209,6 +215,11 @@ int ev_run_seeded(const ev_circuit* c, uint64_t seed, const ev_run_options* opts
  * runs (the serving loop and the benchmark do). */
 int ev_state_run(ev_state* s, const ev_circuit* c, uint64_t seed,
                  const ev_run_options* opts, uint8_t* classical_out);
+/* drive (src/backend/mod.rs:43-72): the same op walk applied to the state as
+ * it stands, without the reset -- what a Backend does with a circuit's ops
+ * on its current state.  The classical register starts at all-zero. */
+int ev_state_drive(ev_state* s, const ev_circuit* c, uint64_t seed,
+                   const ev_run_options* opts, uint8_t* classical_out);
 
 /* <psi|P|psi> for Pauli strings (PauliString::expectation,
  * src/backend/stabilizer.rs:79-125): term t is (-1)^negative[t] times the
@@ -456,6 +467,11 @@ int ev_probe_fp64(double* fma_per_s);
  * (families that reach every rounding case); *mismatches = pairs whose bits
  * differ.  A check of the build, for tests. */
 int ev_softfp_check(uint64_t seed, uint64_t count, uint64_t* mismatches);
+/* y = x W (rows x 64 times 64 x 64, row-major f64) in the digit-sliced
+ * arithmetic of the EV_FUSED_OZAKI pass, restated on the host with the
+ * kernel's own slicing and recombination routines.  A check of the build,
+ * for tests; no reference counterpart. */
+int ev_ozaki_gemm_host(const double* x, uint64_t rows, const double* w, double* y);
 /* max_j |self_j - other_j| over two states of equal size, either amplitude
  * type (the max amplitude error of a complex64 run against complex128). */
 int ev_max_abs_diff(const ev_state* self, const ev_state* other, double* out);

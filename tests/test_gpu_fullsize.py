@@ -78,6 +78,14 @@ def test_random_layers_norm_and_complex64_fidelity_30q(gpu):
     # every size (a factor within one ulp of 1 rounds each amplitude in a
     # direction tied to its mantissa, so the errors do not average out).
     assert abs(st.norm_sqr() - 1.0) < 1e-9
+    del st
+    # complex128 fused on the tensor cores (digit slicing) against the
+    # bit-exact tiled complex128 result, to the complex128 bar of 1e-12
+    oz = State.zero(N30, "complex128")
+    CudaStateVectorBackend.run_into(oz, c, 0, mode="fused", variant="ozaki")
+    assert ref.max_abs_diff(oz) <= 1e-12
+    ov = ref.overlap(oz)
+    assert abs(ov) ** 2 >= 1 - 1e-12
 
 
 def test_ghz_shots_and_collapse_30q(gpu):

@@ -1,7 +1,9 @@
-"""GPU parity of the complex64 fused path: dense k-qubit unitaries applied on
-tensor cores (TF32x3, BF16x3) or CUDA cores (FP32), against the complex128
-oracle.  Bar: fidelity >= 1 - 1e-6 and max |amplitude error| <= 1e-5 (the
-complex64 storage alone rounds at ~6e-8 relative per pass)."""
+"""GPU parity of the fused paths: dense k-qubit unitaries applied on tensor
+cores (complex64: TF32x3, BF16x3; complex128: 8-bit digit slices, the Ozaki
+scheme) or CUDA cores (complex64 FP32), against the complex128 oracle.
+Bars: complex64 fidelity >= 1 - 1e-6 and max |amplitude error| <= 1e-5 (the
+complex64 storage alone rounds at ~6e-8 relative per pass); complex128
+max |amplitude error| <= 1e-12 and identical measurement outcomes."""
 import numpy as np
 import pytest
 
@@ -82,3 +84,88 @@ def test_fused_tma_staging(gpu, variant, monkeypatch):
     c.compose(workloads.random_layers(14, 3, seed=2))
     ex, wbits, _, _ = check(c, variant, 5, seed=3)
     assert ex.classical() == wbits
+
+
+def check128(c, seed=0):
+    want, wbits, rc = O.run_seeded(c, seed, parallel=True)
+    assert rc == 0
+    ex = CudaStateVectorBackend.run_seeded(c, seed, dtype="complex128", mode="fused",
+                                           variant="ozaki")
+    got = ex.state().amplitudes()
+    err = float(np.max(np.abs(got - want)))
+    assert err <= 1e-12, err
+    assert ex.classical() == wbits
+    return ex, err
+
+
+def test_ozaki_complex128_circuits(gpu):
+    """Random layers, Haar layers with CZ bricks, QFT (closed form), multi-
+    controlled and dense 2-qubit gates across blocks: max error <= 1e-12."""
+    check128(workloads.random_layers(14, 12, seed=5))
+    check128(workloads.random_layers(18, 20, seed=8))
+    check128(workloads.haar_layers(15, 10, seed=6))
+    n, j = 13, 4321
+    ex, _ = check128(workloads.qft_on_basis(n, j))
+    assert np.max(np.abs(ex.state().amplitudes() - workloads.qft_closed_form(n, j))) < 1e-12
+    rng = np.random.default_rng(3)
+    c = Circuit(14)
+    for _ in range(80):
+        qs = [int(x) for x in rng.choice(14, 4, replace=False)]
+        c.ry(qs[0], float(rng.uniform(0, 6)))
+        c.controlled(qs[1:3], Gate1.rx(float(rng.uniform(0, 6))), qs[0])
+        c.gate2(Gate2.rzz(float(rng.uniform(0, 6))), qs[2], qs[3])
+    check128(c)
+
+
+def test_ozaki_complex128_measurement_and_small_registers(gpu):
+    """Mid-circuit measurement and classical control between fused runs give
+    the oracle's outcomes; registers below 12 qubits take the tile pass."""
+    c = workloads.ghz_midmeasure(16)
+    c.compose(workloads.random_layers(16, 3, seed=2))
+    for seed in range(6):
+        check128(c, seed=seed)
+    for n in (1, 3, 7, 11, 12):
+        check128(workloads.random_layers(n, 6, seed=n))
+
+
+def test_ozaki_complex128_rows_of_mixed_scale(gpu):
+    """Each row of a step is scaled by its own largest exponent: on an
+    uploaded state whose rows differ in scale by up to 1e-30 (and hold exact
+    zeros), one fused block on each qubit window matches the oracle row by
+    row to 1e-14 of the row's largest amplitude, and to 1e-12 absolute."""
+    from everett_gb300 import State
+    rng = np.random.default_rng(4)
+    n = 13
+    for lo in (0, 3, 8):
+        mask = 31 << lo
+        idx = np.arange(1 << n)
+        key = idx & ~mask
+        # one scale per row (the 32 amplitudes that agree outside the window)
+        scale = np.exp(rng.uniform(-69, 0, size=1 << n))[key]
+        amps = O.sample_state(n) * scale
+        amps[rng.integers(0, 1 << n, size=200)] = 0
+        amps /= np.linalg.norm(amps)
+        c = Circuit(n)
+        for q in range(lo, lo + 5):
+            c.rx(q, 0.3 + q).rz(q, 1.1 * q)
+        c.cnot(lo, lo + 4).cz(lo + 1, lo + 3)
+        want = amps.copy()
+        O.apply_ops(c, want, 0, len(c))
+        st = State.from_amplitudes(amps)
+        CudaStateVectorBackend.drive(st, c, 0, mode="fused", variant="ozaki")
+        got = st.amplitudes()
+        assert np.max(np.abs(got - want)) <= 1e-12, lo
+        order = np.argsort(key, kind="stable")
+        g, w = got[order].reshape(-1, 32), want[order].reshape(-1, 32)
+        rowmax = np.abs(w).max(axis=1)
+        rel = np.abs(g - w).max(axis=1) / np.where(rowmax > 0, rowmax, 1)
+        assert rel.max() <= 1e-14, (lo, rel.max())
+
+
+def test_ozaki_rejects_complex64_and_complex64_variants_reject_complex128(gpu):
+    import everett_gb300.error as E
+    c = workloads.random_layers(13, 2, seed=1)
+    with pytest.raises(E.EverettError):
+        CudaStateVectorBackend.run(c, dtype="complex64", mode="fused", variant="ozaki")
+    with pytest.raises(E.EverettError):
+        CudaStateVectorBackend.run(c, dtype="complex128", mode="fused", variant="bf16x3")
