@@ -26,6 +26,7 @@
 // and scatter the rows to HBM.  Every mbarrier wait is bounded: on timeout
 // the kernel records an error, frees its TMEM and returns.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include <cstdio>
 #include <cstdlib>
@@ -855,71 +856,113 @@ __global__ void __launch_bounds__(kTmaThreads)
 
 // ---- tcgen05 kernel, complex128 by digit slicing (ev_ozaki.cuh) ---------------
 //
-// One CTA per SM: seven A digit slices of 16 KiB, seven B digit slices of
-// 8 KiB and 448 TMEM columns (seven diagonal accumulators of 128 x 64 f32).
-// Thread t owns row t mod 128 and the four groups of four amplitudes
-// g = t/128 + 2 gi, as in k_fused_tc; the two threads of a row exchange their
-// largest exponent through shared memory.  A step: digits of the rows into
-// the seven A slices (one 16-byte chunk per group and slice), then the rows
-// of the next step are loaded into the same registers so that their latency
-// hides behind the MMAs; one thread issues the MMAs of the output half
-// n < 32 (28 digit pairs x 4 K-steps, N = 32) and commits them to bar[0],
-// then those of n >= 32 to bar[1].  Warps 0-3 recombine the first half
-// while the tensor core still computes the second; warps 4-7 the second.
-// Every wait is bounded; on timeout the kernel records an error, frees TMEM
-// and returns.
+// One CTA of 512 threads per SM: seven A digit slices of 16 KiB, the B digit
+// slices (56 KiB) and 448 TMEM columns.  Digits travel as FP16 (exact for
+// |digit| <= 2048; A and B of one MMA share the type).
+//
+// Layouts.  B rows are ordered [half h][slice j][32 columns n mod 32] and the
+// TMEM accumulators [half h][diagonal d][32 columns], so that for one output
+// half the products of A slice i with B slices 0..6-i -- diagonals i..6 --
+// are ONE MMA of N = 32 (7 - i) whose B rows and D columns are contiguous:
+// 2 halves x 7 slices x 4 K-steps = 56 MMAs per step.
+//
+// Roles of a thread.  Preparation: warp w, lane l handles row 8w + l/4,
+// quarter l mod 4 of it (groups of four amplitudes g = l mod 4 and g + 4);
+// the four threads of a row are adjacent lanes and take the row's largest
+// exponent with two shuffles.  Recombination: thread t reads TMEM lane
+// t mod 128 (its row), output columns 16 (t / 128) .. + 15.
+//
+// A step s: write the A slices from the prepared digits of s; load the rows
+// of s + 1; one thread issues the MMAs of output half 0 (committed to bar[0])
+// and half 1 (bar[1]); meanwhile the others prepare s + 1 (largest exponent,
+// fixed-point values); then recombine s once its half is done.  Every wait
+// is bounded; on timeout the kernel records an error, frees TMEM and returns.
 
-constexpr int kOzThreads = 256;
+constexpr int kOzThreads = 512;
 
 struct OzShape {
   static constexpr int K = oz::kK;
-  static constexpr int A_SLICE = kRows * K * 2;  // 128 rows x 64 BF16
-  static constexpr int B_SLICE = K * K * 2;      // 64 x 64 BF16
+  static constexpr int A_SLICE = kRows * K * 2;  // 128 rows x 64 FP16
+  static constexpr int B_SLICE = K * K * 2;      // 64 x 64 FP16
   static constexpr int SMEM = oz::kDigits * (A_SLICE + B_SLICE) + 1024;
   static constexpr int TMEM_COLS = 512;
+  static constexpr int HALF_COLS = oz::kDigits * 32;  // TMEM columns (and B rows) per half
   static constexpr int BLOB = oz::kDigits * B_SLICE + K * 4;  // B slices, column exponents
 };
 
-// f32 bits of (byte - 128) for the byte of w that sel (0x7440 | byte) picks.
-__device__ __forceinline__ uint32_t oz_byte_digit(uint32_t w, uint32_t sel) {
-  return __float_as_uint(
-      __fadd_rn(__uint_as_float(__byte_perm(w, 0x4B000000u, sel)), -8388736.0f));
+__device__ __forceinline__ uint32_t hsub2_bits(uint32_t a, uint32_t b) {
+  __half2 x, y;
+  memcpy(&x, &a, 4);
+  memcpy(&y, &b, 4);
+  const __half2 r = __hsub2(x, y);
+  uint32_t u;
+  memcpy(&u, &r, 4);
+  return u;
 }
 
-// The seven BF16 digits of re and im (row exponent E), packed per slice as
-// one 32-bit word [re digit | im digit << 16].
-__device__ __forceinline__ void oz_digits_pair(double re, double im, int E, uint32_t w[7]) {
-  const int64_t m0 = oz::fixed55(uint32_t(__double2hiint(re)), uint32_t(__double2loint(re)), E);
-  const int64_t m1 = oz::fixed55(uint32_t(__double2hiint(im)), uint32_t(__double2loint(im)), E);
-  const uint64_t b0 = uint64_t(m0) + oz::kBias, b1 = uint64_t(m1) + oz::kBias;
+// FP16 digits (u - 128) of byte k of w0 and of w1, packed [w0's | w1's << 16]:
+// f16 bits 0x6400 | u are 1024 + u, and 1024 + u - 1152 is exact.
+template <int k>
+__device__ __forceinline__ uint32_t oz_byte_digits(uint32_t w0, uint32_t w1) {
+  const uint32_t t = __byte_perm(w0, w1, uint32_t(k | ((k + 4) << 8)));
+  return hsub2_bits((t & 0x00FF00FFu) | 0x64006400u, 0x64806480u);
+}
+
+// The seven FP16 digits of two biased fixed-point values (b = M + kBias),
+// packed per slice as one 32-bit word [first | second << 16].
+__device__ __forceinline__ void oz_digits(uint64_t b0, uint64_t b1, uint32_t w[7]) {
   const uint32_t l0 = uint32_t(b0), h0 = uint32_t(b0 >> 32);
   const uint32_t l1 = uint32_t(b1), h1 = uint32_t(b1 >> 32);
-  const float t0 = __fadd_rn(__int_as_float(0x4B400000 + (int32_t(h0) >> 16)), -12582912.0f);
-  const float t1 = __fadd_rn(__int_as_float(0x4B400000 + (int32_t(h1) >> 16)), -12582912.0f);
-  w[0] = __byte_perm(__float_as_uint(t0), __float_as_uint(t1), 0x7632);
-  w[1] = __byte_perm(oz_byte_digit(h0, 0x7441), oz_byte_digit(h1, 0x7441), 0x7632);
-  w[2] = __byte_perm(oz_byte_digit(h0, 0x7440), oz_byte_digit(h1, 0x7440), 0x7632);
-  w[3] = __byte_perm(oz_byte_digit(l0, 0x7443), oz_byte_digit(l1, 0x7443), 0x7632);
-  w[4] = __byte_perm(oz_byte_digit(l0, 0x7442), oz_byte_digit(l1, 0x7442), 0x7632);
-  w[5] = __byte_perm(oz_byte_digit(l0, 0x7441), oz_byte_digit(l1, 0x7441), 0x7632);
-  w[6] = __byte_perm(oz_byte_digit(l0, 0x7440), oz_byte_digit(l1, 0x7440), 0x7632);
+  // top digits X0 in [-128, 128]: f16 bits 0x6600 + X0 are 1536 + X0
+  const uint32_t t0 = uint32_t(0x6600 + (int32_t(h0) >> 16));
+  const uint32_t t1 = uint32_t(0x6600 + (int32_t(h1) >> 16));
+  w[0] = hsub2_bits(__byte_perm(t0, t1, 0x5410), 0x66006600u);
+  w[1] = oz_byte_digits<1>(h0, h1);
+  w[2] = oz_byte_digits<0>(h0, h1);
+  w[3] = oz_byte_digits<3>(l0, l1);
+  w[4] = oz_byte_digits<2>(l0, l1);
+  w[5] = oz_byte_digits<1>(l0, l1);
+  w[6] = oz_byte_digits<0>(l0, l1);
 }
 
-__device__ __forceinline__ void mma_bf16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t acc) {
+__device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t acc) {
   asm volatile(
       "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
       "l"(a), "l"(b), "r"(idesc), "r"(acc));
 }
 
-template <int d>
-__device__ __forceinline__ void oz_add_diag(uint32_t lane_tmem, int c0, int64_t acc[16]) {
-  uint32_t w[16];
-  tmem_ld16(lane_tmem + uint32_t(d * oz::kK + c0), w);
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t v[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+               : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]),
+                 "=r"(v[6]), "=r"(v[7])
+               : "r"(taddr));
+}
+
+// Row preparation: the largest exponent of the row (over its four threads)
+// and the biased fixed-point values of this thread's 16 reals.
+__device__ __forceinline__ int oz_prepare(const double2 (&x)[2][4], uint64_t (&b)[2][4][2]) {
+  int em = 0;
 #pragma unroll
-  for (int c = 0; c < 16; ++c) oz::accumulate<d>(acc[c], __uint_as_float(w[c]));
+  for (int gi = 0; gi < 2; ++gi)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      em = max(em, oz::exp_of(uint32_t(__double2hiint(x[gi][i].x))));
+      em = max(em, oz::exp_of(uint32_t(__double2hiint(x[gi][i].y))));
+    }
+  em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, 1));
+  em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, 2));
+#pragma unroll
+  for (int gi = 0; gi < 2; ++gi)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      b[gi][i][0] = uint64_t(oz::fixed55(uint32_t(__double2hiint(x[gi][i].x)),
+                                         uint32_t(__double2loint(x[gi][i].x)), em)) + oz::kBias;
+      b[gi][i][1] = uint64_t(oz::fixed55(uint32_t(__double2hiint(x[gi][i].y)),
+                                         uint32_t(__double2loint(x[gi][i].y)), em)) + oz::kBias;
+    }
+  return em;
 }
 
 __global__ void __launch_bounds__(kOzThreads, 1)
@@ -932,21 +975,22 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   __shared__ __align__(8) uint64_t bar[2];
   __shared__ uint32_t tmem_slot;
   __shared__ int fexp[K];
-  __shared__ int rexp[2][kRows];
+  __shared__ int rowexp[2][kRows];
   unsigned char* sm = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* a_sl = sm;
   unsigned char* b_sl = sm + oz::kDigits * Sh::A_SLICE;
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   for (int i = tid; i < int(sizeof(FusedDesc) / 8); i += blockDim.x)
     reinterpret_cast<uint64_t*>(&d)[i] = reinterpret_cast<const uint64_t*>(gd)[i];
   {
+    // blob [slice j][column n][k] -> B row (n / 32) * 224 + 32 j + n mod 32
     const uint16_t* src = reinterpret_cast<const uint16_t*>(bmat);
     for (int e = tid; e < oz::kDigits * K * K; e += blockDim.x) {
-      const int j = e / (K * K), rem = e % (K * K);
-      *reinterpret_cast<uint16_t*>(b_sl + j * Sh::B_SLICE + sw128_off(rem / K, rem % K, K, 2)) =
-          src[e];
+      const int j = e / (K * K), n = (e / K) % K, k = e % K;
+      const int brow = (n >> 5) * Sh::HALF_COLS + 32 * j + (n & 31);
+      *reinterpret_cast<uint16_t*>(b_sl + sw128_off(brow, k, oz::kDigits * K, 2)) = src[e];
     }
     const int* fe = reinterpret_cast<const int*>(bmat + oz::kDigits * Sh::B_SLICE);
     for (int n = tid; n < K; n += blockDim.x) fexp[n] = fe[n];
@@ -967,108 +1011,127 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
-  // f32 accumulate, BF16 A and B, K-major, N = 32, M = 128
-  const uint32_t idesc =
-      (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(32 >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
   uint32_t phase = 0;
   bool ok = true;
-  const int quarter = warp & 3, half = warp >> 2;
-  const int row = quarter * 32 + (tid & 31);
-  const uint32_t rsw = uint32_t((row >> 3) * 1024 + (row & 7) * 128);
-  const uint32_t rx = uint32_t(row & 7);
-  const uint64_t roff = d.rtab[row];
+  // preparation role
+  const int prow = 8 * warp + (lane >> 2), pq = lane & 3;
+  const uint32_t prsw = uint32_t((prow >> 3) * 1024 + (prow & 7) * 128);
+  const uint32_t prx = uint32_t(prow & 7);
+  const uint64_t proff = d.rtab[prow];
+  // recombination role
+  const int quarter = warp & 3, part = warp >> 2, half = part >> 1;
+  const int erow = quarter * 32 + lane;
+  const uint64_t eroff = d.rtab[erow];
   const uint32_t lane_tmem = tmem + (uint32_t(quarter * 32) << 16);
-  double2 x[4][4];
+  const uint32_t col0 = uint32_t(half * Sh::HALF_COLS + (part & 1) * 16);
+
+  double2 x[2][4];
+  uint64_t b[2][4][2];
+  int em = 0;
   uint64_t step = blockIdx.x;
   if (step < d.nsteps) {
-    const uint64_t rb = step_base(d, step) | roff;
+    const uint64_t rb = step_base(d, step) | proff;
 #pragma unroll
-    for (int gi = 0; gi < 4; ++gi)
+    for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
-      for (int i = 0; i < 4; ++i) x[gi][i] = __ldcs(s + (rb | d.ftab[4 * (half + 2 * gi) + i]));
+      for (int i = 0; i < 4; ++i) x[gi][i] = __ldcs(s + (rb | d.ftab[4 * (pq + 4 * gi) + i]));
+    em = oz_prepare(x, b);
   }
-  for (; step < d.nsteps && ok; step += gridDim.x) {
-    const uint64_t rbase = step_base(d, step) | roff;
-    int em = 0;
+  for (int par = 0; step < d.nsteps && ok; step += gridDim.x, par ^= 1) {
+    // A slices of this step from the prepared digits
 #pragma unroll
-    for (int gi = 0; gi < 4; ++gi)
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        em = max(em, oz::exp_of(uint32_t(__double2hiint(x[gi][i].x))));
-        em = max(em, oz::exp_of(uint32_t(__double2hiint(x[gi][i].y))));
-      }
-    rexp[half][row] = em;
-    __syncthreads();
-    em = max(rexp[0][row], rexp[1][row]);
-#pragma unroll
-    for (int gi = 0; gi < 4; ++gi) {
-      const int g = half + 2 * gi;  // reals 8g..8g+7: chunk g of the row's 128-byte line
-      const uint32_t o = rsw + ((uint32_t(g) ^ rx) << 4);
+    for (int gi = 0; gi < 2; ++gi) {
+      const int g = pq + 4 * gi;  // reals 8g..8g+7: chunk g of the row's 128-byte line
+      const uint32_t o = prsw + ((uint32_t(g) ^ prx) << 4);
       uint32_t w[4][7];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) oz_digits_pair(x[gi][i].x, x[gi][i].y, em, w[i]);
+      for (int i = 0; i < 4; ++i) oz_digits(b[gi][i][0], b[gi][i][1], w[i]);
 #pragma unroll
       for (int sl = 0; sl < oz::kDigits; ++sl)
         *reinterpret_cast<uint4*>(a_sl + sl * Sh::A_SLICE + o) =
             make_uint4(w[0][sl], w[1][sl], w[2][sl], w[3][sl]);
     }
-    // the next step's rows, in flight during the MMAs and the recombination
+    if (pq == 0) rowexp[par][prow] = em;
+    // the next step's rows, in flight while the MMAs are issued
     const uint64_t nstep = step + gridDim.x;
     if (nstep < d.nsteps) {
-      const uint64_t nb = step_base(d, nstep) | roff;
+      const uint64_t nb = step_base(d, nstep) | proff;
 #pragma unroll
-      for (int gi = 0; gi < 4; ++gi)
+      for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
-        for (int i = 0; i < 4; ++i) x[gi][i] = __ldcs(s + (nb | d.ftab[4 * (half + 2 * gi) + i]));
+        for (int i = 0; i < 4; ++i) x[gi][i] = __ldcs(s + (nb | d.ftab[4 * (pq + 4 * gi) + i]));
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (tid == 0) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t a0 = smem_addr(a_sl), b0 = smem_addr(b_sl);
-#pragma unroll
+      // descriptor start addresses are address >> 4: offsets add directly
+      const uint64_t ad = sw128_desc(smem_addr(a_sl)), bd = sw128_desc(smem_addr(b_sl));
+#pragma unroll 1
       for (int h = 0; h < 2; ++h) {
+#pragma unroll 1
+        for (int i = 0; i < oz::kDigits; ++i) {
+          const uint32_t n = uint32_t(32 * (oz::kDigits - i));
+          // f32 accumulate, FP16 A and B, K-major, N, M = 128
+          const uint32_t idesc = (1u << 4) | ((n >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
+          const uint64_t a = ad + uint64_t(i * (Sh::A_SLICE >> 4));
+          const uint64_t bb = bd + uint64_t(h * (Sh::HALF_COLS * 128 >> 4));
+          const uint32_t dt = tmem + uint32_t(h * Sh::HALF_COLS + 32 * i);
 #pragma unroll
-        for (int dg = 0; dg < oz::kDigits; ++dg)
-#pragma unroll
-          for (int i = 0; i <= dg; ++i) {
-            const int j = dg - i;
-#pragma unroll
-            for (int kk = 0; kk < 4; ++kk)
-              mma_bf16(tmem + uint32_t(dg * K + h * 32),
-                       sw128_desc(a0 + uint32_t(i * Sh::A_SLICE + kk * 32)),
-                       sw128_desc(b0 + uint32_t(j * Sh::B_SLICE + h * 32 * 128 + kk * 32)), idesc,
-                       (i | kk) != 0);
-          }
+          for (int kk = 0; kk < 4; ++kk)
+            mma_f16(dt, a + uint64_t(kk * 2), bb + uint64_t(kk * 2), idesc, (i | kk) != 0);
+        }
         asm volatile(
             "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                 smem_addr(&bar[h]))
             : "memory");
       }
     }
+    // prepare the next step while the tensor core works
+    if (nstep < d.nsteps) em = oz_prepare(x, b);
     if (!mbar_wait(&bar[half], phase, kWaitLimit)) {
       ok = false;
       atomicExch(err, 1);
       break;
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int rem = rowexp[par][erow];
+    const uint64_t rbase = step_base(d, step) | eroff;
 #pragma unroll
-    for (int c0 = half * 32; c0 < half * 32 + 32; c0 += 16) {
-      int64_t acc[16];
+    for (int c0 = 0; c0 < 16; c0 += 8) {
+      const uint32_t ta = lane_tmem + col0 + uint32_t(c0);
+      int64_t acc[8];
+      {
+        uint32_t v[4][8];
 #pragma unroll
-      for (int c = 0; c < 16; ++c) acc[c] = 0;
-      oz_add_diag<0>(lane_tmem, c0, acc);
-      oz_add_diag<1>(lane_tmem, c0, acc);
-      oz_add_diag<2>(lane_tmem, c0, acc);
-      oz_add_diag<3>(lane_tmem, c0, acc);
-      oz_add_diag<4>(lane_tmem, c0, acc);
-      oz_add_diag<5>(lane_tmem, c0, acc);
-      oz_add_diag<6>(lane_tmem, c0, acc);
+        for (int dg = 0; dg < 4; ++dg) tmem_ld8(ta + uint32_t(32 * dg), v[dg]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const int n = c0 + 2 * j;
-        const double re = oz::scaled(acc[2 * j], em + fexp[n] - oz::kPow2Bias);
-        const double im = oz::scaled(acc[2 * j + 1], em + fexp[n + 1] - oz::kPow2Bias);
+        for (int c = 0; c < 8; ++c) {
+          acc[c] = 0;
+          oz::accumulate<0>(acc[c], __uint_as_float(v[0][c]));
+          oz::accumulate<1>(acc[c], __uint_as_float(v[1][c]));
+          oz::accumulate<2>(acc[c], __uint_as_float(v[2][c]));
+          oz::accumulate<3>(acc[c], __uint_as_float(v[3][c]));
+        }
+      }
+      {
+        uint32_t v[3][8];
+#pragma unroll
+        for (int dg = 0; dg < 3; ++dg) tmem_ld8(ta + uint32_t(32 * (dg + 4)), v[dg]);
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int c = 0; c < 8; ++c) {
+          oz::accumulate<4>(acc[c], __uint_as_float(v[0][c]));
+          oz::accumulate<5>(acc[c], __uint_as_float(v[1][c]));
+          oz::accumulate<6>(acc[c], __uint_as_float(v[2][c]));
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int n = half * 32 + (part & 1) * 16 + c0 + 2 * j;
+        const double re = oz::scaled(acc[2 * j], rem + fexp[n] - oz::kPow2Bias);
+        const double im = oz::scaled(acc[2 * j + 1], rem + fexp[n + 1] - oz::kPow2Bias);
         __stcs(s + (rbase | d.ftab[n >> 1]), make_double2(re, im));
       }
     }
@@ -1144,17 +1207,27 @@ static void build_bmat(const Block& b, int variant, std::vector<unsigned char>* 
   }
 }
 
-// BF16 bits of a small integer (|v| <= 256: exact in BF16).
-static uint16_t bf16_of_int(int v) {
-  const float f = float(v);
-  uint32_t u;
-  std::memcpy(&u, &f, 4);
-  return uint16_t(u >> 16);
+// FP16 bits of a small integer (|v| <= 2048: exact in FP16).
+static uint16_t f16_of_int(int v) {
+  if (v == 0) return 0;
+  const uint32_t sign = v < 0 ? 0x8000u : 0u;
+  const uint32_t a = uint32_t(v < 0 ? -v : v);
+  int e = 0;
+  while ((a >> (e + 1)) != 0) ++e;  // a in [2^e, 2^(e+1))
+  return uint16_t(sign | (uint32_t(e + 15) << 10) | ((a << (10 - e)) & 0x3FFu));
+}
+
+// The integer an FP16 digit holds (inverse of f16_of_int).
+static int int_of_f16(uint16_t h) {
+  if ((h & 0x7FFFu) == 0) return 0;
+  const int e = int((h >> 10) & 0x1F) - 15;
+  const int mag = int((0x400u | (h & 0x3FFu)) >> (10 - e));
+  return (h & 0x8000u) ? -mag : mag;
 }
 
 // Digit-sliced operand of W^T for the complex128 pass: row n of W^T (column n
 // of W) is scaled by its own largest biased exponent F_n and written as seven
-// BF16 digit slices [N][K] (slice 0 = most significant), followed by the 64
+// FP16 digit slices [N][K] (slice 0 = most significant), followed by the 64
 // exponents F_n (ev_ozaki.cuh).
 static void oz_slice_columns(const double* Wt, std::vector<unsigned char>* out) {
   constexpr int K = oz::kK;
@@ -1174,7 +1247,7 @@ static void oz_slice_columns(const double* Wt, std::vector<unsigned char>* out) 
       std::memcpy(&u, &Wt[size_t(n) * K + k], 8);
       const int64_t M = oz::fixed55(uint32_t(u >> 32), uint32_t(u), E);
       for (int i = 0; i < oz::kDigits; ++i)
-        sl[size_t(i) * K * K + size_t(n) * K + k] = bf16_of_int(oz::digit(M, i));
+        sl[size_t(i) * K * K + size_t(n) * K + k] = f16_of_int(oz::digit(M, i));
     }
   }
 }
@@ -1386,12 +1459,6 @@ static void oz_gemm_host(const double* x, uint64_t rows, const double* W, double
   oz_slice_columns(Wt.data(), &img);
   const uint16_t* sl = reinterpret_cast<const uint16_t*>(img.data());
   const int32_t* fe = reinterpret_cast<const int32_t*>(img.data() + oz::kDigits * OzShape::B_SLICE);
-  auto bf16_int = [](uint16_t h) {
-    const uint32_t u = uint32_t(h) << 16;
-    float f;
-    std::memcpy(&f, &u, 4);
-    return int64_t(f);
-  };
   for (uint64_t r = 0; r < rows; ++r) {
     const double* xr = x + r * K;
     int E = 0;
@@ -1413,7 +1480,7 @@ static void oz_gemm_host(const double* x, uint64_t rows, const double* W, double
         int64_t sum = 0;
         for (int i = 0; i <= dg; ++i)
           for (int k = 0; k < K; ++k)
-            sum += int64_t(X[k][i]) * bf16_int(sl[size_t(dg - i) * K * K + size_t(n) * K + k]);
+            sum += int64_t(X[k][i]) * int_of_f16(sl[size_t(dg - i) * K * K + size_t(n) * K + k]);
         D[dg] = float(sum);  // |sum| < 2^24: exact
       }
       int64_t acc = 0;

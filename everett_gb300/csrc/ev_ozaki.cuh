@@ -1,4 +1,4 @@
-// ev_ozaki.cuh -- complex128 fused unitaries on the BF16 tensor cores by
+// ev_ozaki.cuh -- complex128 fused unitaries on the FP16 tensor cores by
 // digit slicing: the Ozaki scheme (K. Ozaki, T. Ogita, S. Oishi, S. M. Rump,
 // "Error-free transformations of matrix multiplication by using fast routines
 // of matrix multiplication and its applications", Numerical Algorithms 59
@@ -11,7 +11,7 @@
 // written in balanced base 256 as seven digits
 //     M = sum_{i=0..6} X_i 256^(6-i),   X_i in [-128, 127], X_0 in [-128, 128].
 // Column n of W gets the same treatment on the host with its own exponent
-// F_n.  A digit is exact in BF16, the product of two digits (|.| <= 2^14) is
+// F_n.  A digit is exact in FP16, the product of two digits (|.| <= 2^14) is
 // exact, and the sum over K of the products of one diagonal d = i + j
 // (d + 1 digit pairs, 64 (d + 1) products) stays within 7 * 2^20 < 2^24, so
 // the f32 accumulator of the tensor core holds every partial sum exactly.

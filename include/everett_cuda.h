@@ -102,7 +102,7 @@ enum {
   EV_FUSED_BF16X3 = 1, /* tensor cores, split BF16 products, f32 accumulate */
   EV_FUSED_FP32 = 2,   /* CUDA cores, f32 complex multiply-add              */
   EV_FUSED_OZAKI = 3   /* complex128: tensor cores, each f64 as seven 8-bit
-                          digits in BF16 (per-row / per-column scale), digit
+                          digits in FP16 (per-row / per-column scale), digit
                           products summed exactly in f32, recombined in
                           int64 (the Ozaki scheme); k = 5                  */
 };
