@@ -866,9 +866,9 @@ __global__ void __launch_bounds__(kTmaThreads)
 // are ONE MMA of N = 32 (7 - i) whose B rows and D columns are contiguous:
 // 2 halves x 7 slices x 4 K-steps = 56 MMAs per step.
 //
-// Roles of a thread.  Preparation: warp w, lane l handles row 8w + l/4,
-// quarter l mod 4 of it (groups of four amplitudes g = l mod 4 and g + 4);
-// the four threads of a row are adjacent lanes and take the row's largest
+// Roles of a thread.  Preparation: warp w, lane l handles row 8w + l mod 8,
+// quarter l/8 of it (groups of four amplitudes g = l/8 and g + 4); the four
+// threads of a row (lanes l, l + 8, l + 16, l + 24) take the row's largest
 // exponent with two shuffles.  Recombination: thread t reads TMEM lane
 // t mod 128 (its row), output columns 16 (t / 128) .. + 15.
 //
@@ -879,6 +879,10 @@ __global__ void __launch_bounds__(kTmaThreads)
 // is bounded; on timeout the kernel records an error, frees TMEM and returns.
 
 constexpr int kOzThreads = 512;
+// The thread that issues the MMAs: issue blocks at about the tensor core's
+// pace, so it belongs to a warp that recombines the second output half,
+// which waits for all the MMAs anyway.
+constexpr int kOzIssuer = 256;
 
 struct OzShape {
   static constexpr int K = oz::kK;
@@ -940,29 +944,36 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t v[8]) {
                : "r"(taddr));
 }
 
-// Row preparation: the largest exponent of the row (over its four threads)
-// and the biased fixed-point values of this thread's 16 reals.
-__device__ __forceinline__ int oz_prepare(const double2 (&x)[2][4], uint64_t (&b)[2][4][2]) {
+// Row preparation, in place: v holds the bits of this thread's 16 reals of
+// the row (two groups of four amplitudes, [re, im]) and becomes their biased
+// fixed-point values; returns the row's largest exponent (over its four
+// threads: lanes l, l + 8, l + 16, l + 24).
+__device__ __forceinline__ int oz_prepare(uint64_t (&v)[2][4][2]) {
   int em = 0;
 #pragma unroll
   for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      em = max(em, oz::exp_of(uint32_t(__double2hiint(x[gi][i].x))));
-      em = max(em, oz::exp_of(uint32_t(__double2hiint(x[gi][i].y))));
-    }
-  em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, 1));
-  em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, 2));
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) em = max(em, oz::exp_of(uint32_t(v[gi][i][c] >> 32)));
+  em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, 8));
+  em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, 16));
 #pragma unroll
   for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      b[gi][i][0] = uint64_t(oz::fixed55(uint32_t(__double2hiint(x[gi][i].x)),
-                                         uint32_t(__double2loint(x[gi][i].x)), em)) + oz::kBias;
-      b[gi][i][1] = uint64_t(oz::fixed55(uint32_t(__double2hiint(x[gi][i].y)),
-                                         uint32_t(__double2loint(x[gi][i].y)), em)) + oz::kBias;
-    }
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int c = 0; c < 2; ++c)
+        v[gi][i][c] =
+            uint64_t(oz::fixed55(uint32_t(v[gi][i][c] >> 32), uint32_t(v[gi][i][c]), em)) + oz::kBias;
   return em;
+}
+
+// One amplitude's bits.
+__device__ __forceinline__ void oz_load(const double2* p, uint64_t (&v)[2]) {
+  const double2 a = __ldcs(p);
+  v[0] = uint64_t(__double_as_longlong(a.x));
+  v[1] = uint64_t(__double_as_longlong(a.y));
 }
 
 __global__ void __launch_bounds__(kOzThreads, 1)
@@ -1013,8 +1024,9 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   const uint32_t tmem = tmem_slot;
   uint32_t phase = 0;
   bool ok = true;
-  // preparation role
-  const int prow = 8 * warp + (lane >> 2), pq = lane & 3;
+  // preparation role: the eight lanes of a store phase hold eight different
+  // rows, so their 16-byte chunks land in eight different bank groups
+  const int prow = 8 * warp + (lane & 7), pq = lane >> 3;
   const uint32_t prsw = uint32_t((prow >> 3) * 1024 + (prow & 7) * 128);
   const uint32_t prx = uint32_t(prow & 7);
   const uint64_t proff = d.rtab[prow];
@@ -1025,8 +1037,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   const uint32_t lane_tmem = tmem + (uint32_t(quarter * 32) << 16);
   const uint32_t col0 = uint32_t(half * Sh::HALF_COLS + (part & 1) * 16);
 
-  double2 x[2][4];
-  uint64_t b[2][4][2];
+  uint64_t b[2][4][2];  // the rows' bits, then their biased fixed-point values
   int em = 0;
   uint64_t step = blockIdx.x;
   if (step < d.nsteps) {
@@ -1034,8 +1045,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 #pragma unroll
     for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
-      for (int i = 0; i < 4; ++i) x[gi][i] = __ldcs(s + (rb | d.ftab[4 * (pq + 4 * gi) + i]));
-    em = oz_prepare(x, b);
+      for (int i = 0; i < 4; ++i) oz_load(s + (rb | d.ftab[4 * (pq + 4 * gi) + i]), b[gi][i]);
+    em = oz_prepare(b);
   }
   for (int par = 0; step < d.nsteps && ok; step += gridDim.x, par ^= 1) {
     // A slices of this step from the prepared digits
@@ -1059,11 +1070,11 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 #pragma unroll
       for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
-        for (int i = 0; i < 4; ++i) x[gi][i] = __ldcs(s + (nb | d.ftab[4 * (pq + 4 * gi) + i]));
+        for (int i = 0; i < 4; ++i) oz_load(s + (nb | d.ftab[4 * (pq + 4 * gi) + i]), b[gi][i]);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (tid == 0) {
+    if (tid == kOzIssuer) {
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       // descriptor start addresses are address >> 4: offsets add directly
       const uint64_t ad = sw128_desc(smem_addr(a_sl)), bd = sw128_desc(smem_addr(b_sl));
@@ -1088,7 +1099,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       }
     }
     // prepare the next step while the tensor core works
-    if (nstep < d.nsteps) em = oz_prepare(x, b);
+    if (nstep < d.nsteps) em = oz_prepare(b);
     if (!mbar_wait(&bar[half], phase, kWaitLimit)) {
       ok = false;
       atomicExch(err, 1);
@@ -1100,6 +1111,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 #pragma unroll
     for (int c0 = 0; c0 < 16; c0 += 8) {
       const uint32_t ta = lane_tmem + col0 + uint32_t(c0);
+      int32_t g3[8], g2[8];
       int64_t acc[8];
       {
         uint32_t v[4][8];
@@ -1107,13 +1119,9 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         for (int dg = 0; dg < 4; ++dg) tmem_ld8(ta + uint32_t(32 * dg), v[dg]);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          acc[c] = 0;
-          oz::accumulate<0>(acc[c], __uint_as_float(v[0][c]));
-          oz::accumulate<1>(acc[c], __uint_as_float(v[1][c]));
-          oz::accumulate<2>(acc[c], __uint_as_float(v[2][c]));
-          oz::accumulate<3>(acc[c], __uint_as_float(v[3][c]));
-        }
+        for (int c = 0; c < 8; ++c)
+          oz::combine_hi(__uint_as_float(v[0][c]), __uint_as_float(v[1][c]),
+                         __uint_as_float(v[2][c]), __uint_as_float(v[3][c]), g3[c], g2[c]);
       }
       {
         uint32_t v[3][8];
@@ -1121,11 +1129,10 @@ __global__ void __launch_bounds__(kOzThreads, 1)
         for (int dg = 0; dg < 3; ++dg) tmem_ld8(ta + uint32_t(32 * (dg + 4)), v[dg]);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          oz::accumulate<4>(acc[c], __uint_as_float(v[0][c]));
-          oz::accumulate<5>(acc[c], __uint_as_float(v[1][c]));
-          oz::accumulate<6>(acc[c], __uint_as_float(v[2][c]));
-        }
+        for (int c = 0; c < 8; ++c)
+          acc[c] = oz::combine_g(g3[c], g2[c],
+                                 oz::combine_lo(__uint_as_float(v[0][c]), __uint_as_float(v[1][c]),
+                                                __uint_as_float(v[2][c])));
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
@@ -1449,8 +1456,10 @@ int launch_fused_step(ev_state* s, const SegStep& st, const unsigned char* dblob
 // Host restatement of the digit-sliced product for checks: the same slicing
 // of W's columns and x's rows, the diagonal sums formed exactly (as the
 // tensor core forms them: every partial sum is an integer below 2^24), held
-// as f32 and recombined with the device's own routines.
-static void oz_gemm_host(const double* x, uint64_t rows, const double* W, double* y) {
+// as f32 and recombined with the device's own routines -- diagonal by
+// diagonal, and checked against the kernel's grouped form (false if the two
+// differ for any output).
+static bool oz_gemm_host(const double* x, uint64_t rows, const double* W, double* y) {
   constexpr int K = oz::kK;
   std::vector<double> Wt(size_t(K) * K);
   for (int k = 0; k < K; ++k)
@@ -1491,9 +1500,11 @@ static void oz_gemm_host(const double* x, uint64_t rows, const double* W, double
       oz::accumulate<4>(acc, D[4]);
       oz::accumulate<5>(acc, D[5]);
       oz::accumulate<6>(acc, D[6]);
+      if (oz::combine7(D) != acc) return false;  // the kernel's grouped form
       y[r * K + n] = oz::scaled(acc, E + fe[n] - oz::kPow2Bias);
     }
   }
+  return true;
 }
 
 int plan_segment(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int mode,
@@ -1507,6 +1518,7 @@ int plan_segment(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last
 extern "C" int ev_ozaki_gemm_host(const double* x, uint64_t rows, const double* w, double* y) {
   ev::clear_error();
   if (!x || !w || !y) return ev::fail(EV_ERR_INVALID_ARGUMENT, "ev_ozaki_gemm_host: null argument");
-  ev::oz_gemm_host(x, rows, w, y);
+  if (!ev::oz_gemm_host(x, rows, w, y))
+    return ev::fail(EV_ERR_INVALID_ARGUMENT, "ev_ozaki_gemm_host: grouped recombination differs");
   return EV_OK;
 }

@@ -110,6 +110,39 @@ __host__ __device__ __forceinline__ void accumulate(int64_t& acc, float D) {
   }
 }
 
+// The seven diagonals of one output combined at once, with the same result
+// as accumulate<0..6>: the digit bounds keep three partial sums inside int32,
+//   G3 = 2^8 I0 + I1 (< 2^29),  G2 = 2^8 I2 + I3 (< 2^30),
+//   G1 = 2^8 I4 + I5 + round(D6 / 2^8) (< 2^31),
+// and acc = 2^32 G3 + 2^16 G2 + G1.  The magic constants of the f32-to-int
+// conversions cancel in the wrapping 32-bit sums.
+// (G3, G2) from D0..D3, G1 from D4..D6 (callers can release D0..D3 first).
+__host__ __device__ __forceinline__ void combine_hi(float D0, float D1, float D2, float D3,
+                                                    int32_t& g3, int32_t& g2) {
+  constexpr uint32_t kM = 0x4B400000u;
+  const uint32_t b0 = f32_bits(add_rn(D0, f32_of(kM))), b1 = f32_bits(add_rn(D1, f32_of(kM)));
+  const uint32_t b2 = f32_bits(add_rn(D2, f32_of(kM))), b3 = f32_bits(add_rn(D3, f32_of(kM)));
+  g3 = int32_t((b0 << 8) + b1 - ((kM << 8) + kM));
+  g2 = int32_t((b2 << 8) + b3 - ((kM << 8) + kM));
+}
+__host__ __device__ __forceinline__ int32_t combine_lo(float D4, float D5, float D6) {
+  const uint32_t b6 = f32_bits(add_rn(D6, f32_of(0x4F400000u)));
+#ifdef __CUDA_ARCH__
+  const uint32_t i4 = uint32_t(__float2int_rn(D4)), i5 = uint32_t(__float2int_rn(D5));
+#else
+  const uint32_t i4 = uint32_t(int32_t(D4)), i5 = uint32_t(int32_t(D5));
+#endif
+  return int32_t((i4 << 8) + i5 + b6 - 0x4F400000u);
+}
+__host__ __device__ __forceinline__ int64_t combine_g(int32_t g3, int32_t g2, int32_t g1) {
+  return (int64_t(g3) << 32) + (int64_t(g2) << 16) + int64_t(g1);
+}
+__host__ __device__ __forceinline__ int64_t combine7(const float D[7]) {
+  int32_t g3, g2;
+  combine_hi(D[0], D[1], D[2], D[3], g3, g2);
+  return combine_g(g3, g2, combine_lo(D[4], D[5], D[6]));
+}
+
 // acc * 2^pow2 as an f64 (|acc| < 2^62), rounded to nearest even once,
 // assembled from acc's bits.
 __host__ __device__ __forceinline__ double scaled(int64_t acc, int pow2) {
