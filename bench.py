@@ -114,6 +114,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def bf16_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["bf16_tflops"]), "measured bf16_tflops (burst)"
+    return 1900.0, "fallback"
+
+
 def ncu_figure(name: str, key: str):
     """A number from a committed ncu summary (profiles/<name>.txt)."""
     p = ROOT / "profiles" / f"{name}.txt"
@@ -300,6 +307,43 @@ def extras_c64(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, peak_kin
                                     f"k_fused_tc<5,{variant}> (fused 5-qubit unitary, tcgen05)",
                                     ncu_figure("k_fused_tc_bf16x3", "traffic_bytes_per_launch_full_size")
                                     if variant == "bf16x3" else None)}
+    del st
+    return out
+
+
+def extras_c128_fused(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, peak_kind):
+    """The same circuit through the complex128 fused path: 5-qubit unitaries
+    on the FP16 tensor cores with 8-bit digit slicing, against the bit-exact
+    tiled complex128 result."""
+    from everett_gb300 import State
+    n = circuit.num_qubits()
+    st = State.zero(n, "complex128")
+    kw = dict(mode="fused", variant="ozaki")
+    timed_runs(L, N, st, circuit, 1, **kw)
+    ms, prof = timed_runs(L, N, st, circuit, 2, **kw)
+    ov = ref_state.overlap(st)
+    roof = roofline_of(prof, "fused_unitary", 2.0 * (1 << n) * 16, peak, peak_kind,
+                       "k_fused_oz (fused 5-qubit unitary, complex128 by digit slicing, tcgen05)",
+                       ncu_figure("k_fused_oz", "traffic_bytes_per_launch_full_size"))
+    if roof:
+        # digit-pair MMAs per launch: 2^n / 4096 steps x 2 halves x 28 pairs x
+        # 4 K-steps of 128 x 32 x 16 -- 7168 flops per amplitude
+        flops = 7168.0 * (1 << n)
+        tf = flops / (roof["avg_launch_ms"] / 1e3) / 1e12
+        bf = bf16_peak()
+        roof["tensor"] = {"achieved_tflops": round(tf, 1), "peak_tflops": bf[0],
+                          "frac": round(tf / bf[0], 4), "peak_source": bf[1],
+                          "flops_per_launch": flops}
+    out = {"workload": f"random-layer circuit, {n} qubits, depth 20, complex128 fused "
+                       f"(ozaki: seven 8-bit FP16 digits per f64, exact f32 digit-pair sums, "
+                       f"int64 recombination)",
+           "ms_per_run": round(ms, 2), "speedup_vs_complex128_tiled": round(c128_ms / ms, 2),
+           "gate_GBps": round(bytes_per_step / (ms / 1e3) / 1e9, 1),
+           "max_abs_err_vs_complex128_bit_exact": ref_state.max_abs_diff(st),
+           "fidelity_vs_complex128_bit_exact": abs(ov) ** 2,
+           "amplitude_updates_per_s": float(f"{len(circuit) * (1 << n) / (ms / 1e3):.4g}"),
+           "passes": prof.get("fused_unitary", {}).get("launches", 0) // 2,
+           "roofline": roof}
     del st
     return out
 
@@ -779,7 +823,10 @@ def run_ours(args, dist: Dist):
                          f"qubits, {dt:.1f} s, scalar oracle (the reference's loops)"}
         if not args.no_extras:
             c128_ms = worst_ms / args.steps
-            for key, fn in (("complex64_fused_same_circuit",
+            for key, fn in (("complex128_fused_same_circuit",
+                             lambda: extras_c128_fused(L, N, state, circuit, c128_ms,
+                                                       bytes_per_step, peak, peak_kind)),
+                            ("complex64_fused_same_circuit",
                              lambda: extras_c64(L, N, state, circuit, c128_ms, bytes_per_step,
                                                 peak, peak_kind)),
                             ("qft", lambda: extras_qft(L, N, n, peak)),

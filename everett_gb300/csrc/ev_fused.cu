@@ -856,9 +856,9 @@ __global__ void __launch_bounds__(kTmaThreads)
 
 // ---- tcgen05 kernel, complex128 by digit slicing (ev_ozaki.cuh) ---------------
 //
-// One CTA of 512 threads per SM: seven A digit slices of 16 KiB, the B digit
-// slices (56 KiB) and 448 TMEM columns.  Digits travel as FP16 (exact for
-// |digit| <= 2048; A and B of one MMA share the type).
+// One CTA per SM: 16 worker warps and one MMA warp; seven A digit slices of
+// 16 KiB, the B digit slices (56 KiB) and 448 TMEM columns.  Digits travel
+// as FP16 (exact for |digit| <= 2048; A and B of one MMA share the type).
 //
 // Layouts.  B rows are ordered [half h][slice j][32 columns n mod 32] and the
 // TMEM accumulators [half h][diagonal d][32 columns], so that for one output
@@ -866,23 +866,26 @@ __global__ void __launch_bounds__(kTmaThreads)
 // are ONE MMA of N = 32 (7 - i) whose B rows and D columns are contiguous:
 // 2 halves x 7 slices x 4 K-steps = 56 MMAs per step.
 //
-// Roles of a thread.  Preparation: warp w, lane l handles row 8w + l mod 8,
+// Roles of a worker.  Preparation: warp w, lane l handles row 8w + l mod 8,
 // quarter l/8 of it (groups of four amplitudes g = l/8 and g + 4); the four
 // threads of a row (lanes l, l + 8, l + 16, l + 24) take the row's largest
-// exponent with two shuffles.  Recombination: thread t reads TMEM lane
-// t mod 128 (its row), output columns 16 (t / 128) .. + 15.
+// exponent with two shuffles, and the eight lanes of a store phase hold
+// eight different rows (their 16-byte chunks land in eight bank groups).
+// Recombination: thread t reads TMEM lane t mod 128 (its row), output
+// columns 16 (t / 128) .. + 15.
 //
-// A step s: write the A slices from the prepared digits of s; load the rows
-// of s + 1; one thread issues the MMAs of output half 0 (committed to bar[0])
-// and half 1 (bar[1]); meanwhile the others prepare s + 1 (largest exponent,
-// fixed-point values); then recombine s once its half is done.  Every wait
-// is bounded; on timeout the kernel records an error, frees TMEM and returns.
+// A step s: the workers write the A slices from the prepared digits of s,
+// start loading the rows of s + 1, meet at a named barrier and signal the MMA
+// warp (abar); its lane 0 issues the MMAs of output half 0 (committed to
+// bar[0]) and half 1 (bar[1]) -- issue blocks at about the tensor core's
+// pace, hence a warp of its own; meanwhile the workers prepare s + 1
+// (largest exponent, fixed-point values), then recombine s once its half is
+// done.  A worker's arrival at the barrier of s + 1 also means its TMEM reads
+// of s are complete.  Every wait is bounded; on timeout the kernel records an
+// error, frees TMEM and returns.
 
-constexpr int kOzThreads = 512;
-// The thread that issues the MMAs: issue blocks at about the tensor core's
-// pace, so it belongs to a warp that recombines the second output half,
-// which waits for all the MMAs anyway.
-constexpr int kOzIssuer = 256;
+constexpr int kOzWorkers = 512;                // 16 worker warps
+constexpr int kOzThreads = kOzWorkers + 32;    // and the MMA warp
 
 struct OzShape {
   static constexpr int K = oz::kK;
@@ -984,6 +987,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   extern __shared__ unsigned char smem_raw[];
   __shared__ FusedDesc d;
   __shared__ __align__(8) uint64_t bar[2];
+  __shared__ __align__(8) uint64_t abar;
   __shared__ uint32_t tmem_slot;
   __shared__ int fexp[K];
   __shared__ int rowexp[2][kRows];
@@ -1009,6 +1013,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[0])));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[1])));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&abar)));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -1022,6 +1027,45 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
+  if (warp == kOzWorkers / 32) {
+    if (lane == 0) {
+      uint32_t aphase = 0;
+      for (uint64_t st = blockIdx.x; st < d.nsteps; st += gridDim.x) {
+        if (!mbar_wait(&abar, aphase, kWaitLimit)) {
+          atomicExch(err, 1);
+          break;
+        }
+        aphase ^= 1;
+        {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // descriptor start addresses are address >> 4: offsets add directly
+      const uint64_t ad = sw128_desc(smem_addr(a_sl)), bd = sw128_desc(smem_addr(b_sl));
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+#pragma unroll 1
+        for (int i = 0; i < oz::kDigits; ++i) {
+          const uint32_t n = uint32_t(32 * (oz::kDigits - i));
+          // f32 accumulate, FP16 A and B, K-major, N, M = 128
+          const uint32_t idesc = (1u << 4) | ((n >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
+          const uint64_t a = ad + uint64_t(i * (Sh::A_SLICE >> 4));
+          const uint64_t bb = bd + uint64_t(h * (Sh::HALF_COLS * 128 >> 4));
+          const uint32_t dt = tmem + uint32_t(h * Sh::HALF_COLS + 32 * i);
+#pragma unroll
+          for (int kk = 0; kk < 4; ++kk)
+            mma_f16(dt, a + uint64_t(kk * 2), bb + uint64_t(kk * 2), idesc, (i | kk) != 0);
+        }
+        asm volatile(
+            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                smem_addr(&bar[h]))
+            : "memory");
+      }
+    }
+      }
+    }
+    __syncwarp();
+    __syncthreads();
+    return;
+  }
   uint32_t phase = 0;
   bool ok = true;
   // preparation role: the eight lanes of a store phase hold eight different
@@ -1040,8 +1084,14 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   uint64_t b[2][4][2];  // the rows' bits, then their biased fixed-point values
   int em = 0;
   uint64_t step = blockIdx.x;
+  // Step bases advance by a masked add: with M the mask of the step-index
+  // qubits, base(s + grid) = ((base(s) | ~M) + base(grid)) & M.
+  uint64_t cmask = 0;
+  for (int q = 0; q < d.ncomp_hi; ++q) cmask |= uint64_t(1) << d.comp_hi[q];
+  const uint64_t gbase = step_base(d, gridDim.x);
+  uint64_t sb = step_base(d, step);
   if (step < d.nsteps) {
-    const uint64_t rb = step_base(d, step) | proff;
+    const uint64_t rb = sb | proff;
 #pragma unroll
     for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
@@ -1066,38 +1116,16 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     // the next step's rows, in flight while the MMAs are issued
     const uint64_t nstep = step + gridDim.x;
     if (nstep < d.nsteps) {
-      const uint64_t nb = step_base(d, nstep) | proff;
+      const uint64_t nb = (((sb | ~cmask) + gbase) & cmask) | proff;
 #pragma unroll
       for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
         for (int i = 0; i < 4; ++i) oz_load(s + (nb | d.ftab[4 * (pq + 4 * gi) + i]), b[gi][i]);
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    __syncthreads();
-    if (tid == kOzIssuer) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // descriptor start addresses are address >> 4: offsets add directly
-      const uint64_t ad = sw128_desc(smem_addr(a_sl)), bd = sw128_desc(smem_addr(b_sl));
-#pragma unroll 1
-      for (int h = 0; h < 2; ++h) {
-#pragma unroll 1
-        for (int i = 0; i < oz::kDigits; ++i) {
-          const uint32_t n = uint32_t(32 * (oz::kDigits - i));
-          // f32 accumulate, FP16 A and B, K-major, N, M = 128
-          const uint32_t idesc = (1u << 4) | ((n >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
-          const uint64_t a = ad + uint64_t(i * (Sh::A_SLICE >> 4));
-          const uint64_t bb = bd + uint64_t(h * (Sh::HALF_COLS * 128 >> 4));
-          const uint32_t dt = tmem + uint32_t(h * Sh::HALF_COLS + 32 * i);
-#pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_f16(dt, a + uint64_t(kk * 2), bb + uint64_t(kk * 2), idesc, (i | kk) != 0);
-        }
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_addr(&bar[h]))
-            : "memory");
-      }
-    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    asm volatile("bar.sync 1, %0;" ::"n"(kOzWorkers) : "memory");
+    if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&abar)) : "memory");
     // prepare the next step while the tensor core works
     if (nstep < d.nsteps) em = oz_prepare(b);
     if (!mbar_wait(&bar[half], phase, kWaitLimit)) {
@@ -1107,7 +1135,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     }
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int rem = rowexp[par][erow];
-    const uint64_t rbase = step_base(d, step) | eroff;
+    const uint64_t rbase = sb | eroff;
 #pragma unroll
     for (int c0 = 0; c0 < 16; c0 += 8) {
       const uint32_t ta = lane_tmem + col0 + uint32_t(c0);
@@ -1150,6 +1178,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       break;
     }
     phase ^= 1;
+    sb = ((sb | ~cmask) + gbase) & cmask;
   }
   __syncthreads();
   if (warp == 0) {
