@@ -324,7 +324,7 @@ def extras_c128_fused(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, p
     ov = ref_state.overlap(st)
     roof = roofline_of(prof, "fused_unitary", 2.0 * (1 << n) * 16, peak, peak_kind,
                        "k_fused_oz (fused 5-qubit unitary, complex128 by digit slicing, tcgen05)",
-                       ncu_figure("k_fused_oz", "traffic_bytes_per_launch_full_size"))
+                       ncu_figure("k_fused_oz_c128", "traffic_bytes_per_launch_full_size"))
     if roof:
         # digit-pair MMAs per launch: 2^n / 4096 steps x 2 halves x 28 pairs x
         # 4 K-steps of 128 x 32 x 16 -- 7168 flops per amplitude

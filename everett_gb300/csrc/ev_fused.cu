@@ -1089,6 +1089,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   uint64_t cmask = 0;
   for (int q = 0; q < d.ncomp_hi; ++q) cmask |= uint64_t(1) << d.comp_hi[q];
   const uint64_t gbase = step_base(d, gridDim.x);
+  const int nruns = 1 << (d.k + 7 - d.lowbits);  // the 2^(k+7) amplitudes of a step
+  const uint32_t run_bytes = 16u << d.lowbits;
   uint64_t sb = step_base(d, step);
   if (step < d.nsteps) {
     const uint64_t rb = sb | proff;
@@ -1126,6 +1128,14 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     asm volatile("bar.sync 1, %0;" ::"n"(kOzWorkers) : "memory");
     if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&abar)) : "memory");
+    // the rows of the step after next into L2 (contiguous runs of 2^lowbits
+    // amplitudes, at most 32 of them), so that next step's loads hit L2
+    if (warp == 1 && lane < nruns && nstep + gridDim.x < d.nsteps) {
+      const uint64_t b2 = (((((sb | ~cmask) + gbase) & cmask) | ~cmask) + gbase) & cmask;
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(s + (b2 | d.hitab[lane])),
+                   "r"(run_bytes)
+                   : "memory");
+    }
     // prepare the next step while the tensor core works
     if (nstep < d.nsteps) em = oz_prepare(b);
     if (!mbar_wait(&bar[half], phase, kWaitLimit)) {
