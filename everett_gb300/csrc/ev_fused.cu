@@ -470,7 +470,17 @@ __global__ void __launch_bounds__(kTcThreads)
   const uint32_t rsw = uint32_t((row >> 3) * 1024 + (row & 7) * 128);
   const uint32_t rx = uint32_t(row & 7);
   const uint64_t roff = d.rtab[row];
+  // L2 prefetch of the rows two steps ahead: contiguous runs of 2^lowbits
+  // amplitudes, one bulk prefetch per run from warp 1
+  const int nruns = 1 << (d.k + 7 - d.lowbits);
+  const uint32_t run_bytes = 8u << d.lowbits;
   for (uint64_t step = blockIdx.x; step < d.nsteps && ok; step += gridDim.x) {
+    if (warp == 1 && (tid & 31) < nruns && step + 2 * uint64_t(gridDim.x) < d.nsteps) {
+      const uint64_t b2 = step_base(d, step + 2 * uint64_t(gridDim.x));
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(s + (b2 | d.hitab[tid & 31])),
+                   "r"(run_bytes)
+                   : "memory");
+    }
     const uint64_t rbase = step_base(d, step) | roff;
     float2 x[GPT][4];
 #pragma unroll

@@ -50,6 +50,7 @@ def plain(state, c, seed, **kw):
     ("complex64", "fused", {"variant": "bf16x3"}),
     ("complex64", "fused", {"variant": "tf32x3"}),
     ("complex64", "fused", {"variant": "fp32", "tile_bits": 4}),
+    ("complex128", "fused", {"variant": "ozaki"}),
 ])
 def test_prepared_equals_run(gpu, dtype, mode, kw):
     n = 14
@@ -128,5 +129,5 @@ def test_prepare_rejects_mismatches(gpu):
     st = State.zero(6)
     with pytest.raises(DimensionMismatch):
         PreparedRun(st, algorithms.ghz(7))
-    with pytest.raises(EverettError):
-        PreparedRun(st, algorithms.ghz(6), mode="fused")  # complex128 state
+    with pytest.raises(EverettError):  # a complex64 arithmetic on a complex128 state
+        PreparedRun(st, algorithms.ghz(6), mode="fused", variant="bf16x3")
