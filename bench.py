@@ -444,6 +444,19 @@ def extras_serve():
         srv.close()
         key = "saturated_all_at_once" if rate > 1e5 else f"poisson_{int(rate)}_per_s"
         out[key] = serve.latency_summary(res, wall)
+    # the same mix in complex128: fused digit-sliced passes for 12+ qubits
+    c128 = {"workload": "the same requests in complex128, fused (ozaki) for 12 qubits and up"}
+    srv = serve.Server(dtype="complex128", workers=1, mode="fused", batch_small=False)
+    res, wall = serve.poisson_run(srv, requests, rate=1e6)
+    srv.close()
+    c128["serial_one_request_at_a_time"] = serve.latency_summary(res, wall)
+    for rate in (50.0, 1e6):
+        srv = serve.Server(dtype="complex128", workers=8, mode="fused")
+        res, wall = serve.poisson_run(srv, requests, rate=rate, seed=int(rate) % 1000)
+        srv.close()
+        key = "saturated_all_at_once" if rate > 1e5 else f"poisson_{int(rate)}_per_s"
+        c128[key] = serve.latency_summary(res, wall)
+    out["complex128"] = c128
     return out
 
 

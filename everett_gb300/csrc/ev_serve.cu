@@ -131,7 +131,9 @@ int run_single(ev_server* s, Request* r, std::vector<uint8_t>* classical) {
   o.dtype = s->opts.dtype;
   o.mode = s->opts.mode;
   o.variant = s->opts.variant;
-  if (o.mode == EV_MODE_FUSED && o.dtype != EV_C64) o.mode = EV_MODE_TILED;
+  // a fused arithmetic of the other amplitude type runs the tile pass instead
+  if (o.mode == EV_MODE_FUSED && (o.variant == EV_FUSED_OZAKI) != (o.dtype == EV_C128))
+    o.mode = EV_MODE_TILED;
   const ev_circuit c = circuit_of(*r);
   classical->assign(r->ncl ? r->ncl : 1, 0);
   int rc = ev_state_run(st, &c, r->seed, &o, classical->data());

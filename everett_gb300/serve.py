@@ -48,16 +48,19 @@ class Result:
 
 
 _MODES = {"exact": N.MODE_EXACT, "tiled": N.MODE_TILED, "fused": N.MODE_FUSED}
-_VARIANTS = {"tf32x3": N.FUSED_TF32X3, "bf16x3": N.FUSED_BF16X3, "fp32": N.FUSED_FP32}
+_VARIANTS = {"tf32x3": N.FUSED_TF32X3, "bf16x3": N.FUSED_BF16X3, "fp32": N.FUSED_FP32,
+             "ozaki": N.FUSED_OZAKI}
 
 
 class Server:
-    def __init__(self, dtype="complex64", workers=8, mode="fused", variant="bf16x3",
+    def __init__(self, dtype="complex64", workers=8, mode="fused", variant=None,
                  hbm_budget=0, batch_small=True, batch_qubits=0, start_paused=False):
         o = EvServerOptions()
         o.dtype = N.C128 if dtype in ("complex128", "c128") else N.C64
         o.workers = workers
         o.mode = _MODES[mode]
+        if variant is None:  # the fused arithmetic of the amplitude type
+            variant = "ozaki" if o.dtype == N.C128 else "bf16x3"
         o.variant = _VARIANTS[variant]
         o.hbm_budget = int(hbm_budget)
         o.batch_small = 1 if batch_small else 0

@@ -6,7 +6,10 @@ alone (one at a time) and once together with all the others in flight.
 Shots and classical bits must be identical (the path a request takes and
 every path's arithmetic are independent of the rest of the mix).  For
 complex128 they must also equal the oracle's run (classical bits) and the
-oracle's sampler on the oracle's final state (shots)."""
+oracle's sampler on the oracle's final state (shots) -- in tiled mode because
+its arithmetic is the reference's, in fused mode (5-qubit unitaries by digit
+slicing, within ~1e-16 of it) because no uniform of these seeds falls that
+close to a decision boundary."""
 import numpy as np
 import pytest
 
@@ -21,8 +24,8 @@ def mix(count, seed, nmin, nmax):
     return [workloads.serve_request(rng, nmin, nmax) for _ in range(count)]
 
 
-@pytest.mark.parametrize("dtype,mode", [("complex128", "tiled"), ("complex64", "fused"),
-                                        ("complex64", "tiled")])
+@pytest.mark.parametrize("dtype,mode", [("complex128", "tiled"), ("complex128", "fused"),
+                                        ("complex64", "fused"), ("complex64", "tiled")])
 def test_serving_alone_equals_mixed(gpu, dtype, mode):
     reqs = mix(24, 7, 6, 16)
     alone = []
