@@ -611,7 +611,7 @@ def extras_kernels(n: int, peak: float, reps: int = 3):
             ("norm_sqr", lambda: st.norm_sqr(), Nn * B, 2),
             ("normalize", lambda: st.normalize(), 3 * Nn * B, 4),
             ("overlap", lambda: st.overlap(other), 2 * Nn * B, 4),
-            ("sample_1000_shots", lambda: st.sample(1000, seed=1), Nn * B + 16 * Nn, 3),
+            ("sample_1000_shots", lambda: st.sample(1000, seed=1), Nn * B + 8 * Nn, 3),
             ("pauli_8_diagonal_terms", lambda: st.pauli_expectation(zdiag), Nn * B, 10),
             ("pauli_8_terms_shared_x", lambda: st.pauli_expectation(xshared), Nn * B, 5),
         ]

@@ -410,6 +410,73 @@ __global__ void __launch_bounds__(256)
     out[r] = __dadd_rn(in[r], in[r + w]);
 }
 
+// Several levels per pass.  Level q holds 2^q sums at mass + 2^q - 1, entry
+// e = level q+1 entry e + level q+1 entry e + 2^q.  The entries of L
+// consecutive levels that end in entry r of the lowest of them form a
+// subtree over the 2^L source entries r + j S of the level above them
+// (S = the lowest level's width), so one thread reads those 2^L values once,
+// forms the subtree with the same sums in the same order as level by level,
+// and writes every level of it: each level is written once and no level but
+// the source is read.
+
+// Levels n-1 (leaves) .. n-L from the amplitudes.
+template <typename V, int L>
+__global__ void __launch_bounds__(256)
+    k_mass_leaf_fused(const V* __restrict__ a, int n, double* __restrict__ mass) {
+  constexpr int C = 1 << (L - 1);  // leaves per thread
+  const uint64_t S = uint64_t(1) << (n - L);
+  const uint64_t half = uint64_t(1) << (n - 1);
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < S; r += stride) {
+    V lo[C], hi[C];
+#pragma unroll
+    for (int j = 0; j < C; ++j) {
+      lo[j] = a[r + uint64_t(j) * S];
+      hi[j] = a[r + uint64_t(j) * S + half];
+    }
+    double m[C];
+#pragma unroll
+    for (int j = 0; j < C; ++j) {
+      m[j] = leaf_mass(lo[j], hi[j]);
+      mass[(half - 1) + r + uint64_t(j) * S] = m[j];
+    }
+#pragma unroll
+    for (int lev = 1; lev < L; ++lev) {
+      const int cnt = C >> lev;
+      const uint64_t w = uint64_t(cnt) * S;
+#pragma unroll
+      for (int j = 0; j < cnt; ++j) {
+        m[j] = __dadd_rn(m[j], m[j + cnt]);
+        mass[(w - 1) + r + uint64_t(j) * S] = m[j];
+      }
+    }
+  }
+}
+
+// Levels qsrc-1 .. qsrc-L from level qsrc.
+template <int L>
+__global__ void __launch_bounds__(256) k_mass_level_fused(double* __restrict__ mass, int qsrc) {
+  constexpr int C = 1 << L;  // source entries per thread
+  const uint64_t S = uint64_t(1) << (qsrc - L);
+  const double* __restrict__ src = mass + ((uint64_t(1) << qsrc) - 1);
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < S; r += stride) {
+    double m[C];
+#pragma unroll
+    for (int j = 0; j < C; ++j) m[j] = src[r + uint64_t(j) * S];
+#pragma unroll
+    for (int lev = 1; lev <= L; ++lev) {
+      const int cnt = C >> lev;
+      const uint64_t w = uint64_t(cnt) * S;
+#pragma unroll
+      for (int j = 0; j < cnt; ++j) {
+        m[j] = __dadd_rn(m[j], m[j + cnt]);
+        mass[(w - 1) + r + uint64_t(j) * S] = m[j];
+      }
+    }
+  }
+}
+
 // Levels top..0 of the tree in one block (level top already built).
 __global__ void __launch_bounds__(1024) k_mass_top(double* __restrict__ mass, int top) {
   for (int q = top - 1; q >= 0; --q) {
@@ -552,23 +619,48 @@ static int ensure_mass(ev_state* s) {
 
 static int build_mass(ev_state* s) {
   const int n = int(s->n);
-  ProfScope prof(s, P_SAMPLE, double(s->len()) * double(s->amp_bytes()) + 16.0 * double(s->len()));
-  s->launches += 1 + (n - 2 >= 12 ? n - 13 : 0) + 1;
+  // the amplitudes read once, the 2^n - 1 tree entries written once
+  ProfScope prof(s, P_SAMPLE, double(s->len()) * double(s->amp_bytes()) + 8.0 * double(s->len()));
+  constexpr int L = 4;   // levels per pass
+  constexpr int LL = 4;  // levels of the leaf pass (three measured slower at 30 qubits)
   double* mass = s->mass;
   const uint64_t half = s->len() / 2;
-  double* top = mass + (half - 1);  // level n-1
-  if (s->dtype == EV_C128)
-    k_mass_leaf<double2><<<grid_for(s, half), 256, 0, s->stream>>>(
-        static_cast<const double2*>(s->amps), half, top);
-  else
-    k_mass_leaf<float2><<<grid_for(s, half), 256, 0, s->stream>>>(
-        static_cast<const float2*>(s->amps), half, top);
-  int q = n - 2;
+  int q;  // highest level still to build
+  if (n - LL >= 12) {
+    const uint64_t S = uint64_t(1) << (n - LL);
+    if (s->dtype == EV_C128)
+      k_mass_leaf_fused<double2, LL><<<grid_for(s, S), 256, 0, s->stream>>>(
+          static_cast<const double2*>(s->amps), n, mass);
+    else
+      k_mass_leaf_fused<float2, LL><<<grid_for(s, S), 256, 0, s->stream>>>(
+          static_cast<const float2*>(s->amps), n, mass);
+    s->launches += 1;
+    q = n - 1 - LL;
+  } else {
+    double* top = mass + (half - 1);  // level n-1
+    if (s->dtype == EV_C128)
+      k_mass_leaf<double2><<<grid_for(s, half), 256, 0, s->stream>>>(
+          static_cast<const double2*>(s->amps), half, top);
+    else
+      k_mass_leaf<float2><<<grid_for(s, half), 256, 0, s->stream>>>(
+          static_cast<const float2*>(s->amps), half, top);
+    s->launches += 1;
+    q = n - 2;
+  }
+  for (; q - (L - 1) >= 12; q -= L) {
+    k_mass_level_fused<L><<<grid_for(s, uint64_t(1) << (q - (L - 1))), 256, 0, s->stream>>>(
+        mass, q + 1);
+    s->launches += 1;
+  }
   for (; q >= 12; --q) {
     const uint64_t w = uint64_t(1) << q;
     k_mass_level<<<grid_for(s, w), 256, 0, s->stream>>>(mass + (2 * w - 1), w, mass + (w - 1));
+    s->launches += 1;
   }
-  if (q >= 0) k_mass_top<<<1, 1024, 0, s->stream>>>(mass, q + 1);
+  if (q >= 0) {
+    k_mass_top<<<1, 1024, 0, s->stream>>>(mass, q + 1);
+    s->launches += 1;
+  }
   EV_CUDA(cudaGetLastError());
   return EV_OK;
 }
