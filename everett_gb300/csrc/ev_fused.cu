@@ -1038,7 +1038,10 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_slot;
   if (warp == kOzWorkers / 32) {
+    // the MMA warp
     if (lane == 0) {
+      // descriptor start addresses are address >> 4: offsets add directly
+      const uint64_t ad = sw128_desc(smem_addr(a_sl)), bd = sw128_desc(smem_addr(b_sl));
       uint32_t aphase = 0;
       for (uint64_t st = blockIdx.x; st < d.nsteps; st += gridDim.x) {
         if (!mbar_wait(&abar, aphase, kWaitLimit)) {
@@ -1046,35 +1049,31 @@ __global__ void __launch_bounds__(kOzThreads, 1)
           break;
         }
         aphase ^= 1;
-        {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      // descriptor start addresses are address >> 4: offsets add directly
-      const uint64_t ad = sw128_desc(smem_addr(a_sl)), bd = sw128_desc(smem_addr(b_sl));
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll 1
-      for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < 2; ++h) {
 #pragma unroll 1
-        for (int i = 0; i < oz::kDigits; ++i) {
-          const uint32_t n = uint32_t(32 * (oz::kDigits - i));
-          // f32 accumulate, FP16 A and B, K-major, N, M = 128
-          const uint32_t idesc = (1u << 4) | ((n >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
-          const uint64_t a = ad + uint64_t(i * (Sh::A_SLICE >> 4));
-          const uint64_t bb = bd + uint64_t(h * (Sh::HALF_COLS * 128 >> 4));
-          const uint32_t dt = tmem + uint32_t(h * Sh::HALF_COLS + 32 * i);
+          for (int i = 0; i < oz::kDigits; ++i) {
+            const uint32_t n = uint32_t(32 * (oz::kDigits - i));
+            // f32 accumulate, FP16 A and B, K-major, N, M = 128
+            const uint32_t idesc = (1u << 4) | ((n >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
+            const uint64_t a = ad + uint64_t(i * (Sh::A_SLICE >> 4));
+            const uint64_t bb = bd + uint64_t(h * (Sh::HALF_COLS * 128 >> 4));
+            const uint32_t dt = tmem + uint32_t(h * Sh::HALF_COLS + 32 * i);
 #pragma unroll
-          for (int kk = 0; kk < 4; ++kk)
-            mma_f16(dt, a + uint64_t(kk * 2), bb + uint64_t(kk * 2), idesc, (i | kk) != 0);
+            for (int kk = 0; kk < 4; ++kk)
+              mma_f16(dt, a + uint64_t(kk * 2), bb + uint64_t(kk * 2), idesc, (i | kk) != 0);
+          }
+          asm volatile(
+              "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                  smem_addr(&bar[h]))
+              : "memory");
         }
-        asm volatile(
-            "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                smem_addr(&bar[h]))
-            : "memory");
-      }
-    }
       }
     }
     __syncwarp();
     __syncthreads();
-    return;
+    return;  // TMEM is freed by warp 0
   }
   uint32_t phase = 0;
   bool ok = true;
@@ -1159,28 +1158,21 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 #pragma unroll
     for (int c0 = 0; c0 < 16; c0 += 8) {
       const uint32_t ta = lane_tmem + col0 + uint32_t(c0);
-      int32_t g3[8], g2[8];
       int64_t acc[8];
       {
-        uint32_t v[4][8];
+        uint32_t v[oz::kDigits][8];
 #pragma unroll
-        for (int dg = 0; dg < 4; ++dg) tmem_ld8(ta + uint32_t(32 * dg), v[dg]);
+        for (int dg = 0; dg < oz::kDigits; ++dg) tmem_ld8(ta + uint32_t(32 * dg), v[dg]);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int c = 0; c < 8; ++c)
+        for (int c = 0; c < 8; ++c) {
+          int32_t g3, g2;
           oz::combine_hi(__uint_as_float(v[0][c]), __uint_as_float(v[1][c]),
-                         __uint_as_float(v[2][c]), __uint_as_float(v[3][c]), g3[c], g2[c]);
-      }
-      {
-        uint32_t v[3][8];
-#pragma unroll
-        for (int dg = 0; dg < 3; ++dg) tmem_ld8(ta + uint32_t(32 * (dg + 4)), v[dg]);
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-        for (int c = 0; c < 8; ++c)
-          acc[c] = oz::combine_g(g3[c], g2[c],
-                                 oz::combine_lo(__uint_as_float(v[0][c]), __uint_as_float(v[1][c]),
-                                                __uint_as_float(v[2][c])));
+                         __uint_as_float(v[2][c]), __uint_as_float(v[3][c]), g3, g2);
+          acc[c] = oz::combine_g(g3, g2,
+                                 oz::combine_lo(__uint_as_float(v[4][c]), __uint_as_float(v[5][c]),
+                                                __uint_as_float(v[6][c])));
+        }
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
