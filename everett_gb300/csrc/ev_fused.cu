@@ -1,4 +1,5 @@
-// ev_fused.cu -- complex64 gate runs fused into dense k-qubit unitaries.
+// ev_fused.cu -- gate runs fused into dense k-qubit unitaries (complex64,
+// and complex128 by digit slicing).
 //
 // The host groups consecutive gate records into blocks that act on at most
 // k qubits (a record may move ahead of earlier records that share none of
@@ -12,13 +13,16 @@
 //               W[2f][2a+1] = Im U[a][f], W[2f+1][2a+1] = Re U[a][f],
 // a real GEMM with K = N = 2^(k+1).
 //
-// Three arithmetics:
-//   EV_FUSED_TF32X3  tcgen05.mma kind::tf32, x = x_hi + x_lo and
+// Four arithmetics:
+//   EV_FUSED_TF32X3  complex64; tcgen05.mma kind::tf32, x = x_hi + x_lo and
 //                    W = W_hi + W_lo split into TF32 parts, D accumulates
 //                    x_hi W_hi + x_hi W_lo + x_lo W_hi in f32 (TMEM)
-//   EV_FUSED_BF16X3  the same with BF16 parts (kind::f16)
-//   EV_FUSED_FP32    CUDA cores, f32 complex multiply-add
-// The tensor-core kernel stages 128 rows per step: loads gather the rows
+//   EV_FUSED_BF16X3  complex64; the same with BF16 parts (kind::f16)
+//   EV_FUSED_FP32    complex64; CUDA cores, f32 complex multiply-add
+//   EV_FUSED_OZAKI   complex128; k = 5, each f64 as seven 8-bit FP16 digits
+//                    (kind::f16), exact digit-pair sums in TMEM, int64
+//                    recombination (ev_ozaki.cuh, k_fused_oz below)
+// The complex64 tensor-core kernel stages 128 rows per step: loads gather the rows
 // (addresses contiguous for at least 128 amplitudes because the row qubits
 // are the lowest qubits outside F), split into hi/lo and write the A operand
 // in the 128-byte-swizzled K-major layout; one thread issues the MMAs and
