@@ -348,6 +348,48 @@ def extras_c128_fused(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, p
     return out
 
 
+def extras_cfg0(L, N):
+    """The 20-qubit depth-20 random-layer circuit with 10000 full-register
+    shots: the GPU paths (circuit and shots timed on the device) beside the
+    scalar oracle of the reference's loops on one host core (a CPU baseline
+    leg: the whole circuit and the same shots)."""
+    import numpy as np
+
+    import oracle as O
+    from everett_gb300 import State, workloads
+    n, depth, shots = 20, 20, 10000
+    c = workloads.random_layers(n, depth, seed=1)
+    t0 = time.perf_counter()
+    want, _, _ = O.run_seeded(c, 0)
+    cpu_shots = O.sample_tree(want, 7, shots)
+    cpu_ms = (time.perf_counter() - t0) * 1e3
+    out = {"workload": f"random-layer circuit, {n} qubits, depth {depth} ({len(c)} ops), "
+                       f"complex128, then {shots} full-register shots",
+           "cpu_oracle_1_core_ms": round(cpu_ms, 1)}
+    for name, kw in (("tiled", dict(mode="tiled")),
+                     ("fused_ozaki", dict(mode="fused", variant="ozaki"))):
+        st = State.zero(n, "complex128")
+        from everett_gb300 import CudaStateVectorBackend
+        CudaStateVectorBackend.run_into(st, c, 0, **kw)
+        st.sample(shots, seed=7)
+        h = st.handle
+        reps = 5
+        N.check(L.ev_state_record_event(h, 0))
+        for _ in range(reps):
+            CudaStateVectorBackend.run_into(st, c, 0, **kw)
+            got_shots = st.sample(shots, seed=7)
+        N.check(L.ev_state_record_event(h, 1))
+        ms = C.c_float()
+        N.check(L.ev_state_elapsed_ms(h, 0, 1, C.byref(ms)))
+        err = float(np.max(np.abs(st.amplitudes() - want)))
+        out[name] = {"ms_per_run_with_shots": round(ms.value / reps, 3),
+                     "speedup_vs_cpu_oracle_1_core": round(cpu_ms / (ms.value / reps), 1),
+                     "max_abs_err_vs_oracle": err,
+                     "shots_equal_oracle": bool(np.array_equal(got_shots, cpu_shots))}
+        del st
+    return out
+
+
 def extras_qft(L, N, n, peak):
     import numpy as np
 
@@ -842,6 +884,7 @@ def run_ours(args, dist: Dist):
                             ("complex64_fused_same_circuit",
                              lambda: extras_c64(L, N, state, circuit, c128_ms, bytes_per_step,
                                                 peak, peak_kind)),
+                            ("cfg0_20q_shots", lambda: extras_cfg0(L, N)),
                             ("qft", lambda: extras_qft(L, N, n, peak)),
                             ("haar28_depth40", lambda: extras_haar(L, N)),
                             ("batch_tfim4096", extras_batch),
