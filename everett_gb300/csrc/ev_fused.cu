@@ -1283,6 +1283,12 @@ static int int_of_f16(uint16_t h) {
 // exponents F_n (ev_ozaki.cuh).
 static void oz_slice_columns(const double* Wt, std::vector<unsigned char>* out) {
   constexpr int K = oz::kK;
+  // FP16 bits of every digit value, -128..128
+  static const std::vector<uint16_t> f16_tab = [] {
+    std::vector<uint16_t> t(257);
+    for (int v = -128; v <= 128; ++v) t[size_t(v + 128)] = f16_of_int(v);
+    return t;
+  }();
   out->assign(OzShape::BLOB, 0);
   uint16_t* sl = reinterpret_cast<uint16_t*>(out->data());
   int32_t* fe = reinterpret_cast<int32_t*>(out->data() + oz::kDigits * OzShape::B_SLICE);
@@ -1298,8 +1304,11 @@ static void oz_slice_columns(const double* Wt, std::vector<unsigned char>* out) 
       uint64_t u;
       std::memcpy(&u, &Wt[size_t(n) * K + k], 8);
       const int64_t M = oz::fixed55(uint32_t(u >> 32), uint32_t(u), E);
-      for (int i = 0; i < oz::kDigits; ++i)
-        sl[size_t(i) * K * K + size_t(n) * K + k] = f16_of_int(oz::digit(M, i));
+      const uint64_t b = uint64_t(M) + oz::kBias;  // low bytes: digits 6..1 plus 128
+      uint16_t* col = sl + size_t(n) * K + k;
+      col[0] = f16_tab[size_t((int32_t(uint32_t(b >> 32)) >> 16) + 128)];
+      for (int i = 1; i < oz::kDigits; ++i)
+        col[size_t(i) * K * K] = f16_tab[size_t((b >> (8 * (oz::kDigits - 1 - i))) & 0xFFu)];
     }
   }
 }
