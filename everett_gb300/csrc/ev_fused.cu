@@ -889,8 +889,8 @@ __global__ void __launch_bounds__(kTmaThreads)
 // columns 16 (t / 128) .. + 15.
 //
 // A step s: the workers write the A slices from the prepared digits of s,
-// start loading the rows of s + 1, meet at a named barrier and signal the MMA
-// warp (abar); its lane 0 issues the MMAs of output half 0 (committed to
+// start loading the rows of s + 1, meet at a barrier (wbar: an mbarrier, so
+// that the wait is bounded) and signal the MMA warp (abar); its lane 0 issues the MMAs of output half 0 (committed to
 // bar[0]) and half 1 (bar[1]) -- issue blocks at about the tensor core's
 // pace, hence a warp of its own; meanwhile the workers prepare s + 1
 // (largest exponent, fixed-point values), then recombine s once its half is
@@ -1001,7 +1001,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   extern __shared__ unsigned char smem_raw[];
   __shared__ FusedDesc d;
   __shared__ __align__(8) uint64_t bar[2];
-  __shared__ __align__(8) uint64_t abar;
+  __shared__ __align__(8) uint64_t abar;  // A slices of a step written
+  __shared__ __align__(8) uint64_t wbar;  // all workers past their digit writes
   __shared__ uint32_t tmem_slot;
   __shared__ int fexp[K];
   __shared__ int rowexp[2][kRows];
@@ -1028,6 +1029,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[0])));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&bar[1])));
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&abar)));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&wbar)),
+                 "n"(kOzWorkers));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -1139,7 +1142,14 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     }
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    asm volatile("bar.sync 1, %0;" ::"n"(kOzWorkers) : "memory");
+    // the workers meet (every one arrives, the wait is bounded), then the
+    // MMA warp is told that the A slices of this step are complete
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&wbar)) : "memory");
+    if (!mbar_wait(&wbar, phase, kWaitLimit)) {
+      ok = false;
+      atomicExch(err, 1);
+      break;
+    }
     if (tid == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&abar)) : "memory");
     // the rows of the step after next into L2 (contiguous runs of 2^lowbits
     // amplitudes, at most 32 of them), so that next step's loads hit L2
