@@ -261,6 +261,18 @@ struct RunPlan {
   ~RunPlan() { release(); }
 };
 
+// The device flag of a run: 0 ok, kFlagNonFinite when the digit-sliced
+// complex128 pass met a non-finite amplitude, otherwise a bounded wait that
+// gave up.
+static int device_flag_status(uint32_t flag) {
+  if (flag == 0) return EV_OK;
+  if (flag == uint32_t(kFlagNonFinite))
+    return fail(EV_ERR_INVALID_ARGUMENT,
+                "a non-finite amplitude reached the fused complex128 pass, whose fixed-point digits "
+                "cannot carry it");
+  return fail(EV_ERR_TIMEOUT, "a bounded device wait gave up during the run");
+}
+
 static int build_plan(ev_state* s, const ev_circuit* c, const ev_run_options* o, bool device_seed,
                       RunPlan* plan) {
   const int mode = o ? o->mode : EV_MODE_EXACT;
@@ -359,13 +371,13 @@ static int build_plan(ev_state* s, const ev_circuit* c, const ev_run_options* o,
 
 // Enqueues a planned run.  zero: reset the state to |0...0> first.  The
 // classical register and the two device flags are copied to the host
-// buffers given (flags[1] != 0: a bounded device wait gave up).
+// buffers given (flags[1]: see device_flag_status).
 static int execute_plan(ev_state* s, const RunPlan& plan, bool zero, uint8_t* classical_host,
                         uint32_t* flags_host) {
   if (zero) EV_TRY(state_zero(s));
   const uint64_t ncl = plan.num_classical ? plan.num_classical : 1;
   EV_CUDA(cudaMemsetAsync(plan.classical, 0, ncl, s->stream));
-  // counter[0]: uniforms consumed; counter[1]: device timeout flag
+  // counter[0]: uniforms consumed; counter[1]: device flag (timeout, non-finite)
   EV_CUDA(cudaMemsetAsync(s->scratch.counter, 0, 2 * sizeof(uint32_t), s->stream));
   if (plan.dseed && plan.nmeas) {
     k_run_uniforms<<<1, 1, 0, s->stream>>>(plan.dseed, plan.uniforms, plan.nmeas);
@@ -427,8 +439,7 @@ static int run_ops(ev_state* s, const ev_circuit* c, uint64_t seed, const ev_run
   uint32_t flags[2] = {0, 0};
   EV_TRY(execute_plan(s, plan, false, classical_out, flags));
   EV_CUDA(cudaStreamSynchronize(s->stream));
-  if (flags[1] != 0) return fail(EV_ERR_TIMEOUT, "a bounded device wait gave up during the run");
-  return EV_OK;
+  return device_flag_status(flags[1]);
 }
 
 static int create_state(uint64_t n, int32_t dtype, ev_state** out) {
@@ -777,8 +788,7 @@ extern "C" int ev_prepared_launch(ev_prepared* p, uint64_t seed, uint8_t* classi
   EV_CUDA(cudaStreamSynchronize(s->stream));
   s->launches += p->kernels;
   if (ncl) std::memcpy(classical_out, p->classical_host(), ncl);
-  if (p->flags_host()[1] != 0) return fail(EV_ERR_TIMEOUT, "a bounded device wait gave up during the run");
-  return EV_OK;
+  return device_flag_status(p->flags_host()[1]);
 }
 
 extern "C" int ev_prepared_kernels(const ev_prepared* p, uint64_t* out) {

@@ -965,7 +965,7 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t v[8]) {
 // the row (two groups of four amplitudes, [re, im]) and becomes their biased
 // fixed-point values; returns the row's largest exponent (over its four
 // threads: lanes l, l + 8, l + 16, l + 24).
-__device__ __forceinline__ int oz_prepare(uint64_t (&v)[2][4][2]) {
+__device__ __forceinline__ int oz_prepare(uint64_t (&v)[2][4][2], int* err) {
   int em = 0;
 #pragma unroll
   for (int gi = 0; gi < 2; ++gi)
@@ -975,6 +975,7 @@ __device__ __forceinline__ int oz_prepare(uint64_t (&v)[2][4][2]) {
       for (int c = 0; c < 2; ++c) em = max(em, oz::exp_of(uint32_t(v[gi][i][c] >> 32)));
   em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, 8));
   em = max(em, __shfl_xor_sync(0xFFFFFFFFu, em, 16));
+  if (em == 0x7FF) atomicCAS(err, 0, kFlagNonFinite);  // NaN or infinity in the row
 #pragma unroll
   for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
@@ -1114,7 +1115,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
       for (int i = 0; i < 4; ++i) oz_load(s + (rb | d.ftab[4 * (pq + 4 * gi) + i]), b[gi][i]);
-    em = oz_prepare(b);
+    em = oz_prepare(b, err);
   }
   for (int par = 0; step < d.nsteps && ok; step += gridDim.x, par ^= 1) {
     // A slices of this step from the prepared digits
@@ -1160,7 +1161,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                    : "memory");
     }
     // prepare the next step while the tensor core works
-    if (nstep < d.nsteps) em = oz_prepare(b);
+    if (nstep < d.nsteps) em = oz_prepare(b, err);
     if (!mbar_wait(&bar[half], phase, kWaitLimit)) {
       ok = false;
       atomicExch(err, 1);

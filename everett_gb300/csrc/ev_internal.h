@@ -155,6 +155,11 @@ struct SegStep {
 
 // Plans ops [first, last) of a gate run (mode EV_MODE_TILED or
 // EV_MODE_FUSED) into segment steps whose data are appended to the blob.
+// Value a kernel leaves in the run's device flag (scratch counter 1) when a
+// fused complex128 pass meets a NaN or an infinity (other non-zero values: a
+// bounded wait gave up).
+constexpr int kFlagNonFinite = 2;
+
 int plan_segment(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int mode,
                  int bits, int variant, PlanBlob* blob, std::vector<SegStep>* out);
 // Launches one planned segment step (dblob = the uploaded blob).

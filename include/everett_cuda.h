@@ -104,7 +104,9 @@ enum {
   EV_FUSED_OZAKI = 3   /* complex128: tensor cores, each f64 as seven 8-bit
                           digits in FP16 (per-row / per-column scale), digit
                           products summed exactly in f32, recombined in
-                          int64 (the Ozaki scheme); k = 5                  */
+                          int64 (the Ozaki scheme); k = 5; a NaN or an
+                          infinity in the state makes the run return
+                          EV_ERR_INVALID_ARGUMENT                          */
 };
 typedef struct ev_run_options {
   int32_t dtype;     /* EV_C128 or EV_C64                                  */

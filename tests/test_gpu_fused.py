@@ -162,6 +162,26 @@ def test_ozaki_complex128_rows_of_mixed_scale(gpu):
         assert rel.max() <= 1e-14, (lo, rel.max())
 
 
+def test_ozaki_reports_non_finite_amplitudes(gpu):
+    """Fixed-point digits cannot carry a NaN or an infinity: a fused
+    complex128 pass over a state holding one reports it as an invalid
+    argument instead of returning finite numbers, and the next run on the
+    same state is unaffected."""
+    import everett_gb300.error as E
+    from everett_gb300 import State
+    n = 13
+    c = workloads.random_layers(n, 2, seed=4)
+    for bad in (float("nan"), float("inf")):
+        amps = O.sample_state(n) / np.sqrt(float(1 << n))
+        amps[777] = complex(bad, 0.0)
+        st = State.from_amplitudes(amps)
+        with pytest.raises(E.InvalidArgument):
+            CudaStateVectorBackend.drive(st, c, 0, mode="fused", variant="ozaki")
+        CudaStateVectorBackend.run_into(st, c, 0, mode="fused", variant="ozaki")
+        want, _, _ = O.run_seeded(c, 0)
+        assert np.max(np.abs(st.amplitudes() - want)) <= 1e-12
+
+
 def test_ozaki_rejects_complex64_and_complex64_variants_reject_complex128(gpu):
     import everett_gb300.error as E
     c = workloads.random_layers(13, 2, seed=1)
