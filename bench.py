@@ -297,16 +297,29 @@ def extras_c64(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, peak_kin
         kw = dict(mode="fused", variant=variant, tile_bits=5)
         timed_runs(L, N, st, circuit, 1, **kw)
         ms, prof = timed_runs(L, N, st, circuit, 3, **kw)
+        roof = roofline_of(prof, "fused_unitary", 2.0 * (1 << n) * 8, peak, peak_kind,
+                           f"k_fused_tc<5,{variant}> (fused 5-qubit unitary, tcgen05)",
+                           ncu_figure("k_fused_tc_bf16x3", "traffic_bytes_per_launch_full_size")
+                           if variant == "bf16x3" else None)
+        if roof:
+            # 3 split products of a 64 x 64 real GEMM per row of 32 amplitudes:
+            # 3 * 2 * 64 * 64 / 32 = 768 flops per amplitude (TF32 runs at half
+            # the BF16 rate, so its fraction is against half the BF16 peak)
+            flops = 768.0 * (1 << n)
+            tf = flops / (roof["avg_launch_ms"] / 1e3) / 1e12
+            bf = bf16_peak()
+            pk = bf[0] if variant == "bf16x3" else bf[0] / 2
+            roof["tensor"] = {"achieved_tflops": round(tf, 1), "peak_tflops": round(pk, 1),
+                              "frac": round(tf / pk, 4), "peak_source": bf[1] +
+                              ("" if variant == "bf16x3" else ", halved for TF32"),
+                              "flops_per_launch": flops}
         out[variant] = {
             "ms_per_run": round(ms, 2), "speedup_vs_complex128": round(c128_ms / ms, 1),
             "gate_GBps_complex128_equivalent": round(bytes_per_step / (ms / 1e3) / 1e9, 1),
             "fidelity_vs_complex128": fidelity(ref_state, st),
             "max_abs_err_vs_complex128": ref_state.max_abs_diff(st),
             "amplitude_updates_per_s": float(f"{len(circuit) * (1 << n) / (ms / 1e3):.4g}"),
-            "roofline": roofline_of(prof, "fused_unitary", 2.0 * (1 << n) * 8, peak, peak_kind,
-                                    f"k_fused_tc<5,{variant}> (fused 5-qubit unitary, tcgen05)",
-                                    ncu_figure("k_fused_tc_bf16x3", "traffic_bytes_per_launch_full_size")
-                                    if variant == "bf16x3" else None)}
+            "roofline": roof}
     del st
     return out
 
