@@ -24,6 +24,7 @@
 
 #include "ev_device.cuh"
 #include "ev_internal.h"
+#include "ev_softpair.cuh"
 
 struct ev_dm {
   uint64_t n = 0;
@@ -77,11 +78,108 @@ __device__ __forceinline__ void right2(const double2* u, double2& a, double2& b)
   b = s;
 }
 
+// The same left and right products with their multiplications formed on
+// the integer pipes (ev_softfp.cuh: a correctly rounded product, bit-identical
+// to the FP64 pipe's), for elements whose parts are normal and within the
+// fast domain.  Each matrix entry is classified once per CTA:
+//   FULL  both parts non-zero: the FMA form stays, its plain products move;
+//   REAL  imaginary part +-0: u * x = (RN(u.x x.x), RN(u.x x.y)) exactly
+//         (the FMA form adds a signed zero to a non-zero product);
+//   IMAG  real part +-0: u * x = (-RN(u.y x.y), RN(u.y x.x)) exactly;
+//   ZERO  both parts +-0: the term is a signed zero, and adding it to the
+//         other term of its row (non-zero, or +0 from an exact cancellation)
+//         returns that term unchanged, so it is skipped.
+// A matrix with a row of two ZERO entries (whose sum's sign would need the
+// signed-zero rules) or a part outside the fast domain takes the FP64 path,
+// and so does a 2x2 block with an element outside the domain.  The right
+// products x * conj(u) follow from the same classes.
+enum : uint32_t { SK_FULL = 0, SK_REAL = 1, SK_IMAG = 2, SK_ZERO = 3 };
+struct SoftU1 {
+  softfp::Unpacked ux[4], uy[4], nuy[4];  // u.x, u.y, -u.y
+  uint32_t kind[4];
+  uint32_t ok;
+};
+__device__ __forceinline__ void soft_u1(const double2* u, SoftU1* f) {
+  f->ok = 1;
+  for (int j = 0; j < 4; ++j) {
+    const bool zx = u[j].x == 0.0, zy = u[j].y == 0.0;
+    f->ux[j] = softfp::unpack(u[j].x);
+    f->uy[j] = softfp::unpack(u[j].y);
+    f->nuy[j] = softfp::unpack(-u[j].y);
+    f->kind[j] = zx && zy ? SK_ZERO : zy ? SK_REAL : zx ? SK_IMAG : SK_FULL;
+    if (!zx && !f->ux[j].ok) f->ok = 0;
+    if (!zy && !f->uy[j].ok) f->ok = 0;
+  }
+  if ((f->kind[0] == SK_ZERO && f->kind[1] == SK_ZERO) ||
+      (f->kind[2] == SK_ZERO && f->kind[3] == SK_ZERO))
+    f->ok = 0;
+}
+// u_j * x (cmul(u_j, x)) for an x whose parts are in the domain
+__device__ __forceinline__ double2 soft_left(const SoftU1& f, int j, double2 u, double2 x,
+                                             const SoftAmp& sx) {
+  switch (f.kind[j]) {
+    case SK_REAL: return make_double2(softfp::mul(f.ux[j], sx.x), softfp::mul(f.ux[j], sx.y));
+    case SK_IMAG: return make_double2(-softfp::mul(f.uy[j], sx.y), softfp::mul(f.uy[j], sx.x));
+    default: return scmul(u, f.uy[j], x, sx);  // FULL (ZERO is never used)
+  }
+}
+// x * conj(u_j) (cmul(x, conj(u_j)))
+__device__ __forceinline__ double2 soft_right(const SoftU1& f, int j, double2 u, double2 x,
+                                              const SoftAmp& sx) {
+  switch (f.kind[j]) {
+    case SK_REAL: return make_double2(softfp::mul(sx.x, f.ux[j]), softfp::mul(sx.y, f.ux[j]));
+    case SK_IMAG: return make_double2(softfp::mul(sx.y, f.uy[j]), -softfp::mul(sx.x, f.uy[j]));
+    default:
+      return make_double2(__fma_rn(x.x, u.x, -softfp::mul(sx.y, f.nuy[j])),
+                          __fma_rn(x.x, -u.y, softfp::mul(sx.y, f.ux[j])));
+  }
+}
+// one output of a row (j0, j1): the sum of its two terms, a ZERO term skipped
+template <bool kLeft>
+__device__ __forceinline__ double2 soft_row(const SoftU1& f, const double2* u, int j0, int j1,
+                                            double2 a, const SoftAmp& sa, double2 b,
+                                            const SoftAmp& sb) {
+  if (f.kind[j0] == SK_ZERO)
+    return kLeft ? soft_left(f, j1, u[j1], b, sb) : soft_right(f, j1, u[j1], b, sb);
+  const double2 p = kLeft ? soft_left(f, j0, u[j0], a, sa) : soft_right(f, j0, u[j0], a, sa);
+  if (f.kind[j1] == SK_ZERO) return p;
+  return cadd(p, kLeft ? soft_left(f, j1, u[j1], b, sb) : soft_right(f, j1, u[j1], b, sb));
+}
+// left2 / right2 on the pair (a, b), soft when the matrix and both elements
+// allow it
+__device__ __forceinline__ void left2_any(const double2* u, const SoftU1& f, double2& a, double2& b) {
+  const SoftAmp sa = sunpack(a), sb = sunpack(b);
+  if (f.ok & sok(sa) & sok(sb)) {
+    const double2 t = soft_row<true>(f, u, 0, 1, a, sa, b, sb);
+    const double2 s2 = soft_row<true>(f, u, 2, 3, a, sa, b, sb);
+    a = t;
+    b = s2;
+  } else {
+    left2(u, a, b);
+  }
+}
+__device__ __forceinline__ void right2_any(const double2* u, const SoftU1& f, double2& a,
+                                           double2& b) {
+  const SoftAmp sa = sunpack(a), sb = sunpack(b);
+  if (f.ok & sok(sa) & sok(sb)) {
+    const double2 t = soft_row<false>(f, u, 0, 1, a, sa, b, sb);
+    const double2 s2 = soft_row<false>(f, u, 2, 3, a, sa, b, sb);
+    a = t;
+    b = s2;
+  } else {
+    right2(u, a, b);
+  }
+}
+
 // rho -> U rho U^dagger on qubit t; with mask != 0 the left product applies
 // to rows whose bits in mask are all set, the right product to such columns.
 __global__ void __launch_bounds__(kDmThreads)
     k_dm_1q(double2* __restrict__ rho, int n, int t, U1 u, uint64_t mask, const uint8_t* pred) {
   if (dm_skip(pred)) return;
+  __shared__ SoftU1 su;
+  if (threadIdx.x == 0) soft_u1(u.m, &su);
+  __syncthreads();
+  const SoftU1& f = su;
   const uint64_t half = uint64_t(1) << (n - 1), blocks = half * half;
   const uint64_t dim = uint64_t(1) << n, bit = uint64_t(1) << t;
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
@@ -91,12 +189,12 @@ __global__ void __launch_bounds__(kDmThreads)
     double2 e00 = rho[r0 * dim + c0], e01 = rho[r0 * dim + c1];
     double2 e10 = rho[r1 * dim + c0], e11 = rho[r1 * dim + c1];
     if ((r0 & mask) == mask) {
-      left2(u.m, e00, e10);
-      left2(u.m, e01, e11);
+      left2_any(u.m, f, e00, e10);
+      left2_any(u.m, f, e01, e11);
     }
     if ((c0 & mask) == mask) {
-      right2(u.m, e00, e01);
-      right2(u.m, e10, e11);
+      right2_any(u.m, f, e00, e01);
+      right2_any(u.m, f, e10, e11);
     }
     rho[r0 * dim + c0] = e00;
     rho[r0 * dim + c1] = e01;
@@ -190,6 +288,9 @@ __global__ void __launch_bounds__(kDmThreads)
 __global__ void __launch_bounds__(kDmThreads)
     k_dm_channel(double2* __restrict__ rho, int n, int t, KrausSet ks, const uint8_t* pred) {
   if (dm_skip(pred)) return;
+  __shared__ SoftU1 sk[EV_MAX_KRAUS];
+  for (int k = threadIdx.x; k < ks.nops; k += blockDim.x) soft_u1(ks.k[k], &sk[k]);
+  __syncthreads();
   const uint64_t half = uint64_t(1) << (n - 1), blocks = half * half;
   const uint64_t dim = uint64_t(1) << n, bit = uint64_t(1) << t;
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
@@ -201,10 +302,11 @@ __global__ void __launch_bounds__(kDmThreads)
     double2 a00, a01, a10, a11;
     for (int k = 0; k < ks.nops; ++k) {
       double2 e00 = x00, e01 = x01, e10 = x10, e11 = x11;
-      left2(ks.k[k], e00, e10);
-      left2(ks.k[k], e01, e11);
-      right2(ks.k[k], e00, e01);
-      right2(ks.k[k], e10, e11);
+      const SoftU1& f = sk[k];
+      left2_any(ks.k[k], f, e00, e10);
+      left2_any(ks.k[k], f, e01, e11);
+      right2_any(ks.k[k], f, e00, e01);
+      right2_any(ks.k[k], f, e10, e11);
       if (k == 0) {
         a00 = e00;
         a01 = e01;
