@@ -667,8 +667,11 @@ def extras_kernels(n: int, peak: float, reps: int = 3):
             ("normalize", lambda: st.normalize(), 3 * Nn * B, 4),
             ("overlap", lambda: st.overlap(other), 2 * Nn * B, 4),
             ("sample_1000_shots", lambda: st.sample(1000, seed=1), Nn * B + 8 * Nn, 3),
-            ("pauli_8_diagonal_terms", lambda: st.pauli_expectation(zdiag), Nn * B, 10),
-            ("pauli_8_terms_shared_x", lambda: st.pauli_expectation(xshared), Nn * B, 5),
+            # per aligned block of 8 indices: 8 values (2 each), a 3-level
+            # Walsh-Hadamard transform (24 adds) and one add per term: 6 per
+            # index, 2^n indices for Z-only terms and 2^(n-1) with a shared X
+            ("pauli_8_diagonal_terms", lambda: st.pauli_expectation(zdiag), Nn * B, 6),
+            ("pauli_8_terms_shared_x", lambda: st.pauli_expectation(xshared), Nn * B, 3),
         ]
         res = {}
         for name, fn, nbytes, fp64 in cases:

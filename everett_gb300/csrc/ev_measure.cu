@@ -508,11 +508,30 @@ __global__ void __launch_bounds__(256)
 
 // ---- host ------------------------------------------------------------------
 
-// Blocks and the (even) per-block term range of a reduction over count terms.
-static void red_grid(uint64_t count, int sms, int max_blocks, int* nb_out, uint64_t* chunk_out) {
+// 256-thread blocks of a kernel that one SM holds at once (its register and
+// shared-memory use decide), at most 8, queried once per kernel.  A
+// grid-stride or chunked launch sized to one full wave of these leaves no
+// partial second wave draining on part of the SMs.
+template <auto Kernel>
+static int resident_blocks() {
+  static const int per_sm = [] {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, Kernel, 256, 0) != cudaSuccess) {
+      (void)cudaGetLastError();
+      v = 0;
+    }
+    return v < 1 ? 1 : (v > 8 ? 8 : v);
+  }();
+  return per_sm;
+}
+
+// Blocks and the (even) per-block term range of a reduction over count terms:
+// one block per 4096 terms, at most per_sm blocks on each SM.
+static void red_grid(uint64_t count, int sms, int per_sm, int max_blocks, int* nb_out,
+                     uint64_t* chunk_out) {
   const uint64_t want = (count + 4095) / 4096;
   int nb = int(want < 1 ? 1 : want);
-  int cap = sms * 8 < kMaxRedBlocks ? sms * 8 : kMaxRedBlocks;
+  int cap = sms * per_sm < kMaxRedBlocks ? sms * per_sm : kMaxRedBlocks;
   if (cap > max_blocks) cap = max_blocks;
   if (nb > cap) nb = cap;
   uint64_t chunk = (count + nb - 1) / nb;
@@ -526,29 +545,39 @@ static int reduce(const ev_state* s, const ev_state* other, uint64_t count, int 
                   const uint8_t* pred) {
   int nb = 0;
   uint64_t chunk = 0;
-  red_grid(count, s->num_sms, kMaxRedBlocks, &nb, &chunk);
   const bool c128 = s->dtype == EV_C128;
   if constexpr (OP == R_NORM || OP == R_P1) {
-    if (c128)
+    if (c128) {
+      red_grid(count, s->num_sms, resident_blocks<k_reduce_sq<OP, double2>>(), kMaxRedBlocks, &nb,
+               &chunk);
       k_reduce_sq<OP, double2><<<nb, kRedThreads, 0, s->stream>>>(
           static_cast<const double2*>(s->amps), count, chunk, k, s->scratch.partials, pred);
-    else
+    } else {
+      red_grid(count, s->num_sms, resident_blocks<k_reduce_sq<OP, float2>>(), kMaxRedBlocks, &nb,
+               &chunk);
       k_reduce_sq<OP, float2><<<nb, kRedThreads, 0, s->stream>>>(
           static_cast<const float2*>(s->amps), count, chunk, k, s->scratch.partials, pred);
+    }
   } else if (OP == R_OVERLAP && !c128) {
+    red_grid(count, s->num_sms, resident_blocks<k_overlap_c64>(), kMaxRedBlocks, &nb, &chunk);
     k_overlap_c64<<<nb, kRedThreads, 0, s->stream>>>(static_cast<const float2*>(s->amps),
                                                     static_cast<const float2*>(other->amps), count,
                                                     chunk, s->scratch.partials);
   } else if (OP == R_OVERLAP) {
+    red_grid(count, s->num_sms, resident_blocks<k_overlap_c128>(), kMaxRedBlocks, &nb, &chunk);
     k_overlap_c128<<<nb, kRedThreads, 0, s->stream>>>(static_cast<const double2*>(s->amps),
                                                      static_cast<const double2*>(other->amps), count,
                                                      chunk, s->scratch.partials);
   } else if (c128) {
+    red_grid(count, s->num_sms, resident_blocks<k_reduce<OP, double2>>(), kMaxRedBlocks, &nb,
+             &chunk);
     k_reduce<OP, double2><<<nb, kRedThreads, 0, s->stream>>>(
         static_cast<const double2*>(s->amps),
         other ? static_cast<const double2*>(other->amps) : nullptr, count, chunk, k,
         s->scratch.partials, pred);
   } else {
+    red_grid(count, s->num_sms, resident_blocks<k_reduce<OP, float2>>(), kMaxRedBlocks, &nb,
+             &chunk);
     k_reduce<OP, float2><<<nb, kRedThreads, 0, s->stream>>>(
         static_cast<const float2*>(s->amps),
         other ? static_cast<const float2*>(other->amps) : nullptr, count, chunk, k,
@@ -560,9 +589,9 @@ static int reduce(const ev_state* s, const ev_state* other, uint64_t count, int 
   return EV_OK;
 }
 
-static unsigned grid_for(const ev_state* s, uint64_t work) {
+static unsigned grid_for(const ev_state* s, uint64_t work, int per_sm = 8) {
   const uint64_t want = (work + 255) / 256;
-  const uint64_t cap = uint64_t(s->num_sms) * 8;
+  const uint64_t cap = uint64_t(s->num_sms) * uint64_t(per_sm);
   return unsigned(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
@@ -629,11 +658,13 @@ static int build_mass(ev_state* s) {
   if (n - LL >= 12) {
     const uint64_t S = uint64_t(1) << (n - LL);
     if (s->dtype == EV_C128)
-      k_mass_leaf_fused<double2, LL><<<grid_for(s, S), 256, 0, s->stream>>>(
-          static_cast<const double2*>(s->amps), n, mass);
+      k_mass_leaf_fused<double2, LL>
+          <<<grid_for(s, S, resident_blocks<k_mass_leaf_fused<double2, LL>>()), 256, 0,
+             s->stream>>>(static_cast<const double2*>(s->amps), n, mass);
     else
-      k_mass_leaf_fused<float2, LL><<<grid_for(s, S), 256, 0, s->stream>>>(
-          static_cast<const float2*>(s->amps), n, mass);
+      k_mass_leaf_fused<float2, LL>
+          <<<grid_for(s, S, resident_blocks<k_mass_leaf_fused<float2, LL>>()), 256, 0,
+             s->stream>>>(static_cast<const float2*>(s->amps), n, mass);
     s->launches += 1;
     q = n - 1 - LL;
   } else {
@@ -901,7 +932,7 @@ extern "C" int ev_max_abs_diff(const ev_state* self, const ev_state* other, doub
   EV_CUDA(cudaStreamSynchronize(other->stream));
   int nb = 0;
   uint64_t chunk = 0;
-  red_grid(self->len(), self->num_sms, kMaxRedBlocks, &nb, &chunk);
+  red_grid(self->len(), self->num_sms, 8, kMaxRedBlocks, &nb, &chunk);  // a maximum: any grid
   const bool a128 = self->dtype == EV_C128, b128 = other->dtype == EV_C128;
   double* part = self->scratch.partials;
   if (a128 && b128)
@@ -1039,91 +1070,189 @@ __global__ void __launch_bounds__(kRedThreads)
   if (threadIdx.x < kPauliTerms) partials[blockIdx.x * kPauliTerms + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-// The same sums over aligned blocks of 8 indices.  The parity of j & z is
-// the parity of the block's first index (one popcount per term per block)
-// xor that of (j mod 8) & z, read from a per-term table of 8 bits, so the
-// popcounts drop eightfold.  Valid when x == 0 or the highest bit of x is 3
-// or more: the 8 indices of a block are then 8 consecutive j, and their
-// partners j ^ x the aligned block of j0 ^ x in the order r ^ (x mod 8).
-constexpr int kPauliBlocksPerRun = 4;  // 32 terms per double-float run, as above
+// The same sums over aligned blocks of 8 indices (complex64).  The parity of
+// j & z is the parity of the block's first index j0 xor that of
+// (j mod 8) & (z mod 8), so a term's sum over the block is
+//     (-1)^popc(j0 & z) * W[z mod 8],  W[m] = sum_r (-1)^popc(r & m) v_r,
+// the Walsh-Hadamard transform of the block's 8 values v_r.  One 3-level
+// transform serves every term of the pass: 3 butterflies and one term
+// update per index for 8 terms, where adding each value to each term took
+// 8 updates.  Valid when x == 0 or the highest bit of x is 3 or more: the 8
+// indices of a block are then 8 consecutive j, and their partners j ^ x the
+// aligned block of j0 ^ x in the order r ^ (x mod 8).
+//
+// Values are unnormalised double-float pairs (hi + lo): every hi sum is
+// split exactly by two-sum and its error moves into lo, which carries the
+// exact product errors as well, so a pair holds its value to ~2^-48 of the
+// magnitudes summed into it.  A term's pair covers kPauliRun blocks and is
+// then added to its f64 sum.
+constexpr int kPauliRun = 16;  // blocks per double-float run
 
-template <typename V>
-__global__ void __launch_bounds__(kRedThreads)
-    k_pauli_blk(const V* __restrict__ a, uint64_t nblk, uint64_t chunk, uint64_t xmask, int hbit,
-                PauliPass pp, double* __restrict__ partials) {
+struct F2 {
+  float hi, lo;
+};
+
+// a b + c d with the products split exactly
+__device__ __forceinline__ F2 f2_dot2(float a, float b, float c, float d) {
+  const float p = __fmul_rn(a, b), q = __fmul_rn(c, d);
+  const float pe = __fmaf_rn(a, b, -p), qe = __fmaf_rn(c, d, -q);
+  const float s = __fadd_rn(p, q);
+  const float bp = __fsub_rn(s, p);
+  const float e = __fadd_rn(__fsub_rn(p, __fsub_rn(s, bp)), __fsub_rn(q, bp));
+  return {s, __fadd_rn(__fadd_rn(pe, qe), e)};
+}
+
+// (a, b) <- (a + b, a - b)
+__device__ __forceinline__ void f2_butterfly(F2& a, F2& b) {
+  const float s = __fadd_rn(a.hi, b.hi), d = __fsub_rn(a.hi, b.hi);
+  const float sb = __fsub_rn(s, a.hi), db = __fsub_rn(d, a.hi);
+  const float se = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, sb)), __fsub_rn(b.hi, sb));
+  const float de = __fsub_rn(__fsub_rn(a.hi, __fsub_rn(d, db)), __fadd_rn(b.hi, db));
+  const float ls = __fadd_rn(a.lo, b.lo), ld = __fsub_rn(a.lo, b.lo);
+  a = {s, __fadd_rn(ls, se)};
+  b = {d, __fadd_rn(ld, de)};
+}
+
+// acc += w
+__device__ __forceinline__ void f2_add(F2& acc, float whi, float wlo) {
+  const float s = __fadd_rn(acc.hi, whi);
+  const float bp = __fsub_rn(s, acc.hi);
+  const float e = __fadd_rn(__fsub_rn(acc.hi, __fsub_rn(s, bp)), __fsub_rn(whi, bp));
+  acc = {s, __fadd_rn(__fadd_rn(acc.lo, wlo), e)};
+}
+
+// 3 blocks per SM: 80 registers, no spills (4 spill)
+__global__ void __launch_bounds__(kRedThreads, 3)
+    k_pauli_blk(const float2* __restrict__ a, uint64_t nblk, uint64_t chunk, uint64_t xmask,
+                int hbit, PauliPass pp, double* __restrict__ partials) {
+  __shared__ float2 shw[8][kRedThreads];  // this thread's W, read back at index z mod 8
   const uint64_t lo = uint64_t(blockIdx.x) * chunk;
   const uint64_t hi = lo + chunk < nblk ? lo + chunk : nblk;
-  uint32_t tab[kPauliTerms];
-#pragma unroll
-  for (int t = 0; t < kPauliTerms; ++t) {
-    tab[t] = 0;
-#pragma unroll
-    for (int r = 0; r < 8; ++r) tab[t] |= uint32_t(__popc(uint32_t(r) & uint32_t(pp.z[t])) & 1) << r;
-  }
   const uint64_t xr = xmask & 7;
   double acc[kPauliTerms];
 #pragma unroll
   for (int t = 0; t < kPauliTerms; ++t) acc[t] = 0.0;
-  for (uint64_t base = lo + threadIdx.x; base < hi;
-       base += uint64_t(kPauliBlocksPerRun) * kRedThreads) {
-    FF f[kPauliTerms];
-    for (int g = 0; g < kPauliBlocksPerRun; ++g) {
+  for (uint64_t base = lo + threadIdx.x; base < hi; base += uint64_t(kPauliRun) * kRedThreads) {
+    F2 f[kPauliTerms];
+#pragma unroll
+    for (int t = 0; t < kPauliTerms; ++t) f[t] = {0.f, 0.f};
+    for (int g = 0; g < kPauliRun; ++g) {
       const uint64_t blk = base + uint64_t(g) * kRedThreads;
       if (blk >= hi) break;
       const uint64_t j0 = pp.part == 0 ? blk * 8 : insert0(blk * 8, hbit);
-      V x[8], y[8];
+      // j0 is a multiple of 8: the block is 64 aligned bytes
+      const float4* xp = reinterpret_cast<const float4*>(a + j0);
+      float4 xq[4];
 #pragma unroll
-      for (int r = 0; r < 8; ++r) x[r] = a[j0 + r];
-      if (pp.part != 0) {
+      for (int q = 0; q < 4; ++q) xq[q] = xp[q];
+      F2 w[8];
+      if (pp.part == 0) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          w[2 * q] = f2_dot2(xq[q].x, xq[q].x, xq[q].y, xq[q].y);
+          w[2 * q + 1] = f2_dot2(xq[q].z, xq[q].z, xq[q].w, xq[q].w);
+        }
+      } else {
         const uint64_t p0 = (j0 ^ xmask) & ~uint64_t(7);
+        float2 y[8];
 #pragma unroll
         for (int r = 0; r < 8; ++r) y[r] = a[p0 + (uint64_t(r) ^ xr)];
-      }
-      uint32_t sb = 0;  // bit t: parity of j0 & z_t
 #pragma unroll
-      for (int t = 0; t < kPauliTerms; ++t)
-        if (t < pp.nterms) sb |= uint32_t(__popcll(j0 & pp.z[t]) & 1) << t;
-#pragma unroll
-      for (int r = 0; r < 8; ++r) {
-        const V xv = x[r];
-        const V yv = pp.part != 0 ? y[r] : x[r];
-        if constexpr (sizeof(V) == 8) {
-          FF v;  // the term, exactly split: hi + lo
-          if (pp.part == 0) {
-            v.add_prod(xv.x, xv.x);
-            v.add_prod(xv.y, xv.y);
-          } else if (pp.part == 1) {
-            v.add_prod(yv.x, xv.x);
-            v.add_prod(yv.y, xv.y);
-          } else {
-            v.add_prod(yv.x, xv.y);
-            v.add_prod(-yv.y, xv.x);
+        for (int q = 0; q < 4; ++q) {
+          const float2 x0 = make_float2(xq[q].x, xq[q].y), x1 = make_float2(xq[q].z, xq[q].w);
+          const float2 y0 = y[2 * q], y1 = y[2 * q + 1];
+          if (pp.part == 1) {  // Re(conj(y) x)
+            w[2 * q] = f2_dot2(y0.x, x0.x, y0.y, x0.y);
+            w[2 * q + 1] = f2_dot2(y1.x, x1.x, y1.y, x1.y);
+          } else {  // Im(conj(y) x)
+            w[2 * q] = f2_dot2(y0.x, x0.y, -y0.y, x0.x);
+            w[2 * q + 1] = f2_dot2(y1.x, x1.y, -y1.y, x1.x);
           }
-#pragma unroll
-          for (int t = 0; t < kPauliTerms; ++t)
-            if (t < pp.nterms) {
-              const bool neg = ((tab[t] >> r) ^ (sb >> t)) & 1;
-              f[t].lo = __fadd_rn(f[t].lo, neg ? -v.lo : v.lo);
-              f[t].add(neg ? -v.hi : v.hi);
-            }
-        } else {
-          double v;
-          if (pp.part == 0)
-            v = __fma_rn(xv.x, xv.x, __dmul_rn(xv.y, xv.y));
-          else if (pp.part == 1)
-            v = __fma_rn(yv.x, xv.x, __dmul_rn(yv.y, xv.y));
-          else
-            v = __fma_rn(yv.x, xv.y, -__dmul_rn(yv.y, xv.x));
-#pragma unroll
-          for (int t = 0; t < kPauliTerms; ++t)
-            if (t < pp.nterms) acc[t] += (((tab[t] >> r) ^ (sb >> t)) & 1) ? -v : v;
         }
       }
-    }
-    if constexpr (sizeof(V) == 8) {
 #pragma unroll
-      for (int t = 0; t < kPauliTerms; ++t) acc[t] += f[t].value();
+      for (int h = 1; h < 8; h <<= 1)
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+          if (!(r & h)) f2_butterfly(w[r], w[r + h]);
+#pragma unroll
+      for (int m = 0; m < 8; ++m) shw[m][threadIdx.x] = make_float2(w[m].hi, w[m].lo);
+#pragma unroll
+      for (int t = 0; t < kPauliTerms; ++t)
+        if (t < pp.nterms) {
+          const float2 v = shw[pp.z[t] & 7][threadIdx.x];
+          const uint32_t flip = uint32_t(__popcll(j0 & pp.z[t]) & 1) << 31;
+          f2_add(f[t], __uint_as_float(__float_as_uint(v.x) ^ flip),
+                 __uint_as_float(__float_as_uint(v.y) ^ flip));
+        }
     }
+#pragma unroll
+    for (int t = 0; t < kPauliTerms; ++t) acc[t] += f2d_exact(f[t].hi) + f2d_exact(f[t].lo);
+  }
+  __shared__ double sh[kPauliTerms][kRedThreads];
+#pragma unroll
+  for (int t = 0; t < kPauliTerms; ++t) sh[t][threadIdx.x] = acc[t];
+  __syncthreads();
+  for (int w = kRedThreads / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+#pragma unroll
+      for (int t = 0; t < kPauliTerms; ++t) sh[t][threadIdx.x] += sh[t][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < kPauliTerms) partials[blockIdx.x * kPauliTerms + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// The block transform in complex128, on the FP64 pipe: per block of 8
+// indices 8 values (2 FP64 instructions each), 24 butterfly adds and one add
+// per term, 6 FP64 instructions per index for 8 terms where adding each
+// value to each term took 10.  3 blocks per SM: 80 registers, no spills.
+__global__ void __launch_bounds__(kRedThreads, 3)
+    k_pauli_blk_f64(const double2* __restrict__ a, uint64_t nblk, uint64_t chunk, uint64_t xmask,
+                    int hbit, PauliPass pp, double* __restrict__ partials) {
+  __shared__ double shw[8][kRedThreads];  // this thread's W, read back at index z mod 8
+  const uint64_t lo = uint64_t(blockIdx.x) * chunk;
+  const uint64_t hi = lo + chunk < nblk ? lo + chunk : nblk;
+  const uint64_t xr = xmask & 7;
+  double acc[kPauliTerms];
+#pragma unroll
+  for (int t = 0; t < kPauliTerms; ++t) acc[t] = 0.0;
+  for (uint64_t blk = lo + threadIdx.x; blk < hi; blk += kRedThreads) {
+    const uint64_t j0 = pp.part == 0 ? blk * 8 : insert0(blk * 8, hbit);
+    double w[8];
+    if (pp.part == 0) {
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const double2 x = a[j0 + r];
+        w[r] = __fma_rn(x.x, x.x, __dmul_rn(x.y, x.y));
+      }
+    } else {
+      const uint64_t p0 = (j0 ^ xmask) & ~uint64_t(7);
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const double2 x = a[j0 + r], y = a[p0 + (uint64_t(r) ^ xr)];
+        w[r] = pp.part == 1 ? __fma_rn(y.x, x.x, __dmul_rn(y.y, x.y))
+                            : __fma_rn(y.x, x.y, -__dmul_rn(y.y, x.x));
+      }
+    }
+#pragma unroll
+    for (int h = 1; h < 8; h <<= 1)
+#pragma unroll
+      for (int r = 0; r < 8; ++r)
+        if (!(r & h)) {
+          const double u = w[r], v = w[r + h];
+          w[r] = __dadd_rn(u, v);
+          w[r + h] = __dsub_rn(u, v);
+        }
+#pragma unroll
+    for (int m = 0; m < 8; ++m) shw[m][threadIdx.x] = w[m];
+#pragma unroll
+    for (int t = 0; t < kPauliTerms; ++t)
+      if (t < pp.nterms) {
+        const uint64_t flip = uint64_t(__popcll(j0 & pp.z[t]) & 1) << 63;
+        const double v = __longlong_as_double(
+            (long long)(uint64_t(__double_as_longlong(shw[pp.z[t] & 7][threadIdx.x])) ^ flip));
+        acc[t] = __dadd_rn(acc[t], v);
+      }
   }
   __shared__ double sh[kPauliTerms][kRedThreads];
 #pragma unroll
@@ -1207,14 +1336,26 @@ extern "C" int ev_pauli_expectation(const ev_state* s, const uint64_t* x_masks,
     const uint64_t work = x == 0 ? s->len() : s->len() / 2;
     int nb = 0;
     uint64_t chunk = 0;
-    if (s->dtype == EV_C64 && (x == 0 || hbit >= 3) && work >= 8) {
-      // blocks of 8 indices (complex64; complex128 stays on the FP64 adds of
-      // the per-index kernel, which measured no slower)
-      red_grid(work / 8, s->num_sms, kMaxRedBlocks * 4 / kPauliTerms, &nb, &chunk);
-      k_pauli_blk<float2><<<nb, kRedThreads, 0, s->stream>>>(
-          static_cast<const float2*>(s->amps), work / 8, chunk, x, hbit, pp, s->scratch.partials);
+    if ((x == 0 || hbit >= 3) && work >= 8) {
+      // aligned blocks of 8 indices, one Walsh-Hadamard transform each
+      if (s->dtype == EV_C128) {
+        red_grid(work / 8, s->num_sms, resident_blocks<k_pauli_blk_f64>(),
+                 kMaxRedBlocks * 4 / kPauliTerms, &nb, &chunk);
+        k_pauli_blk_f64<<<nb, kRedThreads, 0, s->stream>>>(static_cast<const double2*>(s->amps),
+                                                            work / 8, chunk, x, hbit, pp,
+                                                            s->scratch.partials);
+      } else {
+        red_grid(work / 8, s->num_sms, resident_blocks<k_pauli_blk>(),
+                 kMaxRedBlocks * 4 / kPauliTerms, &nb, &chunk);
+        k_pauli_blk<<<nb, kRedThreads, 0, s->stream>>>(static_cast<const float2*>(s->amps),
+                                                        work / 8, chunk, x, hbit, pp,
+                                                        s->scratch.partials);
+      }
     } else {
-      red_grid(work, s->num_sms, kMaxRedBlocks * 4 / kPauliTerms, &nb, &chunk);
+      red_grid(work, s->num_sms,
+               s->dtype == EV_C128 ? resident_blocks<k_pauli<double2>>()
+                                   : resident_blocks<k_pauli<float2>>(),
+               kMaxRedBlocks * 4 / kPauliTerms, &nb, &chunk);
       if (s->dtype == EV_C128)
         k_pauli<double2><<<nb, kRedThreads, 0, s->stream>>>(static_cast<const double2*>(s->amps),
                                                              work, chunk, x, hbit, pp,
@@ -1359,7 +1500,7 @@ extern "C" int ev_measure_qubit_noalloc(double* amps, uint64_t n, uint64_t k, do
   const uint64_t count = (uint64_t(1) << n) / 2;
   int nb = 0;
   uint64_t chunk = 0;
-  red_grid(count, sms, kNoAllocBlocks, &nb, &chunk);
+  red_grid(count, sms, resident_blocks<k_reduce_sq<R_P1, double2>>(), kNoAllocBlocks, &nb, &chunk);
   k_reduce_sq<R_P1, double2><<<nb, kRedThreads, 0, st>>>(a, count, chunk, int(k), partials, nullptr);
   k_finish<<<1, kRedThreads, 0, st>>>(partials, nb, result, nullptr);
   k_decide<<<1, 1, 0, st>>>(result, u, nullptr, nullptr, meas, nullptr, nullptr);
