@@ -634,6 +634,9 @@ def extras_kernels(n: int, peak: float, reps: int = 3):
     xshared = ["+" + "".join(("XY"[int(y)] if xb else "IZ"[int(b)])
                              for xb, y, b in zip(xpart, ypart, prng.integers(0, 2, n)))
                for _ in range(8)]
+    # eight strings with X on qubits 0 and 2 (partners inside blocks of 8)
+    xlow = ["+X" + "IZ"[int(prng.integers(0, 2))] + "X"
+            + "".join("IZ"[int(b)] for b in prng.integers(0, 2, n - 3)) for _ in range(8)]
     from everett_gb300 import CudaStateVectorBackend
     dense = workloads.random_layers(n, 2, seed=11)
     for dtype, B in (("complex128", 16), ("complex64", 8)):
@@ -672,6 +675,8 @@ def extras_kernels(n: int, peak: float, reps: int = 3):
             # index, 2^n indices for Z-only terms and 2^(n-1) with a shared X
             ("pauli_8_diagonal_terms", lambda: st.pauli_expectation(zdiag), Nn * B, 6),
             ("pauli_8_terms_shared_x", lambda: st.pauli_expectation(xshared), Nn * B, 3),
+            # X below qubit 3: the blocks cover all 2^n indices
+            ("pauli_8_terms_low_x", lambda: st.pauli_expectation(xlow), Nn * B, 6),
         ]
         res = {}
         for name, fn, nbytes, fp64 in cases:

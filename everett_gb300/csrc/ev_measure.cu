@@ -1077,9 +1077,12 @@ __global__ void __launch_bounds__(kRedThreads)
 // the Walsh-Hadamard transform of the block's 8 values v_r.  One 3-level
 // transform serves every term of the pass: 3 butterflies and one term
 // update per index for 8 terms, where adding each value to each term took
-// 8 updates.  Valid when x == 0 or the highest bit of x is 3 or more: the 8
-// indices of a block are then 8 consecutive j, and their partners j ^ x the
-// aligned block of j0 ^ x in the order r ^ (x mod 8).
+// 8 updates.  When x == 0 or the highest bit h of x is 3 or more, the 8
+// indices of a block are 8 consecutive j (bit h clear), and their partners
+// j ^ x the aligned block of j0 ^ x in the order r ^ (x mod 8).  When h < 3
+// the partner lies in the same block: the blocks then cover all 2^n indices
+// and the values of the indices with bit h set are zero, so each pair
+// (j, j ^ x) counts once, from the index with bit h clear.
 //
 // Values are unnormalised double-float pairs (hi + lo): every hi sum is
 // split exactly by two-sum and its error moves into lo, which carries the
@@ -1139,7 +1142,7 @@ __global__ void __launch_bounds__(kRedThreads, 3)
     for (int g = 0; g < kPauliRun; ++g) {
       const uint64_t blk = base + uint64_t(g) * kRedThreads;
       if (blk >= hi) break;
-      const uint64_t j0 = pp.part == 0 ? blk * 8 : insert0(blk * 8, hbit);
+      const uint64_t j0 = (pp.part == 0 || hbit < 3) ? blk * 8 : insert0(blk * 8, hbit);
       // j0 is a multiple of 8: the block is 64 aligned bytes
       const float4* xp = reinterpret_cast<const float4*>(a + j0);
       float4 xq[4];
@@ -1169,6 +1172,10 @@ __global__ void __launch_bounds__(kRedThreads, 3)
             w[2 * q + 1] = f2_dot2(y1.x, x1.y, -y1.y, x1.x);
           }
         }
+        if (hbit < 3)  // partner in the block: count each pair once
+#pragma unroll
+          for (int r = 0; r < 8; ++r)
+            if ((r >> hbit) & 1) w[r] = {0.f, 0.f};
       }
 #pragma unroll
       for (int h = 1; h < 8; h <<= 1)
@@ -1217,7 +1224,7 @@ __global__ void __launch_bounds__(kRedThreads, 3)
 #pragma unroll
   for (int t = 0; t < kPauliTerms; ++t) acc[t] = 0.0;
   for (uint64_t blk = lo + threadIdx.x; blk < hi; blk += kRedThreads) {
-    const uint64_t j0 = pp.part == 0 ? blk * 8 : insert0(blk * 8, hbit);
+    const uint64_t j0 = (pp.part == 0 || hbit < 3) ? blk * 8 : insert0(blk * 8, hbit);
     double w[8];
     if (pp.part == 0) {
 #pragma unroll
@@ -1233,6 +1240,10 @@ __global__ void __launch_bounds__(kRedThreads, 3)
         w[r] = pp.part == 1 ? __fma_rn(y.x, x.x, __dmul_rn(y.y, x.y))
                             : __fma_rn(y.x, x.y, -__dmul_rn(y.y, x.x));
       }
+      if (hbit < 3)  // partner in the block: count each pair once
+#pragma unroll
+        for (int r = 0; r < 8; ++r)
+          if ((r >> hbit) & 1) w[r] = 0.0;
     }
 #pragma unroll
     for (int h = 1; h < 8; h <<= 1)
@@ -1336,22 +1347,25 @@ extern "C" int ev_pauli_expectation(const ev_state* s, const uint64_t* x_masks,
     const uint64_t work = x == 0 ? s->len() : s->len() / 2;
     int nb = 0;
     uint64_t chunk = 0;
-    if ((x == 0 || hbit >= 3) && work >= 8) {
-      // aligned blocks of 8 indices, one Walsh-Hadamard transform each
+    if (s->len() >= 8) {
+      // aligned blocks of 8 indices, one Walsh-Hadamard transform each; an X
+      // mask below bit 3 pairs indices inside a block, whose blocks then
+      // cover every index
+      const uint64_t nblk = (x != 0 && hbit >= 3 ? work : s->len()) / 8;
       if (s->dtype == EV_C128) {
-        red_grid(work / 8, s->num_sms, resident_blocks<k_pauli_blk_f64>(),
+        red_grid(nblk, s->num_sms, resident_blocks<k_pauli_blk_f64>(),
                  kMaxRedBlocks * 4 / kPauliTerms, &nb, &chunk);
         k_pauli_blk_f64<<<nb, kRedThreads, 0, s->stream>>>(static_cast<const double2*>(s->amps),
-                                                            work / 8, chunk, x, hbit, pp,
+                                                            nblk, chunk, x, hbit, pp,
                                                             s->scratch.partials);
       } else {
-        red_grid(work / 8, s->num_sms, resident_blocks<k_pauli_blk>(),
+        red_grid(nblk, s->num_sms, resident_blocks<k_pauli_blk>(),
                  kMaxRedBlocks * 4 / kPauliTerms, &nb, &chunk);
         k_pauli_blk<<<nb, kRedThreads, 0, s->stream>>>(static_cast<const float2*>(s->amps),
-                                                        work / 8, chunk, x, hbit, pp,
+                                                        nblk, chunk, x, hbit, pp,
                                                         s->scratch.partials);
       }
-    } else {
+    } else {  // fewer than 8 amplitudes
       red_grid(work, s->num_sms,
                s->dtype == EV_C128 ? resident_blocks<k_pauli<double2>>()
                                    : resident_blocks<k_pauli<float2>>(),

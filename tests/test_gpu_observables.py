@@ -38,6 +38,15 @@ def test_pauli_expectation_matches_oracle(gpu, dtype):
         x = rng.integers(0, 2, n).astype(bool)
         ps += [PauliString(x, rng.integers(0, 2, n).astype(bool), bool(rng.integers(0, 2)))
                for _ in range(19)]
+        # X parts within qubits 0..2: each index's partner lies in its own
+        # aligned block of 8
+        for low in ((True,), (False, True), (True, False, True)):
+            if len(low) > n:
+                continue
+            xl = np.zeros(n, dtype=bool)
+            xl[:len(low)] = low
+            ps += [PauliString(xl, rng.integers(0, 2, n).astype(bool), bool(rng.integers(0, 2)))
+                   for _ in range(6)]
         got = st.pauli_expectation(ps)
         for p, g in zip(ps, got):
             xm, zm = p.masks()
