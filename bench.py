@@ -662,7 +662,9 @@ def extras_kernels(n: int, peak: float, reps: int = 3):
             ("cnot", lambda: st.apply_2q(hi, 3, Gate2.cnot()), Nn * B, 0),
             ("cz", lambda: st.apply_2q(hi, 3, Gate2.cz()), Nn * B // 2, 0),
             ("swap", lambda: st.apply_2q(hi, 3, Gate2.swap()), Nn * B, 0),
-            ("2q_dense", lambda: st.apply_2q(hi, 3, g2), 2 * Nn * B, 22),
+            # 16 FMA-form products (their 32 FMAs on the FP64 pipe, the 32
+            # plain products on the integer pipes) and 24 adds per quad
+            ("2q_dense", lambda: st.apply_2q(hi, 3, g2), 2 * Nn * B, 14),
             ("controlled_1q_1ctrl", lambda: st.apply_controlled_1q([hi], 5, g_dense), Nn * B, 3),
             ("measure_high", lambda: st.measure_qubit(hi, 0.25), 2 * Nn * B, 2),
             ("measure_low", lambda: st.measure_qubit(lo, 0.25), 2 * Nn * B, 2),

@@ -210,6 +210,63 @@ __global__ void __launch_bounds__(256) k_quad(V* __restrict__ s, uint64_t nquads
   }
 }
 
+// The imaginary parts of a 4x4 matrix, unpacked on the host for the
+// integer-pipe products (the factors of the plain multiplications of the
+// FMA-form complex multiply).
+struct SoftM2 {
+  softfp::Unpacked u[16];
+};
+
+// Dense (K2_DENSE) and diagonal (K2_DIAG) 4x4 updates on complex128 with the
+// plain products on the integer pipes (ev_softpair.cuh), bit-identical to
+// k_quad: the FMAs and adds stay on the FP64 pipe.  A quad holding an
+// amplitude outside softfp's domain takes the FP64 pipe for that quad.
+template <int KIND>
+__global__ void __launch_bounds__(256)
+    k_quad_soft(double2* __restrict__ s, uint64_t nquads, int lo, int hi, uint64_t bit_a,
+                uint64_t bit_b, M2<double2> m, SoftM2 sm, const uint8_t* pred) {
+  if (skip(pred)) return;
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < nquads; i += stride) {
+    const uint64_t base = insert0(insert0(i, lo), hi);
+    const uint64_t out[4] = {base, base | bit_b, base | bit_a, base | bit_a | bit_b};
+    double2 a[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) a[c] = s[out[c]];
+    if constexpr (KIND == K2_DIAG) {
+#pragma unroll
+      for (int c = 0; c < 4; ++c) s[out[c]] = soft_diag(m.m[5 * c], sm.u[5 * c], a[c]);
+    } else {
+      SoftAmp ua[4];
+      uint32_t ok = 1u;
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        ua[c] = sunpack(a[c]);
+        ok &= sok(ua[c]);
+      }
+      if (ok) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          double2 acc = scmul(m.m[4 * r + 0], sm.u[4 * r + 0], a[0], ua[0]);
+          acc = cadd(acc, scmul(m.m[4 * r + 1], sm.u[4 * r + 1], a[1], ua[1]));
+          acc = cadd(acc, scmul(m.m[4 * r + 2], sm.u[4 * r + 2], a[2], ua[2]));
+          acc = cadd(acc, scmul(m.m[4 * r + 3], sm.u[4 * r + 3], a[3], ua[3]));
+          s[out[r]] = acc;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          double2 acc = cmul(m.m[4 * r + 0], a[0]);
+          acc = cadd(acc, cmul(m.m[4 * r + 1], a[1]));
+          acc = cadd(acc, cmul(m.m[4 * r + 2], a[2]));
+          acc = cadd(acc, cmul(m.m[4 * r + 3], a[3]));
+          s[out[r]] = acc;
+        }
+      }
+    }
+  }
+}
+
 // ---- host side ---------------------------------------------------------
 
 static bool is0(const double* z) { return z[0] == 0.0 && z[1] == 0.0; }
@@ -247,9 +304,9 @@ Kind2 classify2(const double m[32]) {
   return diag ? K2_DIAG : K2_DENSE;
 }
 
-static unsigned grid_for(const ev_state* s, uint64_t work) {
+static unsigned grid_for(const ev_state* s, uint64_t work, int per_sm = 8) {
   const uint64_t want = (work + 255) / 256;
-  const uint64_t cap = uint64_t(s->num_sms) * 8;
+  const uint64_t cap = uint64_t(s->num_sms) * uint64_t(per_sm);
   return unsigned(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
@@ -334,8 +391,8 @@ static M2<V> to_m2(const double m[32]) {
 }
 
 template <typename V>
-static void go_apply2(ev_state* s, Kind2 kind, uint64_t a, uint64_t b, const double m[32],
-                      const uint8_t* pred) {
+static void go_apply2_fp64(ev_state* s, Kind2 kind, uint64_t a, uint64_t b, const double m[32],
+                           const uint8_t* pred) {
   V* st = static_cast<V*>(s->amps);
   const M2<V> mm = to_m2<V>(m);
   const uint64_t nq = s->len() / 4;
@@ -349,6 +406,44 @@ static void go_apply2(ev_state* s, Kind2 kind, uint64_t a, uint64_t b, const dou
     case K2_DIAG: k_quad<K2_DIAG><<<g, 256, 0, s->stream>>>(st, nq, lo, hi, ba, bb, mm, pred); break;
     case K2_DENSE: k_quad<K2_DENSE><<<g, 256, 0, s->stream>>>(st, nq, lo, hi, ba, bb, mm, pred); break;
   }
+}
+
+template <typename V>
+static void go_apply2(ev_state* s, Kind2 kind, uint64_t a, uint64_t b, const double m[32],
+                      const uint8_t* pred) {
+  go_apply2_fp64<V>(s, kind, a, b, m, pred);
+}
+
+// complex128 dense and diagonal 4x4: the integer-pipe products when every
+// imaginary part the kind multiplies by is in softfp's domain.
+template <>
+void go_apply2<double2>(ev_state* s, Kind2 kind, uint64_t a, uint64_t b, const double m[32],
+                        const uint8_t* pred) {
+  if (kind == K2_DENSE || kind == K2_DIAG) {
+    SoftM2 sm;
+    uint32_t ok = 1u;
+    for (int e = 0; e < 16; ++e) {
+      sm.u[e] = softfp::unpack(m[2 * e + 1]);
+      if (kind == K2_DENSE || e % 5 == 0) ok &= sm.u[e].ok;
+    }
+    if (ok) {
+      double2* st = static_cast<double2*>(s->amps);
+      const M2<double2> mm = to_m2<double2>(m);
+      const uint64_t nq = s->len() / 4;
+      const int lo = int(a < b ? a : b), hi = int(a < b ? b : a);
+      const uint64_t ba = uint64_t(1) << a, bb = uint64_t(1) << b;
+      if (kind == K2_DENSE)
+        k_quad_soft<K2_DENSE>
+            <<<grid_for(s, nq, resident_blocks<k_quad_soft<K2_DENSE>>()), 256, 0, s->stream>>>(
+                st, nq, lo, hi, ba, bb, mm, sm, pred);
+      else
+        k_quad_soft<K2_DIAG>
+            <<<grid_for(s, nq, resident_blocks<k_quad_soft<K2_DIAG>>()), 256, 0, s->stream>>>(
+                st, nq, lo, hi, ba, bb, mm, sm, pred);
+      return;
+    }
+  }
+  go_apply2_fp64<double2>(s, kind, a, b, m, pred);
 }
 
 int launch_apply2(ev_state* s, uint64_t a, uint64_t b, const double m[32], const uint8_t* pred) {

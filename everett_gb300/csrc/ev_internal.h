@@ -200,4 +200,21 @@ struct Rng {
   double next_f64() { return double(next_u64() >> 11) * (1.0 / 9007199254740992.0); }
 };
 
+// 256-thread blocks of a kernel that one SM holds at once (its register and
+// shared-memory use decide), at most 8, queried once per kernel.  A
+// grid-stride or chunked launch sized to one full wave of these leaves no
+// partial second wave draining on part of the SMs.
+template <auto Kernel>
+int resident_blocks() {
+  static const int per_sm = [] {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, Kernel, 256, 0) != cudaSuccess) {
+      (void)cudaGetLastError();
+      v = 0;
+    }
+    return v < 1 ? 1 : (v > 8 ? 8 : v);
+  }();
+  return per_sm;
+}
+
 }  // namespace ev

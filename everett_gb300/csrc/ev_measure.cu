@@ -508,23 +508,6 @@ __global__ void __launch_bounds__(256)
 
 // ---- host ------------------------------------------------------------------
 
-// 256-thread blocks of a kernel that one SM holds at once (its register and
-// shared-memory use decide), at most 8, queried once per kernel.  A
-// grid-stride or chunked launch sized to one full wave of these leaves no
-// partial second wave draining on part of the SMs.
-template <auto Kernel>
-static int resident_blocks() {
-  static const int per_sm = [] {
-    int v = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, Kernel, 256, 0) != cudaSuccess) {
-      (void)cudaGetLastError();
-      v = 0;
-    }
-    return v < 1 ? 1 : (v > 8 ? 8 : v);
-  }();
-  return per_sm;
-}
-
 // Blocks and the (even) per-block term range of a reduction over count terms:
 // one block per 4096 terms, at most per_sm blocks on each SM.
 static void red_grid(uint64_t count, int sms, int per_sm, int max_blocks, int* nb_out,
