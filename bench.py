@@ -658,7 +658,8 @@ def extras_kernels(n: int, peak: float, reps: int = 3):
             ("1q_real_h", lambda: st.apply_1q(hi - 3, Gate1.h()), 2 * Nn * B, 2),
             ("1q_diag_rz", lambda: st.apply_1q(hi - 1, Gate1.rz(0.3)), 2 * Nn * B, 2),
             ("1q_phase", lambda: st.apply_1q(hi - 2, Gate1.phase(0.3)), Nn * B, 1),
-            ("1q_anti_x", lambda: st.apply_1q(7, Gate1.x()), 2 * Nn * B, 4),
+            # X: a permutation (entries 0 and 1), no FP64 instruction
+            ("1q_anti_x", lambda: st.apply_1q(7, Gate1.x()), 2 * Nn * B, 0),
             ("cnot", lambda: st.apply_2q(hi, 3, Gate2.cnot()), Nn * B, 0),
             ("cz", lambda: st.apply_2q(hi, 3, Gate2.cz()), Nn * B // 2, 0),
             ("swap", lambda: st.apply_2q(hi, 3, Gate2.swap()), Nn * B, 0),

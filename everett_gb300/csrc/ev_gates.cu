@@ -14,7 +14,9 @@
 // Matrix-structure specialisations keep the reference's results: a zero
 // entry contributes an exact +-0 to the FMA-form sum and a real entry r
 // reduces fma(r, x, -(0*y)) to the rounded product r*x, so dropping those
-// terms changes no value (only, at most, the sign of a zero).
+// terms changes no value (only, at most, the sign of a zero).  In the same
+// way an anti-diagonal complex128 gate with entries in {1, i, -1, -i} (X, Y)
+// is applied as a permutation with sign flips.
 #include <cstdio>
 
 #include <type_traits>
@@ -95,6 +97,25 @@ __device__ __forceinline__ void pair_update_soft(double2* __restrict__ s, uint64
   }
 }
 
+// An entry in {1, i, -1, -i} as its power of i (0..3), else -1.
+__device__ __forceinline__ int unit_power(double2 m) {
+  if (m.y == 0.0) return m.x == 1.0 ? 0 : (m.x == -1.0 ? 2 : -1);
+  if (m.x == 0.0) return m.y == 1.0 ? 1 : (m.y == -1.0 ? 3 : -1);
+  return -1;
+}
+__device__ __forceinline__ double neg_if(double v, uint64_t flip) {
+  return __longlong_as_double((long long)(uint64_t(__double_as_longlong(v)) ^ flip));
+}
+// i^p a by moving parts and flipping sign bits: the FMA-form product with a
+// unit entry, whose products with the entry's zero part only add +-0, so
+// the two agree up to the sign of a zero (the latitude the zero-entry
+// specialisations above already take).
+__device__ __forceinline__ double2 unit_mul(int p, double2 a) {
+  constexpr uint64_t kSign = 0x8000000000000000ull;
+  const double x = (p & 1) ? a.y : a.x, y = (p & 1) ? a.x : a.y;
+  return make_double2(neg_if(x, (p == 1 || p == 2) ? kSign : 0u), neg_if(y, p >= 2 ? kSign : 0u));
+}
+
 // apply_1q over all 2^(n-1) pairs (kernel.rs:100-119).
 template <int KIND, typename V>
 __global__ void __launch_bounds__(256) k_pair(V* __restrict__ s, uint64_t npairs, int k, M1<V> m,
@@ -103,6 +124,19 @@ __global__ void __launch_bounds__(256) k_pair(V* __restrict__ s, uint64_t npairs
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   const uint64_t bit = uint64_t(1) << k;
   if constexpr (std::is_same<V, double2>::value) {
+    if constexpr (KIND == K1_ANTI) {  // X, Y and their sign variants: a permutation
+      const int p1 = unit_power(m.m1), p2 = unit_power(m.m2);
+      if ((p1 | p2) >= 0) {
+        for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < npairs;
+             i += stride) {
+          const uint64_t i0 = insert0(i, k), i1 = i0 | bit;
+          const double2 a0 = s[i0], a1 = s[i1];
+          s[i0] = unit_mul(p1, a1);
+          s[i1] = unit_mul(p2, a0);
+        }
+        return;
+      }
+    }
     const SoftM1 f = soft_matrix<KIND>(m.m0, m.m1, m.m2, m.m3);
     if (f.ok) {
       for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < npairs; i += stride) {
@@ -149,6 +183,21 @@ __global__ void __launch_bounds__(256) k_ctrl(V* __restrict__ s, uint64_t count,
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   const uint64_t tbit = uint64_t(1) << target;
   if constexpr (std::is_same<V, double2>::value) {
+    if constexpr (KIND == K1_ANTI) {  // controlled X, Y and sign variants: a permutation
+      const int p1 = unit_power(m.m1), p2 = unit_power(m.m2);
+      if ((p1 | p2) >= 0) {
+        for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count;
+             i += stride) {
+          uint64_t j = i;
+          for (int q = 0; q < pos.np; ++q) j = insert0(j, pos.p[q]);
+          const uint64_t i0 = j | ctrl_mask, i1 = i0 | tbit;
+          const double2 a0 = s[i0], a1 = s[i1];
+          s[i0] = unit_mul(p1, a1);
+          s[i1] = unit_mul(p2, a0);
+        }
+        return;
+      }
+    }
     const SoftM1 f = soft_matrix<KIND>(m.m0, m.m1, m.m2, m.m3);
     if (f.ok) {
       for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < count; i += stride) {
