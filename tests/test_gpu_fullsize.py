@@ -106,3 +106,20 @@ def test_ghz_shots_and_collapse_30q(gpu):
         assert bits[0] == bits[1]
         want = full if bits[0] else 0
         assert abs(ex.state().probability(want) - 1.0) < 1e-6
+
+
+def test_ghz_pauli_expectations_30q(gpu):
+    """GHZ(30) = (|0...0> + |1...1>)/sqrt 2 in complex64: <Z^30> = <Z0 Z29> =
+    <X^30> = 1 and <Z0> = <X0 X2> = 0, whatever the size.  One call covers the
+    Z-only pass, a shared X mask on the top qubit and an X mask inside the
+    low three qubits.  The amplitudes are fl32(1/sqrt 2), whose doubled square
+    is 1 - 6e-8: the bar is 1e-6 for the unit values, 1e-12 for the zeros
+    (the two contributions cancel exactly)."""
+    st = State.zero(N30, "complex64")
+    CudaStateVectorBackend.run_into(st, algorithms.ghz(N30), 0, mode="tiled")
+    strings = ["+" + "Z" * N30, "+Z" + "I" * (N30 - 1), "+Z" + "I" * (N30 - 2) + "Z",
+               "+" + "X" * N30, "-" + "X" * N30, "+XIX" + "I" * (N30 - 3)]
+    got = st.pauli_expectation(strings)
+    want = [1.0, 0.0, 1.0, 1.0, -1.0, 0.0]
+    for s, g, w in zip(strings, got, want):
+        assert abs(g - w) < (1e-6 if w else 1e-12), (s[:6], g, w)
