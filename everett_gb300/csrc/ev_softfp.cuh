@@ -84,14 +84,13 @@ EV_SOFT_FN uint32_t mul_128(uint64_t a, uint64_t b, uint64_t* hi) {
 }
 
 // An operand unpacked once and used in several products: the significand
-// with its leading 1 at bit 63, the sign bit (bit 31), and the biased
-// exponent minus 512 in the exponent field's place (bits 20..30), so that the
-// sum of two such fields plus the normalisation bit is the product's biased
-// exponent minus one, in place.
+// with its leading 1 at bit 63, and the word holding the sign bit (bit 31)
+// and the biased exponent minus 512 in the exponent field's place (bits
+// 20..30).  Adding two such words adds the exponents and, as the exponent
+// sum stays below 2^11, leaves the xor of the signs in bit 31.
 struct Unpacked {
   uint64_t sig;
   uint32_t ex;
-  uint32_t sg;
   uint32_t ok;  // normal, biased exponent in [512, 1534]
 };
 
@@ -100,9 +99,10 @@ EV_SOFT_FN Unpacked unpack(double x) {
   const uint32_t w = (uint32_t)(u >> 32);
   Unpacked r;
   r.sig = (u << 11) | (1ull << 63);
-  r.ex = (w & 0x7FF00000u) - (512u << 20);  // wraps outside the domain
-  r.sg = w & 0x80000000u;
-  r.ok = r.ex <= (1022u << 20);
+  // An exponent below 512 wraps the field to [1536, 2047]; one above 1534
+  // leaves it in [1023, 1535]; the sign bit is not borrowed from in range.
+  r.ex = (w & 0xFFF00000u) - (512u << 20);
+  r.ok = (r.ex & 0x7FFFFFFFu) <= (1022u << 20);
   return r;
 }
 
@@ -122,10 +122,10 @@ EV_SOFT_FN double mul(const Unpacked& a, const Unpacked& b) {
   const uint64_t h = hi | (uint64_t)(sticky != 0);
   const uint32_t lsb = ((uint32_t)h >> sh) & 1u;
   const uint64_t m = (h + ((1ull << (sh - 1)) - 1u + lsb)) >> sh;  // in [2^52, 2^53]
-  // Sign, and the biased exponent minus one in place (in [0, 2045]): adding
-  // the significand with its leading 1 at bit 52 completes the exponent, and
-  // a significand that rounded up to 2^53 carries into it.
-  const uint32_t word = (a.sg ^ b.sg) | (a.ex + b.ex + (top << 20));
+  // Sign (bit 31) and the biased exponent minus one in place (in [0, 2045]):
+  // adding the significand with its leading 1 at bit 52 completes the
+  // exponent, and a significand that rounded up to 2^53 carries into it.
+  const uint32_t word = a.ex + b.ex + (top << 20);
   return from_bits(((uint64_t)word << 32) + m);
 }
 

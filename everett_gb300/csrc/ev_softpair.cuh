@@ -63,6 +63,21 @@ __device__ __forceinline__ SoftM1 soft_matrix(double2 m0, double2 m1, double2 m2
   return f;
 }
 
+// The same factors for a matrix m (interleaved [re, im], row-major 2x2) of
+// kind k1, formed once on the host for records whose matrices travel with
+// them; the return value is SoftM1::ok.
+__host__ __device__ inline uint32_t soft_factors(int k1, const double* m, softfp::Unpacked u[4]) {
+  const int part = k1 == K1_REAL ? 0 : 1;
+  for (int j = 0; j < 4; ++j) u[j] = softfp::unpack(m[2 * j + part]);
+  switch (k1) {
+    case K1_DIAG: return u[0].ok & u[3].ok;
+    case K1_PHASE: return u[3].ok;
+    case K1_REAL:
+    case K1_DENSE: return u[0].ok & u[1].ok & u[2].ok & u[3].ok;
+    default: return 0;
+  }
+}
+
 // new0 = m0*a0 + m1*a1, new1 = m2*a0 + m3*a1 for a record of kind K1 (REAL,
 // DENSE, DIAG or PHASE; PHASE reads and writes a1 only), with the products
 // of new0 (both == false) or of both outputs on the integer pipes.

@@ -38,6 +38,14 @@ static SoftLevels tile_soft_levels() {
   return SoftLevels{e[0] - '0', e[1] - '0'};
 }
 
+// Chained application of records (TileOp::run): EV_TILE_CHAIN=0 applies
+// every record on its own, 1 forms pair chains only, 2 (default) pair and
+// quad chains; all give the same results.
+static int tile_chain_level() {
+  const char* e = getenv("EV_TILE_CHAIN");
+  return (e == nullptr || e[0] < '0' || e[0] > '2') ? 2 : e[0] - '0';
+}
+
 // One persistent block per resident slot; tiles strided over the grid.  The
 // pass's op records and index tables are staged in shared memory once per
 // block: [tile 2^k amplitudes][row offsets 2^(k-L)][op records][comp qubits].
@@ -80,11 +88,19 @@ __global__ void __launch_bounds__(kTileThreads, 2)
     for (uint32_t l = threadIdx.x; l < size; l += blockDim.x)
       tile[l] = s[base | offs[l >> L] | (l & lowmask)];
     __syncthreads();
-    for (int o = 0; o < nops; ++o) {
+    for (int o = 0; o < nops;) {
       const TileOp& op = ops[o];
-      if ((base & op.emask) != op.emask) continue;  // uniform across the block
-      apply_tile_op(tile, k, op, op.m);
-      __syncthreads();
+      const int run = op.run > 1 ? op.run : 1;
+      if ((base & op.emask) == op.emask) {  // uniform across the block
+        if (run > 1 && op.hi != 0)
+          tile_quad_chain(tile, size, ops + o, run);
+        else if (run > 1)
+          tile_chain(tile, size >> op.nins, ops + o, run);
+        else
+          apply_tile_op(tile, k, op, op.m);
+        __syncthreads();
+      }
+      o += run;
     }
 #pragma unroll 4
     for (uint32_t l = threadIdx.x; l < size; l += blockDim.x)
@@ -132,6 +148,7 @@ int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, 
       plan_passes(c, first, last, n, k, L, uint64_t(kMaxPassOps), s->dtype == EV_C64);
   const uint64_t ntiles = uint64_t(1) << (n - k);
   const SoftLevels soft = tile_soft_levels();
+  const int chains = tile_chain_level();
   std::vector<TileOp> ops;
   for (const Pass& p : passes) {
     TilePlan plan{};
@@ -154,6 +171,7 @@ int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, 
       if (s->dtype == EV_C128 && ops[j].kind == T_1Q)
         ops[j].soft = uint8_t(ops[j].k1 == K1_REAL ? soft.real : soft.other);
     }
+    if (chains) mark_chains(ops.data(), ops.size(), chains == 2);
     SegStep st;
     st.fused = 0;
     st.off0 = blob->add(&plan, sizeof(plan));

@@ -38,12 +38,18 @@ struct __align__(16) TileOp {
                    // (ev_softfp.cuh): 0 none, 1 first amplitude of each
                    // pair, 2 both
   uint32_t lmask;  // local control mask
-  uint32_t pad2;
+  uint8_t run;     // records from this one on that form a chain (T_1Q
+                   // records on the same target with the same controls,
+                   // applied pair by pair in registers); 0 or 1: none
+  uint8_t sok;     // complex128 T_1Q: the factors in m[8..15] are in the
+                   // integer-pipe product's domain (SoftM1::ok)
+  uint8_t pad2[2];
   uint64_t emask;  // controls outside the tile (global bit mask)
   uint64_t ins;    // T_1Q: sorted local positions of (local controls + target),
                    // 4 bits each, lowest position in the low nibble
   uint64_t pad3[2];
-  double m[32];
+  double m[32];    // T_1Q: the 2x2 matrix in m[0..7], then its product
+                   // factors unpacked (4 softfp::Unpacked, soft_factors)
 };
 
 static_assert(sizeof(TileOp) % 16 == 0, "op records are staged with 16-byte copies");
@@ -184,6 +190,142 @@ __device__ __forceinline__ void tile_2q(V* t, uint32_t count, const Op& op, cons
   }
 }
 
+// One 1-qubit record on one pair in registers, with the arithmetic of
+// tile_1q_fp64 (FP64 or FP32 pipe).
+template <int K1, typename V>
+__device__ __forceinline__ void pair_fp(const double* mm, V& a0, V& a1) {
+  using R = typename Real<V>::T;
+  if constexpr (K1 == K1_DENSE) {
+    const V m0 = ldm<V>(mm, 0), m1 = ldm<V>(mm, 1), m2 = ldm<V>(mm, 2), m3 = ldm<V>(mm, 3);
+    const V n0 = cadd(cmul(m0, a0), cmul(m1, a1));
+    a1 = cadd(cmul(m2, a0), cmul(m3, a1));
+    a0 = n0;
+  } else if constexpr (K1 == K1_REAL) {
+    const R r0 = R(mm[0]), r1 = R(mm[2]), r2 = R(mm[4]), r3 = R(mm[6]);
+    const V n0 = cadd(rmul(r0, a0), rmul(r1, a1));
+    a1 = cadd(rmul(r2, a0), rmul(r3, a1));
+    a0 = n0;
+  } else if constexpr (K1 == K1_DIAG) {
+    a0 = cmul(ldm<V>(mm, 0), a0);
+    a1 = cmul(ldm<V>(mm, 3), a1);
+  } else if constexpr (K1 == K1_PHASE) {
+    a1 = cmul(ldm<V>(mm, 3), a1);
+  } else if constexpr (K1 == K1_ANTI) {
+    const V n0 = cmul(ldm<V>(mm, 1), a1);
+    a1 = cmul(ldm<V>(mm, 2), a0);
+    a0 = n0;
+  }
+}
+
+// One record of a chain on two pairs held in registers: complex128 records
+// with their factors in range take the integer-pipe products, the rest the
+// plain arithmetic.  The two pairs are updated one after the other: a
+// straight-line block over both needs more registers than a 64-register
+// thread has, and its spills cost more than its extra overlap gains.
+template <int K1, typename V, typename Op>
+__device__ __forceinline__ void chain_rec(const Op& op, V& a0, V& a1, V& b0, V& b1) {
+  const double* mm = op.m;
+  if constexpr (std::is_same<V, double2>::value && K1 != K1_ANTI && K1 != K1_IDENT) {
+    if (op.soft && op.sok) {  // uniform across the block
+      SoftM1 f;
+      f.m0 = ldm<double2>(mm, 0);
+      f.m1 = ldm<double2>(mm, 1);
+      f.m2 = ldm<double2>(mm, 2);
+      f.m3 = ldm<double2>(mm, 3);
+      const softfp::Unpacked* u = reinterpret_cast<const softfp::Unpacked*>(mm + 8);
+      f.u0 = u[0];
+      f.u1 = u[1];
+      f.u2 = u[2];
+      f.u3 = u[3];
+      f.ok = 1;
+      const bool both = op.soft == 2;
+      soft_pair<K1>(a0, a1, f, both);
+      soft_pair<K1>(b0, b1, f, both);
+      return;
+    }
+  }
+  pair_fp<K1>(mm, a0, a1);
+  pair_fp<K1>(mm, b0, b1);
+}
+
+template <typename V, typename Op>
+__device__ __forceinline__ void chain_rec_any(const Op& op, V& a0, V& a1, V& b0, V& b1);
+
+// A chain of `run` 1-qubit records that share their target and controls:
+// each thread loads two pairs, applies every record of the chain to them in
+// circuit order and stores them once.  Every amplitude sees the same
+// operations in the same order as record-by-record application.
+template <typename V, typename Op>
+__device__ void tile_chain(V* t, uint32_t count, const Op* ops, int run) {
+  const Op& op0 = ops[0];
+  const uint32_t tbit = 1u << op0.p0, lmask = op0.lmask;
+  const int nins = op0.nins;
+  const uint64_t ins = op0.ins;
+  const int ins_first = int(ins & 15);
+  const uint32_t stride = blockDim.x;
+  for (uint32_t i = threadIdx.x; i < count; i += 2 * stride) {
+    const uint32_t i2 = i + stride;
+    const bool two = i2 < count;
+    uint32_t ja = ins0(i, ins_first), jb = ins0(two ? i2 : i, ins_first);
+    for (int q = 1; q < nins; ++q) {
+      const int p = int((ins >> (4 * q)) & 15);
+      ja = ins0(ja, p);
+      jb = ins0(jb, p);
+    }
+    ja |= lmask;
+    jb |= lmask;
+    V a0 = t[ja], a1 = t[ja | tbit], b0 = t[jb], b1 = t[jb | tbit];
+    for (int r = 0; r < run; ++r) chain_rec_any(ops[r], a0, a1, b0, b1);
+    t[ja] = a0;
+    t[ja | tbit] = a1;
+    if (two) {
+      t[jb] = b0;
+      t[jb | tbit] = b1;
+    }
+  }
+}
+
+// chain_rec for the record's kind.
+template <typename V, typename Op>
+__device__ __forceinline__ void chain_rec_any(const Op& op, V& a0, V& a1, V& b0, V& b1) {
+  switch (op.k1) {
+    case K1_DENSE: chain_rec<K1_DENSE>(op, a0, a1, b0, b1); break;
+    case K1_REAL: chain_rec<K1_REAL>(op, a0, a1, b0, b1); break;
+    case K1_DIAG: chain_rec<K1_DIAG>(op, a0, a1, b0, b1); break;
+    case K1_PHASE: chain_rec<K1_PHASE>(op, a0, a1, b0, b1); break;
+    case K1_ANTI: chain_rec<K1_ANTI>(op, a0, a1, b0, b1); break;
+    default: break;  // identity
+  }
+}
+
+// A chain of `run` uncontrolled 1-qubit records whose targets are two local
+// positions lo < hi (TileOp::lo/hi of the first record): each thread holds
+// the four amplitudes of a quad in registers; a record on lo updates the
+// pairs (q0, q1) and (q2, q3), one on hi the pairs (q0, q2) and (q1, q3).
+// The pairs of a record are disjoint and each amplitude sees its records in
+// circuit order, so the results equal record-by-record application.
+template <typename V, typename Op>
+__device__ void tile_quad_chain(V* t, uint32_t size, const Op* ops, int run) {
+  const int lo = ops[0].lo, hi = ops[0].hi;
+  const uint32_t lob = 1u << lo, hib = 1u << hi;
+  const uint32_t count = size >> 2;
+  for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
+    const uint32_t base = ins0(ins0(i, lo), hi);
+    V q0 = t[base], q1 = t[base | lob], q2 = t[base | hib], q3 = t[base | lob | hib];
+    for (int r = 0; r < run; ++r) {
+      const Op& op = ops[r];
+      if (op.p0 == lo)
+        chain_rec_any(op, q0, q1, q2, q3);
+      else
+        chain_rec_any(op, q0, q2, q1, q3);
+    }
+    t[base] = q0;
+    t[base | lob] = q1;
+    t[base | hib] = q2;
+    t[base | lob | hib] = q3;
+  }
+}
+
 template <typename V, typename Op>
 __device__ void apply_tile_op(V* t, int k, const Op& op, const double* mm) {
   const uint32_t size = 1u << k;
@@ -310,6 +452,7 @@ inline void encode_op(const ev_circuit* c, const ev_op& op, uint64_t tset, const
   }
   out->kind = T_1Q;
   out->k1 = uint8_t(classify1(op.m));
+  out->sok = uint8_t(soft_factors(out->k1, op.m, reinterpret_cast<softfp::Unpacked*>(out->m + 8)));
   out->p0 = uint8_t(local[op.q0]);
   uint32_t lmask = 0;
   uint64_t emask = 0;
@@ -330,6 +473,41 @@ inline void encode_op(const ev_circuit* c, const ev_op& op, uint64_t tset, const
     if ((all >> p) & 1) packed |= uint64_t(p) << (4 * ni++);
   out->ins = packed;
   out->nins = uint8_t(ni);
+}
+
+// Marks the chains of a pass's records (TileOp::run).  A run of
+// consecutive uncontrolled 1-qubit records with the same outside controls
+// whose targets are two local positions becomes a quad chain (lo/hi set on
+// its first record); a run on one target with the same controls becomes a
+// pair chain.
+inline void mark_chains(TileOp* ops, size_t nops, bool quads = true) {
+  for (size_t j = 0; j < nops;) {
+    TileOp& h = ops[j];
+    size_t e = j + 1;
+    int t2 = -1;
+    if (h.kind == T_1Q && h.lmask == 0 && quads) {
+      while (e < nops && e - j < 255 && ops[e].kind == T_1Q && ops[e].lmask == 0 &&
+             ops[e].emask == h.emask) {
+        const int p = ops[e].p0;
+        if (p != h.p0 && p != t2) {
+          if (t2 >= 0) break;
+          t2 = p;
+        }
+        ++e;
+      }
+    } else if (h.kind == T_1Q) {
+      while (e < nops && e - j < 255 && ops[e].kind == T_1Q && ops[e].p0 == h.p0 &&
+             ops[e].lmask == h.lmask && ops[e].emask == h.emask)
+        ++e;
+    }
+    h.run = uint8_t(e - j);
+    if (t2 >= 0) {
+      h.lo = uint8_t(std::min<int>(h.p0, t2));
+      h.hi = uint8_t(std::max<int>(h.p0, t2));
+    }
+    for (size_t r = j + 1; r < e; ++r) ops[r].run = 0;
+    j = e;
+  }
 }
 
 }  // namespace ev

@@ -371,6 +371,36 @@ def test_tiled_integer_pipe_levels_bit_exact(gpu, monkeypatch, level):
     assert exact(CudaStateVectorBackend.run(rl, mode="tiled").state().amplitudes(), want), level
 
 
+@pytest.mark.parametrize("chain", ["0", "1", "2"])
+def test_tiled_chains_bit_exact(gpu, monkeypatch, chain):
+    """The tile pass applies runs of 1-qubit records in registers: runs on one
+    target with the same controls (pair chains) and uncontrolled runs over
+    two targets (quad chains).  Every chaining level (none, pair chains,
+    pair and quad chains) gives the oracle's bits, with every 1-qubit kind,
+    controls inside and outside the tile, and tiles of 4 to 12 qubits."""
+    monkeypatch.setenv("EV_TILE_CHAIN", chain)
+    rng = np.random.default_rng(31)
+    n = 13
+    c = Circuit(n)
+    for layer in range(5):
+        for q in range(n):
+            for _ in range(int(rng.integers(1, 4))):
+                c.gate1(GATES_1Q[int(rng.integers(0, len(GATES_1Q)))], q)
+            if rng.random() < 0.3:
+                ctrl = [(q + int(rng.integers(1, n))) % n]
+                for _ in range(int(rng.integers(1, 3))):
+                    c.controlled(ctrl, GATES_1Q[int(rng.integers(0, len(GATES_1Q)))], q)
+        for i in range(layer % 2, n - 1, 2):
+            c.cnot(i, i + 1)
+    want, _, _ = O.run_seeded(c, 0)
+    for tb in (4, 6, 9, 12):
+        got = CudaStateVectorBackend.run(c, mode="tiled", tile_bits=tb).state().amplitudes()
+        assert exact(got, want), (chain, tb)
+    rl = workloads.random_layers(16, 6, 9)
+    want, _, _ = O.run_seeded(rl, 0, parallel=True)
+    assert exact(CudaStateVectorBackend.run(rl, mode="tiled").state().amplitudes(), want), chain
+
+
 def test_gates_on_mixed_range_amplitudes_bit_exact(gpu):
     """The complex128 gate kernels form plain products on the integer pipes
     for operands in a normal range and fall back pair by pair otherwise: a
