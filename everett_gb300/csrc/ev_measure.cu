@@ -1441,32 +1441,117 @@ extern "C" int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* o
 // C++ runtime with its own device pool) that must not see a foreign
 // allocation or the device-wide synchronisation cudaMalloc/cudaFree imply.
 //
-// The array is 1024 reduction blocks x 4 partials plus 12 words
-// (4108 doubles, ~32 KiB); every GPU that loads the library holds it until
+// The array is 2048 reduction blocks x 4 partials plus 12 words
+// (8204 doubles, ~64 KiB); every GPU that loads the library holds it until
 // the process exits.  Host code must not pass the array's name to a kernel
-// (on the host it is only a stand-in, not a device address), so on the first
-// call on each device, with that device current, the entry point resolves the
-// address with cudaGetSymbolAddress and caches it; make that first call
-// before any stream capture.  All calls share the array and each overwrites
-// what the previous one left, so calls that overlap on the GPU (different
-// streams, no ordering between them) race; calls on one stream, or otherwise
-// ordered, are safe.
+// (on the host it is only a stand-in, not a device address), so the first
+// call in each CUDA context (the device's primary context, or a context the
+// caller made current with the driver API), with that context current,
+// resolves the address with cudaGetSymbolAddress and caches it under the
+// (device, context) pair; make that first call before any stream capture.
+// All calls share the array and each overwrites what the previous one left,
+// so calls that overlap on the GPU (different streams, no ordering between
+// them) race; calls on one stream, or otherwise ordered, are safe.  Each call
+// returns once its measurement has completed on the caller's stream.
 namespace {
 constexpr int kNoAllocBlocks = 2048;
 constexpr uint64_t kNoAllocMaxQubits = 40;
 __device__ __align__(256) double g_noalloc_scratch[kNoAllocBlocks * 4 + 12];
-std::mutex g_noalloc_mu;
-double* g_noalloc_addr[256] = {};
 
+struct NoAllocSlot {
+  int device;
+  void* context;
+  double* addr;
+};
+constexpr int kNoAllocSlots = 64;
+std::mutex g_noalloc_mu;
+NoAllocSlot g_noalloc_slot[kNoAllocSlots];
+int g_noalloc_used = 0;
+
+// Driver functions reached through the runtime (the library links no driver
+// library, so it still loads where no driver is installed).
+using CtxGetCurrentFn = int (*)(void**);
+using MemGetAddressRangeFn = int (*)(unsigned long long*, size_t*, unsigned long long);
+template <typename Fn>
+Fn driver_fn(const char* name) {
+  void* p = nullptr;
+  cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+  if (cudaGetDriverEntryPointByVersion(name, &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return reinterpret_cast<Fn>(p);
+}
+
+int current_context(void** ctx) {
+  static const CtxGetCurrentFn fn = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent");
+  if (!fn) return fail(EV_ERR_CUDA, "ev_measure_qubit_noalloc: cuCtxGetCurrent unavailable");
+  *ctx = nullptr;
+  if (fn(ctx) != 0) return fail(EV_ERR_CUDA, "ev_measure_qubit_noalloc: cuCtxGetCurrent failed");
+  return EV_OK;
+}
+
+// The scratch array's device address in the current context.
 int noalloc_scratch(int device, double** out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (device < 0 || device >= 256) return fail(EV_ERR_INVALID_ARGUMENT, "device %d out of range", device);
-  if (!g_noalloc_addr[device]) {
+  void* ctx = nullptr;
+  EV_TRY(current_context(&ctx));
+  if (ctx == nullptr) {
+    // No context is current on this thread yet: the runtime binds the
+    // device's primary context on its next call, this one.
     void* p = nullptr;
     EV_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_addr[device] = static_cast<double*>(p);
+    EV_TRY(current_context(&ctx));
   }
-  *out = g_noalloc_addr[device];
+  for (int i = 0; i < g_noalloc_used; ++i)
+    if (g_noalloc_slot[i].device == device && g_noalloc_slot[i].context == ctx) {
+      *out = g_noalloc_slot[i].addr;
+      return EV_OK;
+    }
+  if (g_noalloc_used == kNoAllocSlots)
+    return fail(EV_ERR_INVALID_ARGUMENT, "ev_measure_qubit_noalloc: more than %d contexts",
+                kNoAllocSlots);
+  void* p = nullptr;
+  EV_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  g_noalloc_slot[g_noalloc_used++] = NoAllocSlot{device, ctx, static_cast<double*>(p)};
+  *out = static_cast<double*>(p);
+  return EV_OK;
+}
+
+// Refuses, before any launch, a buffer the kernels could not use: not
+// 16-byte aligned (they move whole complex128 values), not device or managed
+// memory of the current device, or shorter than 2^n amplitudes.
+int check_caller_buffer(const double* amps, uint64_t n, int device) {
+  if (reinterpret_cast<uintptr_t>(amps) % 16 != 0)
+    return fail(EV_ERR_INVALID_ARGUMENT,
+                "ev_measure_qubit_noalloc: amplitude buffer is not 16-byte aligned");
+  cudaPointerAttributes attr{};
+  if (cudaPointerGetAttributes(&attr, amps) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return fail(EV_ERR_INVALID_ARGUMENT,
+                "ev_measure_qubit_noalloc: amplitude buffer is not CUDA memory");
+  }
+  if (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)
+    return fail(EV_ERR_INVALID_ARGUMENT,
+                "ev_measure_qubit_noalloc: amplitude buffer is not device memory");
+  if (attr.type == cudaMemoryTypeDevice && attr.device != device)
+    return fail(EV_ERR_INVALID_ARGUMENT,
+                "ev_measure_qubit_noalloc: amplitude buffer is on device %d, current is %d",
+                attr.device, device);
+  static const MemGetAddressRangeFn range = driver_fn<MemGetAddressRangeFn>("cuMemGetAddressRange");
+  unsigned long long base = 0;
+  size_t size = 0;
+  const unsigned long long at = reinterpret_cast<unsigned long long>(amps);
+  if (!range || range(&base, &size, at) != 0)
+    return fail(EV_ERR_INVALID_ARGUMENT,
+                "ev_measure_qubit_noalloc: cannot find the allocation of the amplitude buffer");
+  const unsigned long long need = (unsigned long long)(uint64_t(16) << n);
+  if (at < base || at - base > size || size - (at - base) < need)
+    return fail(EV_ERR_INVALID_ARGUMENT,
+                "ev_measure_qubit_noalloc: the allocation holds fewer than 2^%llu amplitudes "
+                "from the given address",
+                (unsigned long long)n);
   return EV_OK;
 }
 }  // namespace
@@ -1485,6 +1570,7 @@ extern "C" int ev_measure_qubit_noalloc(double* amps, uint64_t n, uint64_t k, do
   int device = 0, sms = 0;
   EV_CUDA(cudaGetDevice(&device));
   EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  EV_TRY(check_caller_buffer(amps, n, device));
   double* scratch = nullptr;
   EV_TRY(noalloc_scratch(device, &scratch));
   double* partials = scratch;

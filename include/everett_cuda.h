@@ -171,13 +171,15 @@ int ev_measure_qubit(ev_state* s, uint64_t k, double u, int32_t* outcome);
  * doubles), for callers that cannot call cudaMalloc: one whose device memory
  * is all handed out by its own allocator, or one that cannot accept the
  * device-wide synchronisation of an allocation.  It allocates nothing: its
- * scratch is a fixed ~32 KiB array in the library's device memory, held on
- * every GPU that loads the library until the process exits.  n <= 40
- * (EV_ERR_INVALID_ARGUMENT beyond).  stream may be NULL (legacy default
- * stream); the call returns after the measurement has completed.  The first
- * call on a device resolves the array's device address, so make it before
- * any stream capture.  Calls share the array: calls that overlap on the GPU
- * race, ordered calls do not. */
+ * scratch is a fixed ~64 KiB array (2048 reduction blocks) in the library's
+ * device memory, held on every GPU that loads the library until the process
+ * exits.  n <= 40 (EV_ERR_INVALID_ARGUMENT beyond).  The buffer must be
+ * 16-byte aligned device (or managed) memory of the current device holding
+ * 2^n amplitudes; anything else is EV_ERR_INVALID_ARGUMENT before any launch.
+ * stream may be NULL (legacy default stream); the call returns after the
+ * measurement has completed.  The first call in a CUDA context resolves the
+ * array's device address there, so make it before any stream capture.  Calls
+ * share the array: calls that overlap on the GPU race, ordered calls do not. */
 int ev_measure_qubit_noalloc(double* amps, uint64_t n, uint64_t k, double u,
                              void* stream, int32_t* outcome);
 

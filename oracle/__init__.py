@@ -54,6 +54,8 @@ def lib(parallel: bool = False) -> C.CDLL:
         "oracle_stab_run": ([P, U, P, P, P, P], C.c_int),
         "oracle_rng_u64": ([U, U, P], None),
         "oracle_rng_f64": ([U, U, P], None),
+        "oracle_rng_raw": ([P, U, P], None),
+        "oracle_rng_seed_words": ([U, P], None),
         "oracle_validate": ([P], C.c_int),
         "oracle_run_seeded": ([P, U, P, P], C.c_int),
         "oracle_apply_ops": ([P, U, U, P], None),
@@ -198,6 +200,21 @@ def rng_u64(seed: int, count: int) -> np.ndarray:
 def rng_f64(seed: int, count: int) -> np.ndarray:
     out = np.zeros(count, dtype=np.float64)
     lib().oracle_rng_f64(seed, count, out.ctypes.data)
+    return out
+
+
+def rng_raw(state, count: int) -> np.ndarray:
+    """xoshiro256++ outputs from a raw 4-word state (no seeding)."""
+    st = np.array(state, dtype=np.uint64)
+    out = np.zeros(count, dtype=np.uint64)
+    lib().oracle_rng_raw(st.ctypes.data, count, out.ctypes.data)
+    return out
+
+
+def rng_seed_words(seed: int) -> np.ndarray:
+    """The 4 state words Rng::seed_from_u64(seed) derives with SplitMix64."""
+    out = np.zeros(4, dtype=np.uint64)
+    lib().oracle_rng_seed_words(seed, out.ctypes.data)
     return out
 
 

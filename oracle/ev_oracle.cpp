@@ -86,6 +86,7 @@ const int kSwapRows[4] = {0, 2, 1, 3};
 // ---- Rng: xoshiro256++ seeded by SplitMix64 (src/rng.rs:18-58) -------------
 struct Rng {
   uint64_t s[4];
+  Rng(uint64_t s0, uint64_t s1, uint64_t s2, uint64_t s3) : s{s0, s1, s2, s3} {}
   explicit Rng(uint64_t seed) {
     for (int w = 0; w < 4; ++w) {
       seed += 0x9E3779B97F4A7C15ULL;
@@ -443,6 +444,17 @@ void oracle_rng_u64(uint64_t seed, uint64_t count, uint64_t* out) {
 void oracle_rng_f64(uint64_t seed, uint64_t count, double* out) {
   Rng r(seed);
   for (uint64_t j = 0; j < count; ++j) out[j] = r.next_f64();
+}
+// The generator step alone, from a raw state (no SplitMix64 seeding), and the
+// four seeding words seed_from_u64 derives: the two halves of the stream that
+// the tests pin to the algorithms' published output vectors.
+void oracle_rng_raw(const uint64_t* state, uint64_t count, uint64_t* out) {
+  Rng r(state[0], state[1], state[2], state[3]);
+  for (uint64_t j = 0; j < count; ++j) out[j] = r.next_u64();
+}
+void oracle_rng_seed_words(uint64_t seed, uint64_t* words) {
+  const Rng r(seed);
+  for (int w = 0; w < 4; ++w) words[w] = r.s[w];
 }
 
 // ---- circuits ----------------------------------------------------------------
