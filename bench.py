@@ -18,8 +18,13 @@ the circuit from |0...0>.
                 bandwidth (the pass is bound by the FP64 pipe instead; the
                 committed ncu summary gives its FP64 utilisation)
   cpu_baseline  the CPU oracle (the reference's scalar loops restated in
-                C++) on one host core over a bounded prefix of the same
-                circuit family at 24 qubits, same unit
+                C++) on one host core over the first ops of the same
+                30-qubit circuit, same unit
+  gate_bytes_pct_of_hbm_peak   value over the measured HBM copy bandwidth:
+                the gate-by-gate bytes the tile passes stand for, not traffic
+  hbm_traffic_pct_of_peak      the bytes HBM actually moves (the tile
+                passes' ncu DRAM traffic per launch x launches) per second,
+                over the same peak
 
 Additional measured sections (same run, rank 0): the complex64 fused
 tensor-core path on the same 30-qubit circuit (time, speed-up over
@@ -28,7 +33,8 @@ the 28-qubit Haar/CZ depth-40 circuit per fused arithmetic, the 4096-circuit
 TFIM batch, and the serving mix under Poisson arrivals.
 
 --impl reference times the same oracle with its independent loops split over
-every host core, each step a bounded prefix at 26 qubits.
+every host core on the same 30-qubit circuit, each step ~4 s of ops resuming
+where the previous step stopped.
 
 Under torchrun (N>1) every rank runs an independent replica on its own GPU
 (the path does not shard); value is the ranks' summed work over the slowest
@@ -37,6 +43,7 @@ rank's time.
 from __future__ import annotations
 
 import argparse
+import contextlib
 import ctypes as C
 import json
 import math
@@ -65,6 +72,8 @@ def parse_args():
     ap.add_argument("--mode", default="tiled", choices=["tiled", "exact"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-clocks", action="store_true",
+                    help="sample nvidia-smi clocks during the end-to-end steps too")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--kernel-reps", type=int, default=3,
                     help="timed calls per case for --case kernels (0: one untimed call each)")
@@ -186,51 +195,86 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_oracle_rate(n: int, depth: int, seconds: float, parallel: bool):
-    """GB/s of the CPU oracle over a prefix of the random-layer circuit."""
-    import numpy as np
+class OracleWindow:
+    """The CPU oracle (the reference's scalar loops restated in C++) walking
+    the random-layer circuit op by op on a host state; each step resumes where
+    the previous one stopped, from |0...0> again after the circuit's last op.
+    Only op application is timed."""
 
-    import oracle as O
-    from everett_gb300 import workloads
-    c = workloads.random_layers(n, depth, seed=1)
-    amps = np.zeros(1 << n, dtype=np.complex128)
-    amps[0] = 1
-    ops = c.ops()
-    done = 0
-    nbytes = 0
-    t0 = time.perf_counter()
-    while done < len(ops) and time.perf_counter() - t0 < seconds:
-        O.apply_ops(c, amps, done, done + 1, parallel=parallel)
-        nbytes += workloads.op_bytes(ops[done], n, 16)
-        done += 1
-    dt = time.perf_counter() - t0
-    return nbytes / dt / 1e9, done, dt
+    def __init__(self, n: int, depth: int, parallel: bool):
+        import numpy as np
+
+        from everett_gb300 import workloads
+        self.n, self.parallel = n, parallel
+        self.circuit = workloads.random_layers(n, depth, seed=1)
+        self.ops = self.circuit.ops()
+        self.amps = np.zeros(1 << n, dtype=np.complex128)
+        self.amps.fill(0)  # touch every page before any op is timed
+        self.amps[0] = 1
+        self.pos = 0
+
+    def step(self, seconds: float):
+        """Applies ops for about `seconds`; returns (GB/s, ops, seconds)."""
+        import oracle as O
+        from everett_gb300 import workloads
+        nbytes = done = 0
+        busy = 0.0
+        while busy < seconds:
+            if self.pos == len(self.ops):
+                self.amps[:] = 0
+                self.amps[0] = 1
+                self.pos = 0
+            t0 = time.perf_counter()
+            O.apply_ops(self.circuit, self.amps, self.pos, self.pos + 1, parallel=self.parallel)
+            busy += time.perf_counter() - t0
+            nbytes += workloads.op_bytes(self.ops[self.pos], self.n, 16)
+            self.pos += 1
+            done += 1
+        return nbytes / busy / 1e9, done, busy
+
+
+def workload_name(n: int, depth: int) -> str:
+    return f"random-layer circuit, {n} qubits, depth {depth}, complex128"
+
+
+def oracle_window(n: int, depth: int, parallel: bool):
+    """An OracleWindow at n qubits, or at 26 when the host cannot hold the
+    2^n-amplitude state (the fallback is named in the line)."""
+    try:
+        return OracleWindow(n, depth, parallel)
+    except MemoryError:
+        return OracleWindow(min(n, 26), depth, parallel)
 
 
 def run_reference(args, dist: Dist):
     if dist.rank != 0:
         return
     cores = os.cpu_count() or 1
-    n = min(args.qubits, 26)
-    steps = []
+    win = oracle_window(args.qubits, args.depth, parallel=True)
+    n = win.n
+    seconds = 4.0
+    timed = []
     for i in range(args.warmup + args.steps):
-        rate, ops_done, dt = cpu_oracle_rate(n, args.depth, 6.0, parallel=True)
+        res = win.step(seconds)
         if i >= args.warmup:
-            steps.append((rate, ops_done, dt))
-    rate = statistics.median(s[0] for s in steps)
-    ms = statistics.median(s[2] for s in steps) * 1000
+            timed.append(res)
+    gbytes = sum(r[0] * r[2] for r in timed)
+    busy = sum(r[2] for r in timed)
+    rate = gbytes / busy
+    ops = sum(r[1] for r in timed)
     line = {
         "impl": "reference", "metric": METRIC, "value": round(rate, 3), "unit": "GB/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": round(ms, 1), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random-layer circuit)",
-        "config": {"workload": f"random-layer circuit, {n} qubits (bounded prefix per step), "
-                               f"depth {args.depth}, complex128",
-                   "parallelism": "replicas only", "l2": "CPU run"},
+        "ms_per_step": round(1e3 * busy / len(timed), 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded random-layer circuit)",
+        "config": {"workload": workload_name(n, args.depth), "parallelism": "replicas only",
+                   "l2": "CPU run"},
         "cpu_baseline": {"value": round(rate, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-                         "sample": f"{steps[0][1]} ops of the {n}-qubit circuit per step, "
-                                   f"oracle restatement of the reference's scalar loops, "
-                                   f"OpenMP over independent pairs"},
+                         "sample": f"{ops} ops of the {n}-qubit circuit over {len(timed)} steps of "
+                                   f"~{seconds:.0f} s, each resuming where the last stopped; "
+                                   f"oracle restatement of the reference's scalar loops, OpenMP "
+                                   f"over independent pairs"},
         "e2e": {"value": round(rate, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -845,7 +889,10 @@ def run_ours(args, dist: Dist):
         cl = np.zeros(1, dtype=np.uint8)
         dist.barrier()
         run_s = dl_s = 0.0
-        with Clocks(gpu_index if dist.world == 1 else 0) as clk_e2e:
+        # no nvidia-smi sampler here: its queries slow the host link (a 16 GiB
+        # read-back measured 27-41 GB/s with it running, 136-190 GB/s without)
+        clk_e2e = Clocks(gpu_index if dist.world == 1 else 0) if args.e2e_clocks else None
+        with (clk_e2e if clk_e2e is not None else contextlib.nullcontext()):
             t0 = time.perf_counter()
             for _ in range(args.steps):
                 t1 = time.perf_counter()
@@ -861,8 +908,9 @@ def run_ours(args, dist: Dist):
                "unit": "GB/s", "h2d_bytes_per_step": int(ops.nbytes),
                "d2h_bytes_per_step": int(out_bytes),
                "ms_per_step_run": round(1e3 * run_s / args.steps, 1),
-               "ms_per_step_download": round(1e3 * dl_s / args.steps, 1),
-               "clocks": clk_e2e.summary()}
+               "ms_per_step_download": round(1e3 * dl_s / args.steps, 1)}
+        if clk_e2e is not None:
+            e2e["clocks"] = clk_e2e.summary()
 
     peak, peak_kind = measured_peaks()
     roofline = roofline_of(prof, "tile_pass", 2.0 * (1 << n) * 16, peak, peak_kind,
@@ -893,13 +941,22 @@ def run_ours(args, dist: Dist):
             f"{ncu_figure('k_tile_c128', 'fp64_pipe_pct')}%, fma-heavy pipe "
             f"{ncu_figure('k_tile_c128', 'fmaheavy_pipe_pct')}% busy")
 
+    # what HBM actually moves: the tile passes' measured DRAM traffic per
+    # launch (ncu) times the launches of a step, over the step's time
+    hbm_traffic_pct = None
+    if roofline is not None and roofline.get("traffic"):
+        per_step = roofline["traffic"] * roofline["launches"] / args.steps
+        hbm_traffic_pct = round(100 * per_step / (worst_ms / args.steps / 1e3) / 1e9 / peak, 2)
+
     cpu = None
     extras = {}
     if dist.rank == 0:
-        rate, ops_done, dt = cpu_oracle_rate(min(n, 24), depth, args.cpu_seconds, parallel=False)
+        win = oracle_window(n, depth, parallel=False)
+        rate, ops_done, dt = win.step(args.cpu_seconds)
         cpu = {"value": round(rate, 3), "unit": "GB/s", "cores": 1, "kind": "port",
-               "sample": f"first {ops_done} ops of the random-layer circuit at {min(n, 24)} "
+               "sample": f"first {ops_done} ops of the random-layer circuit at {win.n} "
                          f"qubits, {dt:.1f} s, scalar oracle (the reference's loops)"}
+        del win
         if not args.no_extras:
             c128_ms = worst_ms / args.steps
             for key, fn in (("complex128_fused_same_circuit",
@@ -929,13 +986,13 @@ def run_ours(args, dist: Dist):
             "ms_per_step": round(worst_ms / args.steps, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded random-layer circuit)",
-            "config": {"workload": f"random-layer circuit, {n} qubits, depth {depth}, "
-                                   f"complex128, {args.mode} mode",
+            "config": {"workload": workload_name(n, depth), "mode": args.mode,
                        "ops": len(circuit), "algorithmic_bytes_per_step": bytes_per_step,
                        "parallelism": "replicas only" if dist.world > 1 else "1 GPU",
                        "l2": f"inputs larger than L2 ({(1 << n) * 16 / 2**30:.1f} GiB state), "
                              f"no flush"},
-            "pct_hbm_peak": round(100 * value / peak, 1),
+            "gate_bytes_pct_of_hbm_peak": round(100 * value / peak, 1),
+            "hbm_traffic_pct_of_peak": hbm_traffic_pct,
             "amplitude_updates_per_s": float(f"{len(circuit) * (1 << n) / (worst_ms / args.steps / 1e3):.4g}"),
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "gpu_launches": int(lc1.value - lc0.value),

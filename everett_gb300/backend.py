@@ -202,7 +202,7 @@ class PreparedRun:
     exactly as after ``CudaStateVectorBackend.run_into`` with the same seed.
     """
 
-    def __init__(self, state: State, circuit: Circuit, mode="exact", tile_bits=0,
+    def __init__(self, state: State, circuit: Circuit, mode="tiled", tile_bits=0,
                  variant=None):
         c = circuit.ev_struct()
         opts = _options(state.dtype(), mode, tile_bits, variant)
@@ -262,7 +262,7 @@ class CudaStateVectorBackend:
         self._rng = Rng.seed_from_u64(seed)
 
     @classmethod
-    def run(cls, circuit: Circuit, dtype="complex128", mode="exact", tile_bits=0,
+    def run(cls, circuit: Circuit, dtype="complex128", mode="tiled", tile_bits=0,
             variant=None) -> Execution:
         """mode: "exact" (one kernel per op), "tiled" (runs of ops per
         shared-memory pass) or "fused" (dense k-qubit unitaries, k =
@@ -273,7 +273,7 @@ class CudaStateVectorBackend:
                               variant=variant)
 
     @classmethod
-    def run_seeded(cls, circuit: Circuit, seed: int, dtype="complex128", mode="exact",
+    def run_seeded(cls, circuit: Circuit, seed: int, dtype="complex128", mode="tiled",
                    tile_bits=0, variant=None) -> Execution:
         c = circuit.ev_struct()
         opts = _options(dtype, mode, tile_bits, variant)
@@ -285,7 +285,7 @@ class CudaStateVectorBackend:
         return Execution(State(h.value), [bool(b) for b in classical[:ncl]])
 
     @staticmethod
-    def run_into(state: State, circuit: Circuit, seed: int = 0, mode="exact",
+    def run_into(state: State, circuit: Circuit, seed: int = 0, mode="tiled",
                  tile_bits=0, variant=None) -> list:
         """Runs a circuit on an existing state (reset to |0...0> first)."""
         c = circuit.ev_struct()
@@ -297,7 +297,7 @@ class CudaStateVectorBackend:
         return [bool(b) for b in classical[:ncl]]
 
     @staticmethod
-    def drive(state: State, circuit: Circuit, seed: int = 0, mode="exact",
+    def drive(state: State, circuit: Circuit, seed: int = 0, mode="tiled",
               tile_bits=0, variant=None) -> list:
         """Applies a circuit's ops to the state as it stands (drive,
         backend/mod.rs:43-72); returns the classical register."""
@@ -310,7 +310,7 @@ class CudaStateVectorBackend:
         return [bool(b) for b in classical[:ncl]]
 
     @staticmethod
-    def prepare(state: State, circuit: Circuit, mode="exact", tile_bits=0,
+    def prepare(state: State, circuit: Circuit, mode="tiled", tile_bits=0,
                 variant=None) -> PreparedRun:
         """Plans a circuit for a state once and records it as a CUDA graph;
         each ``launch(seed)`` of the result equals ``run_into`` with that

@@ -40,6 +40,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ev_bulk.cuh"
 #include "ev_device.cuh"
 #include "ev_internal.h"
 #include "ev_ozaki.cuh"
@@ -289,10 +290,6 @@ __global__ void __launch_bounds__(256)
 
 // ---- tcgen05 kernel ------------------------------------------------------------
 
-__device__ __forceinline__ uint32_t smem_addr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups
 // 1024 bytes apart.
 __device__ __forceinline__ uint64_t sw128_desc(uint32_t addr) {
@@ -329,21 +326,6 @@ __device__ __forceinline__ void mma_issue(uint32_t dtmem, uint64_t a, uint64_t b
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(dtmem),
         "l"(a), "l"(b), "r"(idesc), "r"(acc));
   }
-}
-
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, uint32_t limit) {
-  const uint32_t a = smem_addr(bar);
-  for (uint32_t it = 0; it < limit; ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done)
-        : "r"(a), "r"(phase)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
 }
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t v[16]) {
@@ -608,26 +590,6 @@ __global__ void __launch_bounds__(kTcThreads)
 // to HBM with bulk stores, waits until they have read it, and refills it
 // with a later step.  On a wait that gives up, the kernel records the error,
 // drains its outstanding copies (bounded), frees TMEM and returns.
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
-               "r"(bytes)
-               : "memory");
-}
-
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-
-__device__ __forceinline__ void bulk_s2g(void* dst, const void* src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst),
-               "r"(smem_addr(src)), "r"(bytes)
-               : "memory");
-}
 
 template <int KB, int VAR, int STAGES>
 struct TmaShape {

@@ -17,6 +17,7 @@
 // it, and a control inside T becomes a local mask.
 #include <cstdlib>
 
+#include "ev_bulk.cuh"
 #include "ev_tile.cuh"
 
 namespace ev {
@@ -46,18 +47,42 @@ static int tile_chain_level() {
   return (e == nullptr || e[0] < '0' || e[0] > '2') ? 2 : e[0] - '0';
 }
 
+// How tiles move between HBM and shared memory.  By default every thread
+// loads and stores its share of the tile with 16-byte accesses.  With
+// EV_TILE_STAGING=tma the bulk-copy (TMA) engine moves them instead: a tile
+// is 2^(k-L) contiguous rows of 2^L amplitudes, warp 0 issues one
+// cp.async.bulk per row, loads complete on an mbarrier and stores are drained
+// (their reads of the tile) before the next tile's loads; rows shorter than
+// 16 bytes (registers of fewer than 2 qubits) keep the plain path.  Both give
+// the same results.  The TMA form measured slower on the complex128 pass
+// (28 qubits: 2585 vs 2378 ms per depth-20 circuit): the pass is bound by
+// its arithmetic, the 256-byte rows issue serially from one warp while the
+// block waits, and the extra live state costs the 64-register threads spills.
+static bool tile_bulk_enabled() {
+  const char* e = getenv("EV_TILE_STAGING");
+  return e != nullptr && e[0] == 't';
+}
+
+constexpr uint32_t kTileWaitLimit = 1u << 24;  // try_wait polls before giving up
+
 // One persistent block per resident slot; tiles strided over the grid.  The
 // pass's op records and index tables are staged in shared memory once per
 // block: [tile 2^k amplitudes][row offsets 2^(k-L)][op records][comp qubits].
+// A load that never completes sets *err (the run's device flag, reported as
+// EV_ERR_TIMEOUT) and ends the block after a bounded drain.
 template <typename V>
 __global__ void __launch_bounds__(kTileThreads, 2)
     k_tile(V* __restrict__ s, uint64_t ntiles, const TilePlan* __restrict__ gplan,
-           const TileOp* __restrict__ gops, int nops, const uint8_t* pred) {
+           const TileOp* __restrict__ gops, int nops, const uint8_t* pred, int bulk, int* err) {
   if (pred != nullptr && *pred == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bar;
   const int k = gplan->k, L = gplan->L, nH = gplan->nH, ncomp = gplan->ncomp;
   const uint32_t size = 1u << k;
   const uint32_t nrows = 1u << (k - L);
+  const uint32_t rowbytes = uint32_t(sizeof(V)) << L;
+  const bool use_bulk = bulk != 0 && rowbytes % 16 == 0;  // uniform across the block
+  const int warp = int(threadIdx.x >> 5), lane = int(threadIdx.x & 31);
   V* tile = reinterpret_cast<V*>(smem_raw);
   uint64_t* offs = reinterpret_cast<uint64_t*>(smem_raw + sizeof(V) * size);
   // op records start on a 16-byte boundary (they are staged with 16-byte
@@ -65,6 +90,10 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   const size_t ops_at = (sizeof(V) * size + sizeof(uint64_t) * nrows + 15) & ~size_t(15);
   TileOp* ops = reinterpret_cast<TileOp*>(smem_raw + ops_at);
   uint8_t* comp = reinterpret_cast<uint8_t*>(ops + nops);
+  if (use_bulk && threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
   {
     const uint4* src = reinterpret_cast<const uint4*>(gops);
     uint4* dst = reinterpret_cast<uint4*>(ops);
@@ -79,15 +108,36 @@ __global__ void __launch_bounds__(kTileThreads, 2)
     offs[h] = o;
   }
   const uint32_t lowmask = (1u << L) - 1;
+  uint32_t phase = 0;
   __syncthreads();
   for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     uint64_t base = 0;
     for (int b = 0; b < ncomp; ++b)
       if ((t >> b) & 1) base |= uint64_t(1) << comp[b];
+    if (use_bulk) {
+      if (warp == 0) {
+        if (lane == 0) {
+          fence_proxy_async_smem();
+          mbar_expect_tx(&bar, rowbytes * nrows);
+        }
+        __syncwarp();
+        for (uint32_t h = uint32_t(lane); h < nrows; h += 32)
+          bulk_g2s(tile + (size_t(h) << L), s + (base | offs[h]), rowbytes, &bar);
+      }
+      const bool ok = mbar_wait(&bar, phase, kTileWaitLimit);
+      if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0) atomicExch(err, 1);
+        mbar_wait(&bar, phase, kTileWaitLimit);  // drain the loads in flight (bounded)
+        if (warp == 0) bulk_wait_all();          // and the last tile's stores
+        return;
+      }
+      phase ^= 1;
+    } else {
 #pragma unroll 4
-    for (uint32_t l = threadIdx.x; l < size; l += blockDim.x)
-      tile[l] = s[base | offs[l >> L] | (l & lowmask)];
-    __syncthreads();
+      for (uint32_t l = threadIdx.x; l < size; l += blockDim.x)
+        tile[l] = s[base | offs[l >> L] | (l & lowmask)];
+      __syncthreads();
+    }
     for (int o = 0; o < nops;) {
       const TileOp& op = ops[o];
       const int run = op.run > 1 ? op.run : 1;
@@ -102,11 +152,23 @@ __global__ void __launch_bounds__(kTileThreads, 2)
       }
       o += run;
     }
+    if (use_bulk) {
+      fence_proxy_async_smem();
+      __syncthreads();
+      if (warp == 0) {
+        for (uint32_t h = uint32_t(lane); h < nrows; h += 32)
+          bulk_s2g(s + (base | offs[h]), tile + (size_t(h) << L), rowbytes);
+        bulk_commit();
+        bulk_wait_read();
+      }
+    } else {
 #pragma unroll 4
-    for (uint32_t l = threadIdx.x; l < size; l += blockDim.x)
-      s[base | offs[l >> L] | (l & lowmask)] = tile[l];
+      for (uint32_t l = threadIdx.x; l < size; l += blockDim.x)
+        s[base | offs[l >> L] | (l & lowmask)] = tile[l];
+    }
     __syncthreads();
   }
+  if (use_bulk && warp == 0) bulk_wait_all();
 }
 
 template <typename V>
@@ -123,8 +185,10 @@ static int launch_tile(ev_state* s, uint64_t ntiles, const TilePlan& plan, const
   if (grid > ntiles) grid = ntiles;
   ProfScope prof(s, P_TILE, 2.0 * double(s->len()) * double(sizeof(V)));
   s->launches += 1;
+  static const int bulk = tile_bulk_enabled() ? 1 : 0;
+  int* derr = reinterpret_cast<int*>(s->scratch.counter + 1);
   k_tile<V><<<unsigned(grid), kTileThreads, smem, s->stream>>>(static_cast<V*>(s->amps), ntiles,
-                                                               dplan, dops, nops, pred);
+                                                               dplan, dops, nops, pred, bulk, derr);
   EV_CUDA(cudaGetLastError());
   return EV_OK;
 }

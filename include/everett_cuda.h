@@ -210,7 +210,8 @@ int ev_validate(const ev_circuit* c);
  * measurement Rng (xoshiro256++ via SplitMix64, src/rng.rs:18-58) and walk
  * the ops.  On success *state_out is a new device-resident state owned by
  * the caller and classical_out[0..num_classical) holds the register
- * (0/1 bytes).  opts may be NULL (complex128, exact mode). */
+ * (0/1 bytes).  opts may be NULL (complex128, tiled mode: bit-identical to
+ * the exact mode and faster). */
 int ev_run_seeded(const ev_circuit* c, uint64_t seed, const ev_run_options* opts,
                   ev_state** state_out, uint8_t* classical_out);
 

@@ -11,8 +11,9 @@
 // tests (kernel.rs:515-770, measure.rs:59-106, state.rs:192-234,
 // tests/algorithms_*.rs, tests/properties.rs), re-expressed in
 // tests/test_oracle.py.  The xoshiro256++ stream has no golden values in the
-// reference (rng.rs:62-95 tests only determinism, range and mean): that part
-// of parity is unpinned.
+// reference (rng.rs:62-95 tests only determinism, range and mean); the tests
+// pin it to the published output vectors of SplitMix64 and xoshiro256++
+// (oracle_rng_seed_words, oracle_rng_raw).
 //
 // Build: -O2 -ffp-contract=off (no implicit FMA contraction), with std::fma
 // wherever the Rust source calls mul_add, so every rounding step matches the

@@ -108,7 +108,7 @@ def test_prepared_counts_launches(gpu):
     n = 12
     st = State.zero(n)
     c = workloads.random_layers(n, 3, 1)
-    prep = PreparedRun(st, c)
+    prep = PreparedRun(st, c, mode="exact")
     k = prep.kernels()
     before = C_launches(st)
     prep.launch(0)
@@ -116,6 +116,8 @@ def test_prepared_counts_launches(gpu):
     assert C_launches(st) - before == 2 * k
     # exact mode: one kernel per gate plus the reset
     assert k >= len(c)
+    # the default (tiled) mode: one kernel per tile pass
+    assert PreparedRun(st, c).kernels() < len(c) // 4
 
 
 def C_launches(st):
