@@ -23,6 +23,15 @@
 // Per-amplitude arithmetic is the tile pass's (ev_tile.cuh), so a batched
 // circuit's state equals the single-circuit tiled run bit for bit, and its
 // shots are drawn exactly as ev_sample draws them (same tree, same uniforms).
+//
+// Circuits with mid-circuit measurement and classical control
+// (backend/mod.rs:51-72) run as BI_WHOLE items: the CTA walks the ops in
+// order with the classical register in shared memory; an IfClassic prefix
+// gates the op after it; a measurement sums p1 over the tile with a fixed
+// block tree, draws its uniform from the circuit's own Rng
+// (Rng::seed_from_u64(run_seed), one uniform per executed measurement, as
+// measure.rs:15-51 does), decides, collapses and renormalises in shared
+// memory.  Such circuits must fit one CTA (n <= the tile size).
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -55,7 +64,17 @@ struct BatchCirc {
   uint32_t plan0, pass0;
   uint64_t ntiles;
   uint64_t state, tree, uni, shots, shot_out, seed;
+  uint64_t run_seed;  // Rng of mid-circuit measurements
+  uint64_t cl;        // offset of the classical register in the results
+  uint32_t ncl;       // classical bits
+  uint32_t classical; // 1: the circuit measures or has classical control
 };
+
+// Batch-only op kinds (beside the tile kinds of ev_tile.cuh): a measurement
+// (p0 = qubit, lmask = classical bit) and an IfClassic prefix (lmask =
+// classical bit) that gates the next op.
+constexpr uint8_t B_MEAS = 200, B_IF = 201;
+constexpr int kBatchMaxClassical = 64;
 
 struct PassRef {
   uint32_t op0, nops;
@@ -82,6 +101,7 @@ struct BatchArgs {
   unsigned* head;
   unsigned* done;
   int* err;
+  uint8_t* cl;
 };
 
 constexpr uint32_t kSpinLimit = 1u << 25;  // x ~64 ns: a wait gives up after ~2 s
@@ -172,6 +192,54 @@ __device__ void finalize(const V* amps, bool global, const BatchCirc& c, uint32_
   }
 }
 
+// Rescaling by the f64 factor of a measurement: complex128 in f64
+// (Complex64 * f64, complex.rs:127-133); complex64 as a float pair in one FMA
+// per component, as the single-state collapse does.
+template <typename V>
+__device__ __forceinline__ V batch_scale(V a, double s) {
+  if constexpr (sizeof(V) == 16) {
+    return make_double2(__dmul_rn(a.x, s), __dmul_rn(a.y, s));
+  } else {
+    const float sh = float(s);
+    const float sl = float(s - double(sh));
+    return make_float2(__fmaf_rn(a.x, sh, __fmul_rn(a.x, sl)), __fmaf_rn(a.y, sh, __fmul_rn(a.y, sl)));
+  }
+}
+
+// measure_qubit (measure.rs:15-51) on a whole state in shared memory: p1 by
+// a fixed block tree, the outcome from the circuit's next uniform, then the
+// collapse and rescale.  rng holds the circuit's xoshiro256++ state.
+template <typename V>
+__device__ void batch_measure(V* tile, uint32_t size, int q, uint32_t cbit, double* red,
+                              uint8_t* cl, uint64_t* rng, double* meas) {
+  const int t = threadIdx.x, nb = blockDim.x;
+  const uint32_t bit = 1u << q;
+  double p1 = 0.0, unused = 0.0;
+  for (uint32_t j = t; j < size; j += nb)
+    if (j & bit) p1 += nsq(tile[j]);
+  block_sum2(red, p1, unused);
+  if (t == 0) {
+    DevRng r(0);
+    for (int w = 0; w < 4; ++w) r.s[w] = rng[w];
+    const double u = r.next_f64();
+    for (int w = 0; w < 4; ++w) rng[w] = r.s[w];
+    const bool outcome = u < p1;
+    const double surviving = outcome ? p1 : __dadd_rn(1.0, -p1);
+    meas[0] = surviving > 0.0 ? __ddiv_rn(1.0, __dsqrt_rn(surviving)) : 0.0;
+    meas[1] = outcome ? 1.0 : 0.0;
+    cl[cbit] = outcome ? 1 : 0;
+  }
+  __syncthreads();
+  const double scale = meas[0];
+  const bool one = meas[1] != 0.0;
+  V zero;
+  zero.x = 0;
+  zero.y = 0;
+  for (uint32_t j = t; j < size; j += nb)
+    tile[j] = (((j & bit) != 0) == one) ? batch_scale(tile[j], scale) : zero;
+  __syncthreads();
+}
+
 template <typename V>
 __global__ void __launch_bounds__(512, 2) k_batch(BatchArgs a, int kmax) {
   extern __shared__ __align__(16) unsigned char sm[];
@@ -181,6 +249,9 @@ __global__ void __launch_bounds__(512, 2) k_batch(BatchArgs a, int kmax) {
   __shared__ TilePlan plan;
   __shared__ unsigned s_item;
   __shared__ int s_ok;
+  __shared__ uint8_t s_cl[kBatchMaxClassical];
+  __shared__ uint64_t s_rng[4];
+  __shared__ double s_meas[2];
   const int t = threadIdx.x, nb = blockDim.x;
   for (;;) {
     if (t == 0) s_item = atomicAdd(a.head, 1u);
@@ -234,12 +305,34 @@ __global__ void __launch_bounds__(512, 2) k_batch(BatchArgs a, int kmax) {
     }
     __syncthreads();
     const PassRef pr = a.passes[c.pass0 + it.pass];
+    const bool classical = c.classical != 0;  // BI_WHOLE items only
+    if (classical) {
+      if (t < kBatchMaxClassical) s_cl[t] = 0;
+      if (t == 0) {
+        const DevRng r(c.run_seed);
+        for (int w = 0; w < 4; ++w) s_rng[w] = r.s[w];
+      }
+      __syncthreads();
+    }
+    bool take = true;  // the IfClassic prefixes read so far hold
     for (uint32_t o = 0; o < pr.nops; ++o) {
       const BatchOp op = a.ops[pr.op0 + o];
+      if (op.kind == B_IF) {
+        take = take && s_cl[op.lmask] != 0;
+        continue;
+      }
+      const bool run = take;
+      take = true;
+      if (!run) continue;
+      if (op.kind == B_MEAS) {
+        batch_measure(tile, size, op.p0, op.lmask, red, s_cl, s_rng, s_meas);
+        continue;
+      }
       if ((base & op.emask) != op.emask) continue;
       apply_tile_op(tile, k, op, a.mats + op.mat);
       __syncthreads();
     }
+    if (classical && t < int(c.ncl)) a.cl[c.cl + t] = s_cl[t];
     for (uint32_t l = t; l < size; l += nb) {
       V* p = st + (base | offs[l >> L] | (l & lowmask));
       if constexpr (sizeof(V) == 16)
@@ -353,6 +446,7 @@ size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 // Per-circuit host plan.
 struct CircPlan {
   int n = 0, k = 0;
+  bool classical = false;
   std::vector<TilePlan> plans;
   std::vector<PassRef> passes;  // op0 relative to this circuit's ops
   std::vector<BatchOp> ops;
@@ -365,13 +459,30 @@ struct MatKey {
   bool operator==(const MatKey& o) const { return h == o.h; }
 };
 
+bool has_classical_ops(const ev_circuit* c) {
+  for (uint64_t j = 0; j < c->nops; ++j)
+    if (c->ops[j].kind == EV_OP_MEASURE || c->ops[j].kind == EV_OP_IF) return true;
+  return false;
+}
+
 void plan_circuit(const ev_circuit* c, int kmax, bool reorder, CircPlan* out) {
   const int n = int(c->num_qubits);
   out->n = n;
   const int k = n <= kmax ? n : kmax;
   out->k = k;
   const int L = std::min(k, 4);
-  std::vector<Pass> passes = plan_passes(c, 0, c->nops, n, k, L, ~uint64_t(0), reorder);
+  out->classical = has_classical_ops(c);
+  std::vector<Pass> passes;
+  if (out->classical) {
+    // one whole-state pass with every op in circuit order (the caller has
+    // checked n <= kmax); measurements and IfClassic prefixes stay in place
+    Pass p;
+    for (uint64_t j = 0; j < c->nops; ++j) p.ops.push_back(j);
+    p.tset = (uint64_t(1) << n) - 1;
+    passes.push_back(std::move(p));
+  } else {
+    passes = plan_passes(c, 0, c->nops, n, k, L, ~uint64_t(0), reorder);
+  }
   // every circuit gets at least one pass: pass 0 is what writes |0...0>
   if (passes.empty()) passes.push_back({{}, (uint64_t(1) << k) - 1});
   std::unordered_map<size_t, std::vector<uint32_t>> seen;  // hash -> offsets
@@ -394,7 +505,16 @@ void plan_circuit(const ev_circuit* c, int kmax, bool reorder, CircPlan* out) {
     out->plans.push_back(plan);
     out->passes.push_back({uint32_t(out->ops.size()), uint32_t(p.ops.size())});
     for (uint64_t j : p.ops) {
-      encode_op(c, c->ops[j], p.tset, local, &tmp);
+      const ev_op& src = c->ops[j];
+      if (src.kind == EV_OP_MEASURE || src.kind == EV_OP_IF) {
+        BatchOp b{};
+        b.kind = src.kind == EV_OP_MEASURE ? B_MEAS : B_IF;
+        b.p0 = uint8_t(src.kind == EV_OP_MEASURE ? src.q0 : 0);
+        b.lmask = uint32_t(src.kind == EV_OP_MEASURE ? src.q1 : src.q0);
+        out->ops.push_back(b);
+        continue;
+      }
+      encode_op(c, src, p.tset, local, &tmp);
       BatchOp b;
       b.kind = tmp.kind;
       b.k1 = tmp.k1;
@@ -500,6 +620,13 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
   int sms = 0;
   EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const size_t ab = dtype == EV_C128 ? 16 : 8;
+  for (uint64_t i = 0; i < count; ++i)
+    if (int(items[i].circuit.num_qubits) > kmax && has_classical_ops(&items[i].circuit))
+      return fail(EV_ERR_INVALID_ARGUMENT,
+                  "batch circuit %llu: measurement and classical control in a batch need a "
+                  "circuit of at most %d qubits (the tile size); it has %llu",
+                  (unsigned long long)i, kmax,
+                  (unsigned long long)items[i].circuit.num_qubits);
   // plan all circuits (in parallel)
   std::vector<CircPlan> cp(count);
   {
@@ -514,7 +641,7 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
   }
   // layout
   std::vector<BatchCirc> circs(count);
-  uint64_t amps = 0, tree = 0, uni = 0, shots = 0, nplans = 0, nops = 0, nmats = 0;
+  uint64_t amps = 0, tree = 0, uni = 0, shots = 0, nplans = 0, nops = 0, nmats = 0, ncl = 0;
   for (uint64_t i = 0; i < count; ++i) {
     BatchCirc& b = circs[i];
     const CircPlan& p = cp[i];
@@ -530,6 +657,11 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
     b.shots = items[i].shots;
     b.shot_out = shots;
     b.seed = items[i].seed;
+    b.run_seed = items[i].run_seed;
+    b.cl = ncl;
+    b.ncl = uint32_t(items[i].circuit.num_classical);
+    b.classical = p.classical ? 1u : 0u;
+    ncl += items[i].circuit.num_classical;
     amps += uint64_t(1) << p.n;
     tree += uint64_t(1) << p.n;
     uni += items[i].shots * uint64_t(p.n);
@@ -591,8 +723,9 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
   const size_t p_states = 0, p_tree = align256(amps * ab), p_uni = align256(p_tree + tree * 8);
   const size_t p_shots = align256(p_uni + uni * 8), p_expz = align256(p_shots + shots * 8);
   const size_t p_done = align256(p_expz + count * 8), p_head = align256(p_done + count * 4);
-  const size_t pool = align256(p_head + 64);
-  const size_t result_bytes = shots * 8 + count * 8;
+  const size_t p_cl = align256(p_head + 64);
+  const size_t pool = align256(p_cl + ncl);
+  const size_t result_bytes = shots * 8 + count * 8 + ncl;
   EV_TRY(grow_dev(&A.dmeta, &A.meta_cap, meta));
   EV_TRY(grow_dev(&A.dpool, &A.pool_cap, pool));
   EV_TRY(grow_host(&A.hstage, &A.stage_cap, std::max(meta, result_bytes)));
@@ -623,6 +756,7 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
   args.done = reinterpret_cast<unsigned*>(dp + p_done);
   args.head = reinterpret_cast<unsigned*>(dp + p_head);
   args.err = reinterpret_cast<int*>(dp + p_head + 16);
+  args.cl = dp + p_cl;
   const size_t smem = (ab << kmax) + (size_t(8) << (kmax > 4 ? kmax - 4 : 0)) + 2 * size_t(threads) * 8;
   const auto t1 = clk::now();
   EV_CUDA(cudaEventRecord(A.e0, A.stream));
@@ -650,6 +784,9 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
   // results: shots | expz, one copy down
   EV_CUDA(cudaMemcpyAsync(hs, dp + p_shots, shots * 8, cudaMemcpyDeviceToHost, A.stream));
   EV_CUDA(cudaMemcpyAsync(hs + shots * 8, dp + p_expz, count * 8, cudaMemcpyDeviceToHost, A.stream));
+  if (ncl)
+    EV_CUDA(cudaMemcpyAsync(hs + shots * 8 + count * 8, dp + p_cl, ncl, cudaMemcpyDeviceToHost,
+                            A.stream));
   int err = 0;
   EV_CUDA(cudaMemcpyAsync(&err, args.err, sizeof(int), cudaMemcpyDeviceToHost, A.stream));
   EV_CUDA(cudaStreamSynchronize(A.stream));
@@ -662,6 +799,8 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
     if (items[i].shots_out && items[i].shots)
       std::memcpy(items[i].shots_out, hshots + circs[i].shot_out, items[i].shots * 8);
     if (items[i].expz_out) *items[i].expz_out = hexpz[i];
+    if (items[i].classical_out && circs[i].ncl)
+      std::memcpy(items[i].classical_out, hs + shots * 8 + count * 8 + circs[i].cl, circs[i].ncl);
   }
   // final states on request (test hook)
   for (uint64_t i = 0; i < count; ++i) {
@@ -706,11 +845,9 @@ extern "C" int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const
     EV_TRY(ev_validate(&c));
     if (c.num_qubits < 1 || c.num_qubits > 30)
       return fail(EV_ERR_INVALID_ARGUMENT, "batch circuit %llu: 1..30 qubits supported", (unsigned long long)i);
-    for (uint64_t j = 0; j < c.nops; ++j)
-      if (c.ops[j].kind == EV_OP_MEASURE || c.ops[j].kind == EV_OP_IF)
-        return fail(EV_ERR_INVALID_ARGUMENT,
-                    "batch circuit %llu: measurement and classical control run through ev_run_seeded",
-                    (unsigned long long)i);
+    if (c.num_classical > uint64_t(kBatchMaxClassical))
+      return fail(EV_ERR_INVALID_ARGUMENT, "batch circuit %llu: at most %d classical bits",
+                  (unsigned long long)i, kBatchMaxClassical);
     if (items[i].shots && !items[i].shots_out)
       return fail(EV_ERR_INVALID_ARGUMENT, "batch circuit %llu: shots requested without an output",
                   (unsigned long long)i);
@@ -743,6 +880,7 @@ extern "C" int ev_batch_run(const ev_batch_circuit* items, uint64_t count, const
         b.shots_out = nullptr;
         b.expz_out = nullptr;
         b.amps_out = nullptr;
+        b.classical_out = nullptr;
         b.shots = 0;
         sample.push_back(b);
       }

@@ -4,9 +4,11 @@
 // as slots and HBM free up: a request needs 2^n x 16 (complex128) or 8
 // (complex64) bytes of state, and the sum over admitted requests stays under
 // the budget.  Admitted requests run concurrently, each on its own stream:
-//   - gate-only requests of at most `batch_qubits` qubits that are admitted
-//     together run together as one persistent batched launch (ev_batch_run)
-//     -- the same-stage work of many small requests in one kernel;
+//   - requests of at most `batch_qubits` qubits (and at most 64 classical
+//     bits) that are admitted together run together as one persistent
+//     batched launch (ev_batch_run), mid-circuit measurements and classical
+//     control included -- the same-stage work of many small requests in one
+//     kernel;
 //   - every other request runs through the device-resident run loop
 //     (ev_state_run: mid-circuit measurements and classical control stay on
 //     the GPU), then draws its shots (ev_sample).
@@ -42,7 +44,7 @@ struct Request {
   uint64_t seed, shots;
   uint64_t* shots_out;
   size_t bytes;
-  bool small_gate_only;
+  bool small;  // runs in batched launches
   clk::time_point t_submit, t_admit;
   bool cancelled = false;
 };
@@ -176,10 +178,10 @@ void worker_loop(ev_server* s) {
             s->pending.pop_front();
             unit.push_back(head);
             s->reserved += head->bytes;
-            if (head->small_gate_only && s->opts.batch_small) {
+            if (head->small && s->opts.batch_small) {
               for (auto it = s->pending.begin(); it != s->pending.end() && unit.size() < 256;) {
                 Request* r = *it;
-                if (!r->cancelled && r->small_gate_only && s->reserved + r->bytes <= s->budget) {
+                if (!r->cancelled && r->small && s->reserved + r->bytes <= s->budget) {
                   unit.push_back(r);
                   s->reserved += r->bytes;
                   it = s->pending.erase(it);
@@ -201,21 +203,26 @@ void worker_loop(ev_server* s) {
     }
     // run the unit outside the lock
     std::vector<ev_server_result> results;
-    if (unit.size() > 1 || (unit[0]->small_gate_only && s->opts.batch_small)) {
+    if (unit.size() > 1 || (unit[0]->small && s->opts.batch_small)) {
       std::vector<ev_batch_circuit> items(unit.size());
+      std::vector<std::vector<uint8_t>> classical(unit.size());
       for (size_t i = 0; i < unit.size(); ++i) {
         items[i] = ev_batch_circuit{};
         items[i].circuit = circuit_of(*unit[i]);
         items[i].seed = unit[i]->seed;
+        items[i].run_seed = unit[i]->seed;  // as run_single: one seed per request
         items[i].shots = unit[i]->shots;
         items[i].shots_out = unit[i]->shots_out;
+        classical[i].assign(unit[i]->ncl ? unit[i]->ncl : 1, 0);
+        items[i].classical_out = classical[i].data();
       }
       ev_batch_options bo{};
       bo.dtype = s->opts.dtype;
       bo.tile_bits = s->opts.batch_qubits;
       bo.threads = 256;
       const int rc = ev_batch_run(items.data(), items.size(), &bo, nullptr);
-      for (Request* r : unit) results.push_back(make_result(*r, rc, nullptr));
+      for (size_t i = 0; i < unit.size(); ++i)
+        results.push_back(make_result(*unit[i], rc, rc == EV_OK ? classical[i].data() : nullptr));
       {
         std::lock_guard<std::mutex> lock(s->mu);
         s->stats.batched_launches++;
@@ -288,10 +295,7 @@ extern "C" int ev_server_submit(ev_server* s, const ev_circuit* c, uint64_t seed
   r->shots = shots;
   r->shots_out = shots_out;
   r->bytes = (size_t(1) << r->nq) * (s->opts.dtype == EV_C128 ? 16 : 8);
-  bool gate_only = true;
-  for (const ev_op& op : r->ops)
-    if (op.kind == EV_OP_MEASURE || op.kind == EV_OP_IF) gate_only = false;
-  r->small_gate_only = gate_only && r->nq >= 1 && int(r->nq) <= s->opts.batch_qubits;
+  r->small = r->nq >= 1 && int(r->nq) <= s->opts.batch_qubits && r->ncl <= 64;
   r->t_submit = clk::now();
   {
     std::lock_guard<std::mutex> lock(s->mu);

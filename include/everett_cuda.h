@@ -245,11 +245,15 @@ int ev_sample(ev_state* s, uint64_t seed, uint64_t shots, uint64_t* out);
 
 /* ---- batched runs (no reference counterpart) ------------------------------
  * Many independent circuits of uneven qubit counts in one persistent launch
- * over a device work queue.  Each circuit holds gate records only
- * (EV_OP_APPLY1/APPLY2/CONTROLLED); it runs from |0...0> and reports
+ * over a device work queue.  Each circuit runs from |0...0> and reports
  * <Z_0> (bloch_vector(0)[2] of the final state, normalised) and `shots`
  * full-register shots drawn exactly as ev_sample draws them with its own
- * seed.  Output pointers may be NULL. */
+ * seed.  A circuit may also measure (EV_OP_MEASURE) and gate ops on its
+ * classical bits (EV_OP_IF), as drive does (src/backend/mod.rs:43-72), with
+ * the uniforms of Rng::seed_from_u64(run_seed); such a circuit must have at
+ * most as many qubits as the tile size (it runs whole in one CTA) and at
+ * most 64 classical bits, else EV_ERR_INVALID_ARGUMENT.  Output pointers
+ * may be NULL. */
 typedef struct ev_batch_circuit {
   ev_circuit circuit;
   uint64_t seed;       /* Rng seed of the shot stream                      */
@@ -257,6 +261,9 @@ typedef struct ev_batch_circuit {
   uint64_t* shots_out; /* [shots]                                          */
   double* expz_out;    /* <Z_0>                                            */
   double* amps_out;    /* final state, 2^n interleaved f64 (test hook)     */
+  uint64_t run_seed;   /* Rng seed of the mid-circuit measurements, as
+                          ev_run_seeded's seed                            */
+  uint8_t* classical_out; /* [num_classical] 0/1 bytes, or NULL           */
 } ev_batch_circuit;
 
 typedef struct ev_batch_options {
@@ -391,8 +398,9 @@ int ev_qasm_emit(const ev_circuit* c, char* buf, uint64_t cap, uint64_t* len);
  * A continuous-batching request loop.  Requests are admitted in arrival
  * order while the state memory of admitted requests (2^n x 16 or 8 bytes)
  * stays within the budget; admitted requests run concurrently on separate
- * streams, and small gate-only requests admitted together share one batched
- * launch.  Mid-circuit measurement and classical control stay on the device.
+ * streams, and small requests admitted together share one batched launch.
+ * Mid-circuit measurement and classical control stay on the device, in
+ * batched launches as in single-request runs.
  * A request's result does not depend on what else is in flight. */
 typedef struct ev_server ev_server;
 
@@ -402,8 +410,8 @@ typedef struct ev_server_options {
   int32_t mode;         /* EV_MODE_* of single-request runs                */
   int32_t variant;      /* EV_FUSED_* when mode is EV_MODE_FUSED           */
   uint64_t hbm_budget;  /* state bytes admitted at once; 0 = 80% of free   */
-  int32_t batch_small;  /* 1: gate-only requests of <= batch_qubits qubits
-                           run through batched launches                    */
+  int32_t batch_small;  /* 1: requests of <= batch_qubits qubits and <= 64
+                           classical bits run through batched launches     */
   int32_t batch_qubits; /* 0 = 13 (complex64) / 12 (complex128)            */
   int32_t start_paused; /* 1: admit nothing until ev_server_resume         */
   int32_t reserved;

@@ -4,14 +4,20 @@ complex128 batches: every final state bit-identical to the oracle's run,
 <Z_0> within 1e-12, shots identical to the oracle's conditional-mass tree.
 complex64 batches: fidelity >= 1 - 1e-6 against the oracle, shots identical
 to the tree of the batch's own final state.  Small tiles force the larger
-circuits through the multi-pass (tile, dependency-counter) queue items."""
+circuits through the multi-pass (tile, dependency-counter) queue items.
+Circuits with mid-circuit measurement and classical control
+(backend/mod.rs:51-72, measure.rs:15-51): classical registers identical to
+the oracle's run with the same seed, amplitudes within 1e-12 (complex128:
+the p1 sums are taken in another order), shots identical to the tree of the
+batch's own final state."""
 import os
 
 import numpy as np
 import pytest
 
 import oracle as O
-from everett_gb300 import Circuit, Gate1, Rng, batch, workloads
+from everett_gb300 import (Apply1, Circuit, Gate1, IfClassic, Measure, Rng, algorithms, batch,
+                           workloads)
 from everett_gb300.error import DeviceTimeout, InvalidArgument
 
 pytestmark = pytest.mark.gpu
@@ -69,11 +75,59 @@ def test_batch_matches_single_runs(gpu):
         assert np.array_equal(a.amplitudes, m.amplitudes)
 
 
-def test_batch_rejects_measurement_and_autotunes(gpu, tmp_path):
-    c = Circuit.with_classical(3, 1)
-    c.h(0).measure(0, 0)
-    with pytest.raises(InvalidArgument):
-        batch.run_batch([c])
+def classical_mix(seed):
+    """Circuits that measure mid-run and gate ops on the outcomes: GHZ with
+    a measurement and a controlled X (the serving mix's kind),
+    teleportation of a prepared state with both corrections, random layers
+    with measurements in between, a nested IfClassic and a conditional
+    measurement, and a gate-only circuit beside them."""
+    out = [workloads.ghz_midmeasure(n) for n in (3, 7, 10)]
+    out.append(algorithms.teleport_state(0.6 + 0.0j, 0.48 + 0.64j))
+    for n in (6, 9):
+        c = Circuit.with_classical(n, 3)
+        c.compose(workloads.random_layers(n, 3, seed + n))
+        c.measure(1, 0).measure(n - 1, 1)
+        c.x_if(0, 2)
+        c.if_classic(1, IfClassic(0, Apply1(Gate1.ry(0.9), 3)))
+        c.compose(workloads.random_layers(n, 2, seed + 2 * n))
+        c.if_classic(1, Measure(2, 2))
+        c.z_if(2, 0)
+        out.append(c)
+    out.append(workloads.random_layers(8, 3, seed))
+    return out
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_batch_measurement_and_classical_control(gpu, dtype):
+    circs = classical_mix(4)
+    run_seeds = [11 + 7 * i for i in range(len(circs))]
+    res, _ = batch.run_batch(circs, seeds=range(len(circs)), shots=200, dtype=dtype,
+                             tile_bits=10, threads=256, return_states=True,
+                             run_seeds=run_seeds)
+    for i, (c, r) in enumerate(zip(circs, res)):
+        want, bits, rc = O.run_seeded(c, run_seeds[i])
+        assert rc == 0
+        assert r.classical == bits, i
+        got = r.amplitudes
+        if dtype == "complex128":
+            assert np.max(np.abs(got - want)) < 1e-12, i
+        else:
+            fid = abs(np.vdot(want, got)) ** 2 / (np.vdot(got, got).real * np.vdot(want, want).real)
+            assert fid >= 1 - 1e-6, i
+        assert np.array_equal(r.shots, O.sample_tree(np.ascontiguousarray(got), i, 200)), i
+    # each circuit's result is the same alone
+    for i in (0, 4):
+        alone, _ = batch.run_batch([circs[i]], seeds=[i], shots=200, dtype=dtype, tile_bits=10,
+                                   threads=256, return_states=True, run_seeds=[run_seeds[i]])
+        assert alone[0].classical == res[i].classical
+        assert np.array_equal(alone[0].amplitudes, res[i].amplitudes)
+        assert np.array_equal(alone[0].shots, res[i].shots)
+
+
+def test_batch_rejects_oversize_classical_and_autotunes(gpu, tmp_path):
+    c = workloads.ghz_midmeasure(9)
+    with pytest.raises(InvalidArgument):  # measurement needs the whole state in one CTA
+        batch.run_batch([c], tile_bits=8)
     os.environ["EV_AUTOTUNE_CACHE"] = str(tmp_path / "tune.txt")
     try:
         circs = tfim_mix(30, 8, 16, seed=5)
