@@ -18,6 +18,7 @@
 // way an anti-diagonal complex128 gate with entries in {1, i, -1, -i} (X, Y)
 // is applied as a permutation with sign flips.
 #include <cstdio>
+#include <cstdlib>
 
 #include <type_traits>
 
@@ -149,6 +150,79 @@ __global__ void __launch_bounds__(256) k_pair(V* __restrict__ s, uint64_t npairs
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < npairs; i += stride) {
     const uint64_t i0 = insert0(i, k);
     pair_update<KIND>(s, i0, i0 | bit, m);
+  }
+}
+
+// apply_1q on one of the lowest five qubits, resolved within a warp: each
+// lane loads one amplitude (a warp moves 32 consecutive amplitudes, 512
+// contiguous bytes in complex128, with 16-byte accesses), takes its partner
+// j ^ 2^k from lane ^ 2^k by __shfl_xor_sync, and computes its own output
+// of the pair -- new0 = m0*a0 + m1*a1 on the lane whose bit k is 0, new1 =
+// m2*a0 + m3*a1 on the other -- with the pair form's operations in the
+// pair form's order, so the results are the same bits.  Each amplitude is
+// read and written once by one lane, in whole 128-byte lines.  Needs 2^n a
+// multiple of 32 (n >= 5) so that every warp is full.
+template <typename V>
+__device__ __forceinline__ V shfl_xor_amp(V a, int mask) {
+  V r;
+  r.x = __shfl_xor_sync(0xFFFFFFFFu, a.x, mask);
+  r.y = __shfl_xor_sync(0xFFFFFFFFu, a.y, mask);
+  return r;
+}
+
+// Instantiated for complex128 dense and anti-diagonal gates (see
+// low_shuffle_enabled for the measurements behind that choice).
+template <int KIND, typename V>
+__global__ void __launch_bounds__(256) k_pair_shfl(V* __restrict__ s, uint64_t len, int k, M1<V> m,
+                                                   const uint8_t* pred) {
+  if (skip(pred)) return;
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  const int lane = int(threadIdx.x & 31), mask = 1 << k;
+  const bool hi = ((lane >> k) & 1) != 0;  // this lane holds a1 of its pair
+  // the lane's matrix row: (m0, m1) for new0, (m2, m3) for new1
+  const V r0 = hi ? m.m2 : m.m0, r1 = hi ? m.m3 : m.m1;
+  if constexpr (std::is_same<V, double2>::value && (KIND == K1_DENSE || KIND == K1_REAL)) {
+    const SoftM1 f = soft_matrix<KIND>(m.m0, m.m1, m.m2, m.m3);
+    if (f.ok) {  // uniform: the row's factors on the integer pipes
+      const softfp::Unpacked u0 = hi ? f.u2 : f.u0, u1 = hi ? f.u3 : f.u1;
+      for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < len; j += stride) {
+        const double2 own = s[j], other = shfl_xor_amp(own, mask);
+        const double2 a0 = hi ? other : own, a1 = hi ? own : other;
+        const SoftAmp s0 = sunpack(a0), s1 = sunpack(a1);
+        double2 out;
+        if (sok(s0) & sok(s1)) {
+          if constexpr (KIND == K1_REAL)
+            out = cadd(srmul(u0, s0), srmul(u1, s1));
+          else
+            out = cadd(scmul(r0, u0, a0, s0), scmul(r1, u1, a1, s1));
+        } else if constexpr (KIND == K1_REAL) {
+          out = cadd(rmul(r0.x, a0), rmul(r1.x, a1));
+        } else {
+          out = cadd(cmul(r0, a0), cmul(r1, a1));
+        }
+        s[j] = out;
+      }
+      return;
+    }
+  }
+  if constexpr (std::is_same<V, double2>::value && KIND == K1_ANTI) {
+    const int p1 = unit_power(m.m1), p2 = unit_power(m.m2);
+    if ((p1 | p2) >= 0) {  // X, Y and their sign variants: a permutation
+      const int p = hi ? p2 : p1;
+      for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < len; j += stride)
+        s[j] = unit_mul(p, shfl_xor_amp(s[j], mask));
+      return;
+    }
+  }
+  for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < len; j += stride) {
+    const V own = s[j], other = shfl_xor_amp(own, mask);
+    const V a0 = hi ? other : own, a1 = hi ? own : other;
+    if constexpr (KIND == K1_DENSE)
+      s[j] = cadd(cmul(r0, a0), cmul(r1, a1));
+    else if constexpr (KIND == K1_REAL)
+      s[j] = cadd(rmul(r0.x, a0), rmul(r1.x, a1));
+    else  // K1_ANTI: new0 = m1*a1, new1 = m2*a0
+      s[j] = cmul(hi ? m.m2 : m.m1, other);
   }
 }
 
@@ -359,12 +433,37 @@ static unsigned grid_for(const ev_state* s, uint64_t work, int per_sm = 8) {
   return unsigned(want < 1 ? 1 : (want < cap ? want : cap));
 }
 
+// complex128 dense and anti-diagonal gates on qubits 0-4 take the
+// warp-shuffle kernel unless EV_LOW_SHUFFLE=0 (the pair kernel; the same
+// results).  Measured at 30 qubits (ms, shuffle vs pair): complex128 dense
+// on qubit 0 11.73 vs 12.42, X on qubit 1 5.26 vs 5.48, but H on qubit 2
+// 8.21 vs 6.41 (each lane unpacks both amplitudes of its pair for the
+// integer-pipe products, twice the pair form's work) and every complex64
+// gate 2.93-2.95 vs 2.63 (8 bytes in flight per lane and load instead of
+// 16) -- so those keep the pair kernel.
+static bool low_shuffle_enabled() {
+  const char* e = getenv("EV_LOW_SHUFFLE");
+  return e == nullptr || e[0] != '0';
+}
+
 template <typename V>
 static void go_apply1(ev_state* s, Kind1 kind, uint64_t k, const double m[8], const uint8_t* pred) {
   V* a = static_cast<V*>(s->amps);
   const M1<V> mm = to_m1<V>(m);
   const uint64_t npairs = s->len() / 2;
   const unsigned g = grid_for(s, npairs);
+  if constexpr (std::is_same<V, double2>::value) {
+    static const bool shfl = low_shuffle_enabled();
+    if (shfl && k < 5 && s->n >= 5 && (kind == K1_DENSE || kind == K1_ANTI)) {
+      const uint64_t len = s->len();
+      const unsigned gl = grid_for(s, len);
+      if (kind == K1_DENSE)
+        k_pair_shfl<K1_DENSE><<<gl, 256, 0, s->stream>>>(a, len, int(k), mm, pred);
+      else
+        k_pair_shfl<K1_ANTI><<<gl, 256, 0, s->stream>>>(a, len, int(k), mm, pred);
+      return;
+    }
+  }
   switch (kind) {
     case K1_DENSE: k_pair<K1_DENSE><<<g, 256, 0, s->stream>>>(a, npairs, int(k), mm, pred); break;
     case K1_REAL: k_pair<K1_REAL><<<g, 256, 0, s->stream>>>(a, npairs, int(k), mm, pred); break;

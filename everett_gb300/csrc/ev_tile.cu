@@ -70,10 +70,10 @@ constexpr uint32_t kTileWaitLimit = 1u << 24;  // try_wait polls before giving u
 // block: [tile 2^k amplitudes][row offsets 2^(k-L)][op records][comp qubits].
 // A load that never completes sets *err (the run's device flag, reported as
 // EV_ERR_TIMEOUT) and ends the block after a bounded drain.
-template <typename V>
+template <typename V, bool BULK>
 __global__ void __launch_bounds__(kTileThreads, 2)
     k_tile(V* __restrict__ s, uint64_t ntiles, const TilePlan* __restrict__ gplan,
-           const TileOp* __restrict__ gops, int nops, const uint8_t* pred, int bulk, int* err) {
+           const TileOp* __restrict__ gops, int nops, const uint8_t* pred, int* err) {
   if (pred != nullptr && *pred == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   const uint32_t size = 1u << k;
   const uint32_t nrows = 1u << (k - L);
   const uint32_t rowbytes = uint32_t(sizeof(V)) << L;
-  const bool use_bulk = bulk != 0 && rowbytes % 16 == 0;  // uniform across the block
+  const bool use_bulk = BULK && rowbytes % 16 == 0;  // uniform across the block
   const int warp = int(threadIdx.x >> 5), lane = int(threadIdx.x & 31);
   V* tile = reinterpret_cast<V*>(smem_raw);
   uint64_t* offs = reinterpret_cast<uint64_t*>(smem_raw + sizeof(V) * size);
@@ -171,26 +171,34 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   if (use_bulk && warp == 0) bulk_wait_all();
 }
 
+template <typename V, bool BULK>
+static int launch_tile_as(ev_state* s, uint64_t ntiles, size_t smem, const TilePlan* dplan,
+                          const TileOp* dops, int nops, const uint8_t* pred) {
+  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_tile<V, BULK>)));
+  int per_sm = 0;
+  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<V, BULK>, kTileThreads,
+                                                        smem));
+  if (per_sm < 1) per_sm = 1;
+  uint64_t grid = uint64_t(s->num_sms) * per_sm;
+  if (grid > ntiles) grid = ntiles;
+  ProfScope prof(s, P_TILE, 2.0 * double(s->len()) * double(sizeof(V)));
+  s->launches += 1;
+  int* derr = reinterpret_cast<int*>(s->scratch.counter + 1);
+  k_tile<V, BULK><<<unsigned(grid), kTileThreads, smem, s->stream>>>(
+      static_cast<V*>(s->amps), ntiles, dplan, dops, nops, pred, derr);
+  EV_CUDA(cudaGetLastError());
+  return EV_OK;
+}
+
 template <typename V>
 static int launch_tile(ev_state* s, uint64_t ntiles, const TilePlan& plan, const TilePlan* dplan,
                        const TileOp* dops, int nops, const uint8_t* pred) {
   const size_t ops_at = (sizeof(V) * (size_t(1) << plan.k) +
                          sizeof(uint64_t) * (size_t(1) << (plan.k - plan.L)) + 15) & ~size_t(15);
   const size_t smem = ops_at + sizeof(TileOp) * size_t(nops) + 64;
-  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_tile<V>)));
-  int per_sm = 0;
-  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<V>, kTileThreads, smem));
-  if (per_sm < 1) per_sm = 1;
-  uint64_t grid = uint64_t(s->num_sms) * per_sm;
-  if (grid > ntiles) grid = ntiles;
-  ProfScope prof(s, P_TILE, 2.0 * double(s->len()) * double(sizeof(V)));
-  s->launches += 1;
-  static const int bulk = tile_bulk_enabled() ? 1 : 0;
-  int* derr = reinterpret_cast<int*>(s->scratch.counter + 1);
-  k_tile<V><<<unsigned(grid), kTileThreads, smem, s->stream>>>(static_cast<V*>(s->amps), ntiles,
-                                                               dplan, dops, nops, pred, bulk, derr);
-  EV_CUDA(cudaGetLastError());
-  return EV_OK;
+  static const bool bulk = tile_bulk_enabled();
+  if (bulk) return launch_tile_as<V, true>(s, ntiles, smem, dplan, dops, nops, pred);
+  return launch_tile_as<V, false>(s, ntiles, smem, dplan, dops, nops, pred);
 }
 
 int default_tile_bits(int dtype) { return dtype == EV_C128 ? 12 : 13; }
@@ -235,7 +243,9 @@ int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, 
       if (s->dtype == EV_C128 && ops[j].kind == T_1Q)
         ops[j].soft = uint8_t(ops[j].k1 == K1_REAL ? soft.real : soft.other);
     }
-    if (chains) mark_chains(ops.data(), ops.size(), chains == 2);
+    // complex128 only: a complex64 chain would convert its f64 matrices to
+    // f32 per pair, and those conversions run at the FP64 rate
+    if (chains && s->dtype == EV_C128) mark_chains(ops.data(), ops.size(), chains == 2);
     SegStep st;
     st.fused = 0;
     st.off0 = blob->add(&plan, sizeof(plan));

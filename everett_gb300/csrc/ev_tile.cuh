@@ -157,6 +157,20 @@ template <int KIND, typename V, typename Op>
 __device__ __forceinline__ void tile_2q(V* t, uint32_t count, const Op& op, const double* mm) {
   const uint32_t ba = 1u << op.p0, bb = 1u << op.p1;
   const int lo = op.lo, hi = op.hi;
+  if constexpr (KIND == T_DIAG2 && !std::is_same<V, double2>::value) {
+    // complex64: the f64 -> f32 conversions of the four entries run at the
+    // FP64 rate on GB300, so they are made once, not per quad
+    const V d0 = ldm<V>(mm, 0), d1 = ldm<V>(mm, 5), d2 = ldm<V>(mm, 10), d3 = ldm<V>(mm, 15);
+    for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
+      const uint32_t base = ins0(ins0(i, lo), hi);
+      const uint32_t i1 = base | bb, i2 = base | ba, i3 = base | ba | bb;
+      t[base] = cmul(d0, t[base]);
+      t[i1] = cmul(d1, t[i1]);
+      t[i2] = cmul(d2, t[i2]);
+      t[i3] = cmul(d3, t[i3]);
+    }
+    return;
+  }
   for (uint32_t i = threadIdx.x; i < count; i += blockDim.x) {
     const uint32_t base = ins0(ins0(i, lo), hi);
     const uint32_t i1 = base | bb, i2 = base | ba, i3 = base | ba | bb;
