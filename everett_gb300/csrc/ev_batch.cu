@@ -149,7 +149,7 @@ __device__ void block_sum2(double* red, double& x, double& y) {
   __syncthreads();
 }
 
-// <Z_0>, sampling tree (level q at offset 2^q - 1, as ev_sample builds it)
+// <Z_0>, sampling tree (level q at offset 2^q, as ev_sample builds it)
 // and shots of one circuit whose amplitudes are at `amps` (shared memory or
 // HBM).
 template <typename V>
@@ -169,13 +169,13 @@ __device__ void finalize(const V* amps, bool global, const BatchCirc& c, uint32_
   if (t == 0) a.expz[ci] = (r0 - r1) / (r0 + r1);
   double* tr = a.trees + c.tree;
   for (uint64_t r = t; r < half; r += nb)
-    __stcg(tr + (half - 1) + r,
+    __stcg(tr + half + r,
            __dadd_rn(nsq(ld_amp(amps + r, global)), nsq(ld_amp(amps + r + half, global))));
   __syncthreads();
   for (int q = int(c.n) - 2; q >= 0; --q) {
     const uint64_t w = uint64_t(1) << q;
     for (uint64_t r = t; r < w; r += nb)
-      __stcg(tr + (w - 1) + r, __dadd_rn(__ldcg(tr + (2 * w - 1) + r), __ldcg(tr + (2 * w - 1) + r + w)));
+      __stcg(tr + w + r, __dadd_rn(__ldcg(tr + 2 * w + r), __ldcg(tr + 2 * w + r + w)));
     __syncthreads();
   }
   const int n = int(c.n);
@@ -183,8 +183,8 @@ __device__ void finalize(const V* amps, bool global, const BatchCirc& c, uint32_
     uint64_t r = 0;
     for (int q = 0; q < n; ++q) {
       const uint64_t w = uint64_t(1) << q;
-      const double m = __ldcg(tr + (w - 1) + r);
-      const double m1 = (q + 1 < n) ? __ldcg(tr + (2 * w - 1) + r + w) : nsq(ld_amp(amps + r + w, global));
+      const double m = __ldcg(tr + w + r);
+      const double m1 = (q + 1 < n) ? __ldcg(tr + 2 * w + r + w) : nsq(ld_amp(amps + r + w, global));
       const double p1 = __ddiv_rn(m1, m);
       if (a.uni[c.uni + s * uint64_t(n) + q] < p1) r |= w;
     }

@@ -379,7 +379,9 @@ __global__ void k_pred_and(const uint8_t* __restrict__ classical, const uint64_t
 }
 
 // ---- sampling tree --------------------------------------------------------
-// mass level q (2^q entries) lives at offset 2^q - 1.  mass[n-1][r] =
+// mass level q (2^q entries) lives at offset 2^q, so every level starts on a
+// 2^q x 8-byte boundary and a warp's run of entries covers whole 32-byte
+// sectors (entry 0 of the 2^n-double buffer is unused).  mass[n-1][r] =
 // |a_r|^2 + |a_{r+2^(n-1)}|^2 and mass[q][r] = mass[q+1][r] + mass[q+1][r+2^q].
 
 // complex128 leaves use the oracle's arithmetic (nsq + nsq, f64), so shots
@@ -410,7 +412,7 @@ __global__ void __launch_bounds__(256)
     out[r] = __dadd_rn(in[r], in[r + w]);
 }
 
-// Several levels per pass.  Level q holds 2^q sums at mass + 2^q - 1, entry
+// Several levels per pass.  Level q holds 2^q sums at mass + 2^q, entry
 // e = level q+1 entry e + level q+1 entry e + 2^q.  The entries of L
 // consecutive levels that end in entry r of the lowest of them form a
 // subtree over the 2^L source entries r + j S of the level above them
@@ -419,26 +421,60 @@ __global__ void __launch_bounds__(256)
 // and writes every level of it: each level is written once and no level but
 // the source is read.
 
-// Levels n-1 (leaves) .. n-L from the amplitudes.
+// Levels n-1 (leaves) .. n-L from the amplitudes.  Each thread takes two
+// neighbouring source columns r, r + 1 (r even): its amplitude loads and its
+// tree stores move 16 bytes each (two complex64 amplitudes; two f64 entries,
+// aligned because every level starts at 2^q), half the memory instructions
+// of one column per thread.  The sums are the same, in the same order.
+template <typename V>
+struct Amp2;  // two consecutive amplitudes as one vector access
+template <>
+struct Amp2<float2> {
+  using T = float4;
+  __device__ static void split(const float4& v, float2& a, float2& b) {
+    a = make_float2(v.x, v.y);
+    b = make_float2(v.z, v.w);
+  }
+};
+template <>
+struct Amp2<double2> {
+  struct T {
+    double2 a, b;
+  };
+  __device__ static void split(const T& v, double2& a, double2& b) {
+    a = v.a;
+    b = v.b;
+  }
+};
+
 template <typename V, int L>
 __global__ void __launch_bounds__(256)
     k_mass_leaf_fused(const V* __restrict__ a, int n, double* __restrict__ mass) {
-  constexpr int C = 1 << (L - 1);  // leaves per thread
+  constexpr int C = 1 << (L - 1);  // leaves per column
+  using A2 = Amp2<V>;
   const uint64_t S = uint64_t(1) << (n - L);
   const uint64_t half = uint64_t(1) << (n - 1);
-  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-  for (uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < S; r += stride) {
-    V lo[C], hi[C];
+  const uint64_t stride = 2 * uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t r = 2 * (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x); r < S; r += stride) {
+    V lo0[C], lo1[C], hi0[C], hi1[C];
 #pragma unroll
     for (int j = 0; j < C; ++j) {
-      lo[j] = a[r + uint64_t(j) * S];
-      hi[j] = a[r + uint64_t(j) * S + half];
+      if constexpr (sizeof(V) == 8) {
+        A2::split(*reinterpret_cast<const float4*>(a + r + uint64_t(j) * S), lo0[j], lo1[j]);
+        A2::split(*reinterpret_cast<const float4*>(a + r + uint64_t(j) * S + half), hi0[j], hi1[j]);
+      } else {
+        lo0[j] = a[r + uint64_t(j) * S];
+        lo1[j] = a[r + 1 + uint64_t(j) * S];
+        hi0[j] = a[r + uint64_t(j) * S + half];
+        hi1[j] = a[r + 1 + uint64_t(j) * S + half];
+      }
     }
-    double m[C];
+    double m0[C], m1[C];
 #pragma unroll
     for (int j = 0; j < C; ++j) {
-      m[j] = leaf_mass(lo[j], hi[j]);
-      mass[(half - 1) + r + uint64_t(j) * S] = m[j];
+      m0[j] = leaf_mass(lo0[j], hi0[j]);
+      m1[j] = leaf_mass(lo1[j], hi1[j]);
+      *reinterpret_cast<double2*>(mass + half + r + uint64_t(j) * S) = make_double2(m0[j], m1[j]);
     }
 #pragma unroll
     for (int lev = 1; lev < L; ++lev) {
@@ -446,32 +482,38 @@ __global__ void __launch_bounds__(256)
       const uint64_t w = uint64_t(cnt) * S;
 #pragma unroll
       for (int j = 0; j < cnt; ++j) {
-        m[j] = __dadd_rn(m[j], m[j + cnt]);
-        mass[(w - 1) + r + uint64_t(j) * S] = m[j];
+        m0[j] = __dadd_rn(m0[j], m0[j + cnt]);
+        m1[j] = __dadd_rn(m1[j], m1[j + cnt]);
+        *reinterpret_cast<double2*>(mass + w + r + uint64_t(j) * S) = make_double2(m0[j], m1[j]);
       }
     }
   }
 }
 
-// Levels qsrc-1 .. qsrc-L from level qsrc.
+// Levels qsrc-1 .. qsrc-L from level qsrc, two columns per thread as above.
 template <int L>
 __global__ void __launch_bounds__(256) k_mass_level_fused(double* __restrict__ mass, int qsrc) {
-  constexpr int C = 1 << L;  // source entries per thread
+  constexpr int C = 1 << L;  // source entries per column
   const uint64_t S = uint64_t(1) << (qsrc - L);
-  const double* __restrict__ src = mass + ((uint64_t(1) << qsrc) - 1);
-  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
-  for (uint64_t r = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; r < S; r += stride) {
-    double m[C];
+  const double* __restrict__ src = mass + (uint64_t(1) << qsrc);
+  const uint64_t stride = 2 * uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t r = 2 * (uint64_t(blockIdx.x) * blockDim.x + threadIdx.x); r < S; r += stride) {
+    double m0[C], m1[C];
 #pragma unroll
-    for (int j = 0; j < C; ++j) m[j] = src[r + uint64_t(j) * S];
+    for (int j = 0; j < C; ++j) {
+      const double2 v = *reinterpret_cast<const double2*>(src + r + uint64_t(j) * S);
+      m0[j] = v.x;
+      m1[j] = v.y;
+    }
 #pragma unroll
     for (int lev = 1; lev <= L; ++lev) {
       const int cnt = C >> lev;
       const uint64_t w = uint64_t(cnt) * S;
 #pragma unroll
       for (int j = 0; j < cnt; ++j) {
-        m[j] = __dadd_rn(m[j], m[j + cnt]);
-        mass[(w - 1) + r + uint64_t(j) * S] = m[j];
+        m0[j] = __dadd_rn(m0[j], m0[j + cnt]);
+        m1[j] = __dadd_rn(m1[j], m1[j + cnt]);
+        *reinterpret_cast<double2*>(mass + w + r + uint64_t(j) * S) = make_double2(m0[j], m1[j]);
       }
     }
   }
@@ -481,8 +523,8 @@ __global__ void __launch_bounds__(256) k_mass_level_fused(double* __restrict__ m
 __global__ void __launch_bounds__(1024) k_mass_top(double* __restrict__ mass, int top) {
   for (int q = top - 1; q >= 0; --q) {
     const uint64_t w = uint64_t(1) << q;
-    const double* in = mass + (2 * w - 1);
-    double* out = mass + (w - 1);
+    const double* in = mass + 2 * w;
+    double* out = mass + w;
     for (uint64_t r = threadIdx.x; r < w; r += blockDim.x) out[r] = __dadd_rn(in[r], in[r + w]);
     __syncthreads();
   }
@@ -498,8 +540,8 @@ __global__ void __launch_bounds__(256)
   uint64_t r = 0;
   for (int q = 0; q < n; ++q) {
     const uint64_t w = uint64_t(1) << q;
-    const double m = mass[(w - 1) + r];
-    const double m1 = (q + 1 < n) ? mass[(2 * w - 1) + r + w] : nsq(a[r + w]);
+    const double m = mass[w + r];
+    const double m1 = (q + 1 < n) ? mass[2 * w + r + w] : nsq(a[r + w]);
     const double p1 = __ddiv_rn(m1, m);
     if (uni[s * uint64_t(n) + q] < p1) r |= w;
   }
@@ -617,7 +659,7 @@ int reduce_norm(const ev_state* s, double* out_host) {
 }
 
 static int ensure_mass(ev_state* s) {
-  const uint64_t need = s->len() - 1;
+  const uint64_t need = s->len();
   if (s->mass && s->mass_len >= need) return EV_OK;
   if (s->mass) cudaFreeAsync(s->mass, s->stream);
   s->mass = nullptr;
@@ -639,19 +681,19 @@ static int build_mass(ev_state* s) {
   const uint64_t half = s->len() / 2;
   int q;  // highest level still to build
   if (n - LL >= 12) {
-    const uint64_t S = uint64_t(1) << (n - LL);
+    const uint64_t S = uint64_t(1) << (n - LL);  // columns, two per thread
     if (s->dtype == EV_C128)
       k_mass_leaf_fused<double2, LL>
-          <<<grid_for(s, S, resident_blocks<k_mass_leaf_fused<double2, LL>>()), 256, 0,
+          <<<grid_for(s, S / 2, resident_blocks<k_mass_leaf_fused<double2, LL>>()), 256, 0,
              s->stream>>>(static_cast<const double2*>(s->amps), n, mass);
     else
       k_mass_leaf_fused<float2, LL>
-          <<<grid_for(s, S, resident_blocks<k_mass_leaf_fused<float2, LL>>()), 256, 0,
+          <<<grid_for(s, S / 2, resident_blocks<k_mass_leaf_fused<float2, LL>>()), 256, 0,
              s->stream>>>(static_cast<const float2*>(s->amps), n, mass);
     s->launches += 1;
     q = n - 1 - LL;
   } else {
-    double* top = mass + (half - 1);  // level n-1
+    double* top = mass + half;  // level n-1
     if (s->dtype == EV_C128)
       k_mass_leaf<double2><<<grid_for(s, half), 256, 0, s->stream>>>(
           static_cast<const double2*>(s->amps), half, top);
@@ -662,13 +704,13 @@ static int build_mass(ev_state* s) {
     q = n - 2;
   }
   for (; q - (L - 1) >= 12; q -= L) {
-    k_mass_level_fused<L><<<grid_for(s, uint64_t(1) << (q - (L - 1))), 256, 0, s->stream>>>(
-        mass, q + 1);
+    k_mass_level_fused<L><<<grid_for(s, uint64_t(1) << (q - L)), 256, 0, s->stream>>>(mass,
+                                                                                      q + 1);
     s->launches += 1;
   }
   for (; q >= 12; --q) {
     const uint64_t w = uint64_t(1) << q;
-    k_mass_level<<<grid_for(s, w), 256, 0, s->stream>>>(mass + (2 * w - 1), w, mass + (w - 1));
+    k_mass_level<<<grid_for(s, w), 256, 0, s->stream>>>(mass + 2 * w, w, mass + w);
     s->launches += 1;
   }
   if (q >= 0) {
