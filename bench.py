@@ -87,8 +87,9 @@ def parse_args():
                     help="run one section alone (for profiling): the complex64 fused or tiled "
                          "path on the random-layer circuit, the TFIM batch, the serving mix, "
                          "prepared-graph replay, or each streaming kernel class alone")
-    ap.add_argument("--variant", default="bf16x3", choices=["bf16x3", "tf32x3", "fp32", "ozaki"],
-                    help="fused arithmetic for --case fused (ozaki: the complex128 one)")
+    ap.add_argument("--variant", default="bf16x3",
+                    choices=["bf16x3", "tf32x3", "fp32", "ozaki", "ozaki6"],
+                    help="fused arithmetic for --case fused (ozaki, ozaki6: the complex128 ones)")
     return ap.parse_args()
 
 
@@ -370,14 +371,16 @@ def extras_c64(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, peak_kin
     return out
 
 
-def extras_c128_fused(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, peak_kind):
+def extras_c128_fused(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, peak_kind,
+                      variant="ozaki"):
     """The same circuit through the complex128 fused path: 5-qubit unitaries
-    on the FP16 tensor cores with 8-bit digit slicing, against the bit-exact
-    tiled complex128 result."""
+    on the FP16 tensor cores with 8-bit digit slicing (seven digits, or six
+    with variant "ozaki6"), against the bit-exact tiled complex128 result."""
     from everett_gb300 import State
     n = circuit.num_qubits()
+    nd = 6 if variant == "ozaki6" else 7
     st = State.zero(n, "complex128")
-    kw = dict(mode="fused", variant="ozaki")
+    kw = dict(mode="fused", variant=variant)
     timed_runs(L, N, st, circuit, 1, **kw)
     ms, prof = timed_runs(L, N, st, circuit, 2, **kw)
     ov = ref_state.overlap(st)
@@ -385,16 +388,17 @@ def extras_c128_fused(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, p
                        "k_fused_oz (fused 5-qubit unitary, complex128 by digit slicing, tcgen05)",
                        ncu_figure("k_fused_oz_c128", "traffic_bytes_per_launch_full_size"))
     if roof:
-        # digit-pair MMAs per launch: 2^n / 4096 steps x 2 halves x 28 pairs x
-        # 4 K-steps of 128 x 32 x 16 -- 7168 flops per amplitude
-        flops = 7168.0 * (1 << n)
+        # digit-pair MMAs per launch: 2^n / 4096 steps x 2 halves x
+        # nd(nd+1)/2 pairs x 4 K-steps of 128 x 32 x 16 -- 7168 flops per
+        # amplitude with seven digits, 5376 with six
+        flops = 256.0 * nd * (nd + 1) * (1 << n)
         tf = flops / (roof["avg_launch_ms"] / 1e3) / 1e12
         bf = bf16_peak()
         roof["tensor"] = {"achieved_tflops": round(tf, 1), "peak_tflops": bf[0],
                           "frac": round(tf / bf[0], 4), "peak_source": bf[1],
                           "flops_per_launch": flops}
     out = {"workload": f"random-layer circuit, {n} qubits, depth 20, complex128 fused "
-                       f"(ozaki: seven 8-bit FP16 digits per f64, exact f32 digit-pair sums, "
+                       f"({variant}: {nd} 8-bit FP16 digits per f64, exact f32 digit-pair sums, "
                        f"int64 recombination)",
            "ms_per_run": round(ms, 2), "speedup_vs_complex128_tiled": round(c128_ms / ms, 2),
            "gate_GBps": round(bytes_per_step / (ms / 1e3) / 1e9, 1),
@@ -1050,6 +1054,10 @@ def run_ours(args, dist: Dist):
             for key, fn in (("complex128_fused_same_circuit",
                              lambda: extras_c128_fused(L, N, state, circuit, c128_ms,
                                                        bytes_per_step, peak, peak_kind)),
+                            ("complex128_fused6_same_circuit",
+                             lambda: extras_c128_fused(L, N, state, circuit, c128_ms,
+                                                       bytes_per_step, peak, peak_kind,
+                                                       variant="ozaki6")),
                             ("complex64_fused_same_circuit",
                              lambda: extras_c64(L, N, state, circuit, c128_ms, bytes_per_step,
                                                 peak, peak_kind)),
@@ -1107,7 +1115,8 @@ def run_case(args):
         return
     L = N.lib()
     c = workloads.random_layers(args.qubits, args.depth, seed=1)
-    dtype = "complex128" if args.case == "fused" and args.variant == "ozaki" else "complex64"
+    dtype = ("complex128" if args.case == "fused" and args.variant in ("ozaki", "ozaki6")
+             else "complex64")
     st = State.zero(args.qubits, dtype)
     kw = (dict(mode="fused", variant=args.variant, tile_bits=args.fuse_bits) if args.case == "fused"
           else dict(mode="tiled"))

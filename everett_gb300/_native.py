@@ -25,7 +25,7 @@ assert OP_DTYPE.itemsize == 288
 OP_APPLY1, OP_APPLY2, OP_CONTROLLED, OP_MEASURE, OP_IF = 1, 2, 3, 4, 5
 C128, C64 = 0, 1
 MODE_EXACT, MODE_TILED, MODE_FUSED = 0, 1, 2
-FUSED_TF32X3, FUSED_BF16X3, FUSED_FP32, FUSED_OZAKI = 0, 1, 2, 3
+FUSED_TF32X3, FUSED_BF16X3, FUSED_FP32, FUSED_OZAKI, FUSED_OZAKI6 = 0, 1, 2, 3, 4
 
 OK = 0
 ERR_QUBIT_OUT_OF_RANGE = 1
@@ -130,6 +130,7 @@ _SIGS = {
     "ev_marginal_low": [_P, _U64, _DP],
     "ev_softfp_check": [_U64, _U64, C.POINTER(_U64)],
     "ev_ozaki_gemm_host": [_DP, _U64, _DP, _DP],
+    "ev_ozaki_gemm_host_digits": [_DP, _U64, _DP, _DP, _I32],
     "ev_max_abs_diff": [_P, _P, _DP],
     "ev_host_alloc": [_U64, C.POINTER(_P)],
     "ev_host_free": [_P],

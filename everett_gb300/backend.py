@@ -23,9 +23,10 @@ _DTYPES = {"complex128": N.C128, "c128": N.C128, "complex64": N.C64, "c64": N.C6
 _MODES = {"exact": N.MODE_EXACT, "tiled": N.MODE_TILED, "fused": N.MODE_FUSED,
           N.MODE_EXACT: N.MODE_EXACT, N.MODE_TILED: N.MODE_TILED, N.MODE_FUSED: N.MODE_FUSED}
 _VARIANTS = {"tf32x3": N.FUSED_TF32X3, "bf16x3": N.FUSED_BF16X3, "fp32": N.FUSED_FP32,
-             "ozaki": N.FUSED_OZAKI,
+             "ozaki": N.FUSED_OZAKI, "ozaki6": N.FUSED_OZAKI6,
              N.FUSED_TF32X3: N.FUSED_TF32X3, N.FUSED_BF16X3: N.FUSED_BF16X3,
-             N.FUSED_FP32: N.FUSED_FP32, N.FUSED_OZAKI: N.FUSED_OZAKI}
+             N.FUSED_FP32: N.FUSED_FP32, N.FUSED_OZAKI: N.FUSED_OZAKI,
+             N.FUSED_OZAKI6: N.FUSED_OZAKI6}
 
 
 class State:
@@ -267,7 +268,8 @@ class CudaStateVectorBackend:
         """mode: "exact" (one kernel per op), "tiled" (runs of ops per
         shared-memory pass) or "fused" (dense k-qubit unitaries, k =
         tile_bits; complex64 arithmetic = variant "tf32x3" (default) |
-        "bf16x3" | "fp32", complex128 = "ozaki": 5-qubit unitaries on the
+        "bf16x3" | "fp32", complex128 = "ozaki" or "ozaki6" (six digits,
+        faster, ~7e-14 of a row's largest value per pass): 5-qubit unitaries on the
         tensor cores by 8-bit digit slicing)."""
         return cls.run_seeded(circuit, 0, dtype=dtype, mode=mode, tile_bits=tile_bits,
                               variant=variant)

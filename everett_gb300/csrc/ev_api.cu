@@ -280,9 +280,9 @@ static int build_plan(ev_state* s, const ev_circuit* c, const ev_run_options* o,
   const int mode = o ? o->mode : EV_MODE_TILED;
   const int tile_bits = o ? o->tile_bits : 0;
   const int variant = o ? o->variant : 0;
-  if (mode == EV_MODE_FUSED && (variant == EV_FUSED_OZAKI) != (s->dtype == EV_C128))
-    return fail(EV_ERR_INVALID_ARGUMENT, variant == EV_FUSED_OZAKI
-                                             ? "the ozaki fused variant needs complex128 amplitudes"
+  if (mode == EV_MODE_FUSED && (variant == EV_FUSED_OZAKI || variant == EV_FUSED_OZAKI6) != (s->dtype == EV_C128))
+    return fail(EV_ERR_INVALID_ARGUMENT, (variant == EV_FUSED_OZAKI || variant == EV_FUSED_OZAKI6)
+                                             ? "the ozaki fused variants need complex128 amplitudes"
                                              : "fused mode needs complex64 amplitudes");
   if (mode < EV_MODE_EXACT || mode > EV_MODE_FUSED)
     return fail(EV_ERR_INVALID_ARGUMENT, "unknown run mode %d", mode);

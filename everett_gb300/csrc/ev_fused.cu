@@ -22,6 +22,8 @@
 //   EV_FUSED_OZAKI   complex128; k = 5, each f64 as seven 8-bit FP16 digits
 //                    (kind::f16), exact digit-pair sums in TMEM, int64
 //                    recombination (ev_ozaki.cuh, k_fused_oz below)
+//   EV_FUSED_OZAKI6  the same with six digits (47 bits per value): a quarter
+//                    fewer MMAs, one digit slice and one diagonal less
 // The complex64 tensor-core kernel stages 128 rows per step: loads gather the rows
 // (addresses contiguous for at least 128 amplitudes because the row qubits
 // are the lowest qubits outside F), split into hi/lo and write the A operand
@@ -863,14 +865,15 @@ __global__ void __launch_bounds__(kTmaThreads)
 constexpr int kOzWorkers = 512;                // 16 worker warps
 constexpr int kOzThreads = kOzWorkers + 32;    // and the MMA warp
 
+template <int ND>
 struct OzShape {
   static constexpr int K = oz::kK;
   static constexpr int A_SLICE = kRows * K * 2;  // 128 rows x 64 FP16
   static constexpr int B_SLICE = K * K * 2;      // 64 x 64 FP16
-  static constexpr int SMEM = oz::kDigits * (A_SLICE + B_SLICE) + 1024;
+  static constexpr int SMEM = ND * (A_SLICE + B_SLICE) + 1024;
   static constexpr int TMEM_COLS = 512;
-  static constexpr int HALF_COLS = oz::kDigits * 32;  // TMEM columns (and B rows) per half
-  static constexpr int BLOB = oz::kDigits * B_SLICE + K * 4;  // B slices, column exponents
+  static constexpr int HALF_COLS = ND * 32;  // TMEM columns (and B rows) per half
+  static constexpr int BLOB = ND * B_SLICE + K * 4;  // B slices, column exponents
 };
 
 __device__ __forceinline__ uint32_t hsub2_bits(uint32_t a, uint32_t b) {
@@ -891,21 +894,32 @@ __device__ __forceinline__ uint32_t oz_byte_digits(uint32_t w0, uint32_t w1) {
   return hsub2_bits((t & 0x00FF00FFu) | 0x64006400u, 0x64806480u);
 }
 
-// The seven FP16 digits of two biased fixed-point values (b = M + kBias),
+// The ND FP16 digits of two biased fixed-point values (b = M + kBias),
 // packed per slice as one 32-bit word [first | second << 16].
-__device__ __forceinline__ void oz_digits(uint64_t b0, uint64_t b1, uint32_t w[7]) {
+template <int ND>
+__device__ __forceinline__ void oz_digits(uint64_t b0, uint64_t b1, uint32_t w[ND]) {
   const uint32_t l0 = uint32_t(b0), h0 = uint32_t(b0 >> 32);
   const uint32_t l1 = uint32_t(b1), h1 = uint32_t(b1 >> 32);
-  // top digits X0 in [-128, 128]: f16 bits 0x6600 + X0 are 1536 + X0
-  const uint32_t t0 = uint32_t(0x6600 + (int32_t(h0) >> 16));
-  const uint32_t t1 = uint32_t(0x6600 + (int32_t(h1) >> 16));
+  // top digits X0 in [-128, 128] (bits 48.. for seven digits, 40.. for
+  // six): f16 bits 0x6600 + X0 are 1536 + X0
+  constexpr int tsh = ND == 7 ? 16 : 8;
+  const uint32_t t0 = uint32_t(0x6600 + (int32_t(h0) >> tsh));
+  const uint32_t t1 = uint32_t(0x6600 + (int32_t(h1) >> tsh));
   w[0] = hsub2_bits(__byte_perm(t0, t1, 0x5410), 0x66006600u);
-  w[1] = oz_byte_digits<1>(h0, h1);
-  w[2] = oz_byte_digits<0>(h0, h1);
-  w[3] = oz_byte_digits<3>(l0, l1);
-  w[4] = oz_byte_digits<2>(l0, l1);
-  w[5] = oz_byte_digits<1>(l0, l1);
-  w[6] = oz_byte_digits<0>(l0, l1);
+  if constexpr (ND == 7) {
+    w[1] = oz_byte_digits<1>(h0, h1);
+    w[2] = oz_byte_digits<0>(h0, h1);
+    w[3] = oz_byte_digits<3>(l0, l1);
+    w[4] = oz_byte_digits<2>(l0, l1);
+    w[5] = oz_byte_digits<1>(l0, l1);
+    w[6] = oz_byte_digits<0>(l0, l1);
+  } else {
+    w[1] = oz_byte_digits<0>(h0, h1);
+    w[2] = oz_byte_digits<3>(l0, l1);
+    w[3] = oz_byte_digits<2>(l0, l1);
+    w[4] = oz_byte_digits<1>(l0, l1);
+    w[5] = oz_byte_digits<0>(l0, l1);
+  }
 }
 
 __device__ __forceinline__ void mma_f16(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t idesc,
@@ -927,6 +941,7 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t v[8]) {
 // the row (two groups of four amplitudes, [re, im]) and becomes their biased
 // fixed-point values; returns the row's largest exponent (over its four
 // threads: lanes l, l + 8, l + 16, l + 24).
+template <int ND>
 __device__ __forceinline__ int oz_prepare(uint64_t (&v)[2][4][2], int* err) {
   int em = 0;
 #pragma unroll
@@ -944,8 +959,8 @@ __device__ __forceinline__ int oz_prepare(uint64_t (&v)[2][4][2], int* err) {
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int c = 0; c < 2; ++c)
-        v[gi][i][c] =
-            uint64_t(oz::fixed55(uint32_t(v[gi][i][c] >> 32), uint32_t(v[gi][i][c]), em)) + oz::kBias;
+        v[gi][i][c] = uint64_t(oz::fixed<ND>(uint32_t(v[gi][i][c] >> 32), uint32_t(v[gi][i][c]), em)) +
+                      oz::Fmt<ND>::kBias;
   return em;
 }
 
@@ -956,10 +971,11 @@ __device__ __forceinline__ void oz_load(const double2* p, uint64_t (&v)[2]) {
   v[1] = uint64_t(__double_as_longlong(a.y));
 }
 
+template <int ND>
 __global__ void __launch_bounds__(kOzThreads, 1)
     k_fused_oz(double2* __restrict__ s, const FusedDesc* __restrict__ gd,
                const unsigned char* __restrict__ bmat, int* __restrict__ err) {
-  using Sh = OzShape;
+  using Sh = OzShape<ND>;
   constexpr int K = Sh::K;
   extern __shared__ unsigned char smem_raw[];
   __shared__ FusedDesc d;
@@ -972,7 +988,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   unsigned char* sm = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   unsigned char* a_sl = sm;
-  unsigned char* b_sl = sm + oz::kDigits * Sh::A_SLICE;
+  unsigned char* b_sl = sm + ND * Sh::A_SLICE;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
   for (int i = tid; i < int(sizeof(FusedDesc) / 8); i += blockDim.x)
@@ -980,12 +996,12 @@ __global__ void __launch_bounds__(kOzThreads, 1)
   {
     // blob [slice j][column n][k] -> B row (n / 32) * 224 + 32 j + n mod 32
     const uint16_t* src = reinterpret_cast<const uint16_t*>(bmat);
-    for (int e = tid; e < oz::kDigits * K * K; e += blockDim.x) {
+    for (int e = tid; e < ND * K * K; e += blockDim.x) {
       const int j = e / (K * K), n = (e / K) % K, k = e % K;
       const int brow = (n >> 5) * Sh::HALF_COLS + 32 * j + (n & 31);
-      *reinterpret_cast<uint16_t*>(b_sl + sw128_off(brow, k, oz::kDigits * K, 2)) = src[e];
+      *reinterpret_cast<uint16_t*>(b_sl + sw128_off(brow, k, ND * K, 2)) = src[e];
     }
-    const int* fe = reinterpret_cast<const int*>(bmat + oz::kDigits * Sh::B_SLICE);
+    const int* fe = reinterpret_cast<const int*>(bmat + ND * Sh::B_SLICE);
     for (int n = tid; n < K; n += blockDim.x) fexp[n] = fe[n];
   }
   if (tid == 0) {
@@ -1023,8 +1039,8 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 #pragma unroll 1
         for (int h = 0; h < 2; ++h) {
 #pragma unroll 1
-          for (int i = 0; i < oz::kDigits; ++i) {
-            const uint32_t n = uint32_t(32 * (oz::kDigits - i));
+          for (int i = 0; i < ND; ++i) {
+            const uint32_t n = uint32_t(32 * (ND - i));
             // f32 accumulate, FP16 A and B, K-major, N, M = 128
             const uint32_t idesc = (1u << 4) | ((n >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
             const uint64_t a = ad + uint64_t(i * (Sh::A_SLICE >> 4));
@@ -1077,7 +1093,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     for (int gi = 0; gi < 2; ++gi)
 #pragma unroll
       for (int i = 0; i < 4; ++i) oz_load(s + (rb | d.ftab[4 * (pq + 4 * gi) + i]), b[gi][i]);
-    em = oz_prepare(b, err);
+    em = oz_prepare<ND>(b, err);
   }
   for (int par = 0; step < d.nsteps && ok; step += gridDim.x, par ^= 1) {
     // A slices of this step from the prepared digits
@@ -1085,11 +1101,11 @@ __global__ void __launch_bounds__(kOzThreads, 1)
     for (int gi = 0; gi < 2; ++gi) {
       const int g = pq + 4 * gi;  // reals 8g..8g+7: chunk g of the row's 128-byte line
       const uint32_t o = prsw + ((uint32_t(g) ^ prx) << 4);
-      uint32_t w[4][7];
+      uint32_t w[4][ND];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) oz_digits(b[gi][i][0], b[gi][i][1], w[i]);
+      for (int i = 0; i < 4; ++i) oz_digits<ND>(b[gi][i][0], b[gi][i][1], w[i]);
 #pragma unroll
-      for (int sl = 0; sl < oz::kDigits; ++sl)
+      for (int sl = 0; sl < ND; ++sl)
         *reinterpret_cast<uint4*>(a_sl + sl * Sh::A_SLICE + o) =
             make_uint4(w[0][sl], w[1][sl], w[2][sl], w[3][sl]);
     }
@@ -1123,7 +1139,7 @@ __global__ void __launch_bounds__(kOzThreads, 1)
                    : "memory");
     }
     // prepare the next step while the tensor core works
-    if (nstep < d.nsteps) em = oz_prepare(b, err);
+    if (nstep < d.nsteps) em = oz_prepare<ND>(b, err);
     if (!mbar_wait(&bar[half], phase, kWaitLimit)) {
       ok = false;
       atomicExch(err, 1);
@@ -1137,25 +1153,29 @@ __global__ void __launch_bounds__(kOzThreads, 1)
       const uint32_t ta = lane_tmem + col0 + uint32_t(c0);
       int64_t acc[8];
       {
-        uint32_t v[oz::kDigits][8];
+        uint32_t v[ND][8];
 #pragma unroll
-        for (int dg = 0; dg < oz::kDigits; ++dg) tmem_ld8(ta + uint32_t(32 * dg), v[dg]);
+        for (int dg = 0; dg < ND; ++dg) tmem_ld8(ta + uint32_t(32 * dg), v[dg]);
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
         for (int c = 0; c < 8; ++c) {
           int32_t g3, g2;
           oz::combine_hi(__uint_as_float(v[0][c]), __uint_as_float(v[1][c]),
                          __uint_as_float(v[2][c]), __uint_as_float(v[3][c]), g3, g2);
-          acc[c] = oz::combine_g(g3, g2,
-                                 oz::combine_lo(__uint_as_float(v[4][c]), __uint_as_float(v[5][c]),
-                                                __uint_as_float(v[6][c])));
+          if constexpr (ND == 7)
+            acc[c] = oz::combine_g(g3, g2,
+                                   oz::combine_lo(__uint_as_float(v[4][c]), __uint_as_float(v[5][c]),
+                                                  __uint_as_float(v[6][c])));
+          else
+            acc[c] = oz::combine_g6(g3, g2,
+                                    oz::combine_lo6(__uint_as_float(v[4][c]), __uint_as_float(v[5][c])));
         }
       }
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int n = half * 32 + (part & 1) * 16 + c0 + 2 * j;
-        const double re = oz::scaled(acc[2 * j], rem + fexp[n] - oz::kPow2Bias);
-        const double im = oz::scaled(acc[2 * j + 1], rem + fexp[n + 1] - oz::kPow2Bias);
+        const double re = oz::scaled(acc[2 * j], rem + fexp[n] - oz::Fmt<ND>::kPow2Bias);
+        const double im = oz::scaled(acc[2 * j + 1], rem + fexp[n + 1] - oz::Fmt<ND>::kPow2Bias);
         __stcs(s + (rbase | d.ftab[n >> 1]), make_double2(re, im));
       }
     }
@@ -1254,6 +1274,7 @@ static int int_of_f16(uint16_t h) {
 // of W) is scaled by its own largest biased exponent F_n and written as seven
 // FP16 digit slices [N][K] (slice 0 = most significant), followed by the 64
 // exponents F_n (ev_ozaki.cuh).
+template <int ND>
 static void oz_slice_columns(const double* Wt, std::vector<unsigned char>* out) {
   constexpr int K = oz::kK;
   // FP16 bits of every digit value, -128..128
@@ -1262,9 +1283,9 @@ static void oz_slice_columns(const double* Wt, std::vector<unsigned char>* out) 
     for (int v = -128; v <= 128; ++v) t[size_t(v + 128)] = f16_of_int(v);
     return t;
   }();
-  out->assign(OzShape::BLOB, 0);
+  out->assign(OzShape<ND>::BLOB, 0);
   uint16_t* sl = reinterpret_cast<uint16_t*>(out->data());
-  int32_t* fe = reinterpret_cast<int32_t*>(out->data() + oz::kDigits * OzShape::B_SLICE);
+  int32_t* fe = reinterpret_cast<int32_t*>(out->data() + ND * OzShape<ND>::B_SLICE);
   for (int n = 0; n < K; ++n) {
     int E = 0;
     for (int k = 0; k < K; ++k) {
@@ -1276,16 +1297,15 @@ static void oz_slice_columns(const double* Wt, std::vector<unsigned char>* out) 
     for (int k = 0; k < K; ++k) {
       uint64_t u;
       std::memcpy(&u, &Wt[size_t(n) * K + k], 8);
-      const int64_t M = oz::fixed55(uint32_t(u >> 32), uint32_t(u), E);
-      const uint64_t b = uint64_t(M) + oz::kBias;  // low bytes: digits 6..1 plus 128
+      const int64_t M = oz::fixed<ND>(uint32_t(u >> 32), uint32_t(u), E);
       uint16_t* col = sl + size_t(n) * K + k;
-      col[0] = f16_tab[size_t((int32_t(uint32_t(b >> 32)) >> 16) + 128)];
-      for (int i = 1; i < oz::kDigits; ++i)
-        col[size_t(i) * K * K] = f16_tab[size_t((b >> (8 * (oz::kDigits - 1 - i))) & 0xFFu)];
+      for (int i = 0; i < ND; ++i)
+        col[size_t(i) * K * K] = f16_tab[size_t(oz::digit_of<ND>(M, i) + 128)];
     }
   }
 }
 
+template <int ND>
 static void build_bmat_oz(const Block& b, std::vector<unsigned char>* out) {
   const int D = 1 << b.F.size(), K = 2 * D;
   std::vector<double> Wt(size_t(K) * K);
@@ -1297,19 +1317,20 @@ static void build_bmat_oz(const Block& b, std::vector<unsigned char>* out) {
       Wt[size_t(2 * a + 1) * K + 2 * f] = u.imag();
       Wt[size_t(2 * a + 1) * K + 2 * f + 1] = u.real();
     }
-  oz_slice_columns(Wt.data(), out);
+  oz_slice_columns<ND>(Wt.data(), out);
 }
 
+template <int ND>
 static int launch_oz(ev_state* s, const FusedDesc* dd, const unsigned char* db, uint64_t nsteps,
                      int* derr) {
-  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_fused_oz)));
+  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_fused_oz<ND>)));
   uint64_t grid = uint64_t(s->num_sms);  // one CTA per SM (shared memory and TMEM)
   if (grid > nsteps) grid = nsteps;
   s->tc_ctas_per_sm = 1;
   if (debug_enabled())
-    fprintf(stderr, "[ev] k_fused_oz smem %d per CTA, grid %llu\n", OzShape::SMEM,
+    fprintf(stderr, "[ev] k_fused_oz<%d> smem %d per CTA, grid %llu\n", ND, OzShape<ND>::SMEM,
             (unsigned long long)grid);
-  k_fused_oz<<<unsigned(grid), kOzThreads, OzShape::SMEM, s->stream>>>(
+  k_fused_oz<ND><<<unsigned(grid), kOzThreads, OzShape<ND>::SMEM, s->stream>>>(
       static_cast<double2*>(s->amps), dd, db, derr);
   EV_CUDA(cudaGetLastError());
   return EV_OK;
@@ -1396,7 +1417,8 @@ int fused_width(int variant, int kbits) {
   int k = kbits > 0 ? kbits : default_fused_bits();
   if (k > 6) k = 6;
   if (k < 1) k = 1;
-  if (variant == EV_FUSED_TF32X3 || variant == EV_FUSED_OZAKI) return 5;
+  if (variant == EV_FUSED_TF32X3 || variant == EV_FUSED_OZAKI || variant == EV_FUSED_OZAKI6)
+    return 5;
   if (variant == EV_FUSED_BF16X3) return k >= 6 ? 6 : 5;
   return k;
 }
@@ -1405,12 +1427,13 @@ int fused_width(int variant, int kbits) {
 // images go into the blob.
 static int plan_fused(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, int kbits,
                       int variant, PlanBlob* blob, std::vector<SegStep>* out) {
-  if (variant < EV_FUSED_TF32X3 || variant > EV_FUSED_OZAKI)
+  if (variant < EV_FUSED_TF32X3 || variant > EV_FUSED_OZAKI6)
     return fail(EV_ERR_INVALID_ARGUMENT, "unknown fused variant %d", variant);
-  if ((variant == EV_FUSED_OZAKI) != (s->dtype == EV_C128))
+  const bool ozaki = variant == EV_FUSED_OZAKI || variant == EV_FUSED_OZAKI6;
+  if (ozaki != (s->dtype == EV_C128))
     return fail(EV_ERR_INVALID_ARGUMENT,
-                variant == EV_FUSED_OZAKI ? "the ozaki fused variant needs a complex128 state"
-                                          : "this fused variant needs a complex64 state");
+                ozaki ? "the ozaki fused variants need a complex128 state"
+                      : "this fused variant needs a complex64 state");
   const int n = int(s->n);
   const int k = fused_width(variant, kbits);
   // registers too small for 128-row steps run through the tile pass
@@ -1420,13 +1443,14 @@ static int plan_fused(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t
   // the measured comparison in the design notes) or the warp-specialised
   // TMA-staged pipeline (EV_FUSED_STAGING=tma), read when a run is planned.
   const char* staging = getenv("EV_FUSED_STAGING");
-  const bool use_tma = staging != nullptr && std::strcmp(staging, "tma") == 0 &&
-                       variant != EV_FUSED_OZAKI;
+  const bool use_tma = staging != nullptr && std::strcmp(staging, "tma") == 0 && !ozaki;
   std::vector<Block> blocks = fuse_ops(c, first, last, n, k);
   std::vector<unsigned char> mat;
   for (const Block& b : blocks) {
     if (variant == EV_FUSED_OZAKI) {
-      build_bmat_oz(b, &mat);
+      build_bmat_oz<7>(b, &mat);
+    } else if (variant == EV_FUSED_OZAKI6) {
+      build_bmat_oz<6>(b, &mat);
     } else if (tc) {
       build_bmat(b, variant, &mat);
     } else {
@@ -1459,7 +1483,8 @@ int launch_fused_step(ev_state* s, const SegStep& st, const unsigned char* dblob
   s->launches += 1;
   const uint64_t nsteps = st.count;
   const bool tma = st.tma != 0;
-  if (st.variant == EV_FUSED_OZAKI) return launch_oz(s, dd, dm, nsteps, derr);
+  if (st.variant == EV_FUSED_OZAKI) return launch_oz<7>(s, dd, dm, nsteps, derr);
+  if (st.variant == EV_FUSED_OZAKI6) return launch_oz<6>(s, dd, dm, nsteps, derr);
   if (st.variant == EV_FUSED_TF32X3)
     return tma ? launch_tma<5, EV_FUSED_TF32X3, 3>(s, dd, dm, nsteps, derr)
                : launch_tc<5, EV_FUSED_TF32X3>(s, dd, dm, nsteps, derr);
@@ -1486,15 +1511,16 @@ int launch_fused_step(ev_state* s, const SegStep& st, const unsigned char* dblob
 // as f32 and recombined with the device's own routines -- diagonal by
 // diagonal, and checked against the kernel's grouped form (false if the two
 // differ for any output).
+template <int ND>
 static bool oz_gemm_host(const double* x, uint64_t rows, const double* W, double* y) {
   constexpr int K = oz::kK;
   std::vector<double> Wt(size_t(K) * K);
   for (int k = 0; k < K; ++k)
     for (int n = 0; n < K; ++n) Wt[size_t(n) * K + k] = W[size_t(k) * K + n];
   std::vector<unsigned char> img;
-  oz_slice_columns(Wt.data(), &img);
+  oz_slice_columns<ND>(Wt.data(), &img);
   const uint16_t* sl = reinterpret_cast<const uint16_t*>(img.data());
-  const int32_t* fe = reinterpret_cast<const int32_t*>(img.data() + oz::kDigits * OzShape::B_SLICE);
+  const int32_t* fe = reinterpret_cast<const int32_t*>(img.data() + ND * OzShape<ND>::B_SLICE);
   for (uint64_t r = 0; r < rows; ++r) {
     const double* xr = x + r * K;
     int E = 0;
@@ -1503,16 +1529,16 @@ static bool oz_gemm_host(const double* x, uint64_t rows, const double* W, double
       std::memcpy(&u, &xr[k], 8);
       E = std::max(E, oz::exp_of(uint32_t(u >> 32)));
     }
-    int X[K][oz::kDigits];
+    int X[K][ND];
     for (int k = 0; k < K; ++k) {
       uint64_t u;
       std::memcpy(&u, &xr[k], 8);
-      const int64_t M = oz::fixed55(uint32_t(u >> 32), uint32_t(u), E);
-      for (int i = 0; i < oz::kDigits; ++i) X[k][i] = oz::digit(M, i);
+      const int64_t M = oz::fixed<ND>(uint32_t(u >> 32), uint32_t(u), E);
+      for (int i = 0; i < ND; ++i) X[k][i] = oz::digit_of<ND>(M, i);
     }
     for (int n = 0; n < K; ++n) {
-      float D[oz::kDigits];
-      for (int dg = 0; dg < oz::kDigits; ++dg) {
+      float D[ND];
+      for (int dg = 0; dg < ND; ++dg) {
         int64_t sum = 0;
         for (int i = 0; i <= dg; ++i)
           for (int k = 0; k < K; ++k)
@@ -1520,15 +1546,15 @@ static bool oz_gemm_host(const double* x, uint64_t rows, const double* W, double
         D[dg] = float(sum);  // |sum| < 2^24: exact
       }
       int64_t acc = 0;
-      oz::accumulate<0>(acc, D[0]);
-      oz::accumulate<1>(acc, D[1]);
-      oz::accumulate<2>(acc, D[2]);
-      oz::accumulate<3>(acc, D[3]);
-      oz::accumulate<4>(acc, D[4]);
-      oz::accumulate<5>(acc, D[5]);
-      oz::accumulate<6>(acc, D[6]);
-      if (oz::combine7(D) != acc) return false;  // the kernel's grouped form
-      y[r * K + n] = oz::scaled(acc, E + fe[n] - oz::kPow2Bias);
+      oz::accumulate_nd<ND, 0>(acc, D[0]);
+      oz::accumulate_nd<ND, 1>(acc, D[1]);
+      oz::accumulate_nd<ND, 2>(acc, D[2]);
+      oz::accumulate_nd<ND, 3>(acc, D[3]);
+      oz::accumulate_nd<ND, 4>(acc, D[4]);
+      oz::accumulate_nd<ND, 5>(acc, D[5]);
+      if constexpr (ND == 7) oz::accumulate_nd<ND, 6>(acc, D[6]);
+      if (oz::combine_nd<ND>(D) != acc) return false;  // the kernel's grouped form
+      y[r * K + n] = oz::scaled(acc, E + fe[n] - oz::Fmt<ND>::kPow2Bias);
     }
   }
   return true;
@@ -1543,9 +1569,17 @@ int plan_segment(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last
 }  // namespace ev
 
 extern "C" int ev_ozaki_gemm_host(const double* x, uint64_t rows, const double* w, double* y) {
+  return ev_ozaki_gemm_host_digits(x, rows, w, y, 7);
+}
+
+extern "C" int ev_ozaki_gemm_host_digits(const double* x, uint64_t rows, const double* w, double* y,
+                                         int32_t digits) {
   ev::clear_error();
   if (!x || !w || !y) return ev::fail(EV_ERR_INVALID_ARGUMENT, "ev_ozaki_gemm_host: null argument");
-  if (!ev::oz_gemm_host(x, rows, w, y))
+  if (digits != 6 && digits != 7)
+    return ev::fail(EV_ERR_INVALID_ARGUMENT, "ev_ozaki_gemm_host: %d digits (6 or 7)", digits);
+  const bool ok = digits == 7 ? ev::oz_gemm_host<7>(x, rows, w, y) : ev::oz_gemm_host<6>(x, rows, w, y);
+  if (!ok)
     return ev::fail(EV_ERR_INVALID_ARGUMENT, "ev_ozaki_gemm_host: grouped recombination differs");
   return EV_OK;
 }

@@ -41,6 +41,55 @@ namespace oz {
 constexpr int kDigits = 7;  // 8-bit digits per value (56 bits)
 constexpr int kK = 64;      // reals per row: 32 amplitudes of a 5-qubit block
 
+// The two digit counts the engine runs.  Seven digits (EV_FUSED_OZAKI) carry
+// 55 bits below each row's (column's) maximum; six digits
+// (EV_FUSED_OZAKI6) carry 47 bits, M = trunc(x * 2^(1069 - E)) with
+// |M| < 2^47, drop the diagonals d >= 6 and recombine
+//     acc = D0 2^32 + D1 2^24 + D2 2^16 + D3 2^8 + D4 + round(D5 2^-8),
+// |acc| < 2^53, y = acc * 2^(E + F_n - 2090).  Every diagonal sum stays below
+// 6 * 64 * 2^14 < 2^24, so the f32 accumulator still holds it exactly.  The
+// error per output, in units u = 2^(E + F_n - 2090) (2^-44 of the largest
+// value times the largest column entry): 0.5 from D5's rounding, the dropped
+// pairs (at most ~113 u, ~2 u for digits of random sign), the truncation of
+// x and W (32 u each at most, ~4 u typical) and the final rounding -- 256
+// times the seven-digit form's, about 7e-14 of the row's largest value.
+template <int ND>
+struct Fmt;
+template <>
+struct Fmt<7> {
+  static constexpr int kBits = 55;                  // |M| < 2^55
+  static constexpr uint64_t kBias = 0x808080808080ull;
+  static constexpr int kPow2Bias = 2098;
+};
+template <>
+struct Fmt<6> {
+  static constexpr int kBits = 47;                  // |M| < 2^47
+  static constexpr uint64_t kBias = 0x8080808080ull;
+  static constexpr int kPow2Bias = 2090;
+};
+
+// M = trunc(x * 2^(1022 + kBits - E)) for the f64 with the given bit halves
+// (E the row's largest biased exponent): 1077 - E for seven digits, 1069 - E
+// for six.  Zero, subnormal values and values 2^53 times below the maximum
+// give 0.
+template <int ND>
+__host__ __device__ __forceinline__ int64_t fixed(uint32_t hi, uint32_t lo, int E) {
+  const int e = int((hi >> 20) & 0x7FFu);
+  const int sh = E - e + (53 - Fmt<ND>::kBits);
+  if (e == 0 || sh >= 53) return 0;
+  const uint64_t mant = (uint64_t((hi & 0xFFFFFu) | 0x100000u) << 32) | lo;
+  const uint64_t m = sh < 0 ? mant << (-sh) : mant >> sh;
+  return (hi >> 31) ? -int64_t(m) : int64_t(m);
+}
+
+// Digit i (0 = most significant) of M in balanced base 256.
+template <int ND>
+__host__ __device__ __forceinline__ int digit_of(int64_t M, int i) {
+  const uint64_t b = uint64_t(M) + Fmt<ND>::kBias;
+  if (i == 0) return int(int64_t(b) >> (8 * (ND - 1)));
+  return int((b >> (8 * (ND - 1 - i))) & 0xFFu) - 128;
+}
+
 // M = trunc(x * 2^(1077 - E)) for the f64 with the given bit halves, where E
 // is the largest biased exponent of its row (or column).  Zero, subnormal
 // values and values 2^53 times below the maximum give 0.
@@ -141,6 +190,51 @@ __host__ __device__ __forceinline__ int64_t combine7(const float D[7]) {
   int32_t g3, g2;
   combine_hi(D[0], D[1], D[2], D[3], g3, g2);
   return combine_g(g3, g2, combine_lo(D[4], D[5], D[6]));
+}
+
+// acc += the contribution of diagonal d of an ND-digit product whose f32 sum
+// is D (the forms of accumulate<d> above, weights 2^(8 (ND - 2 - d))).
+template <int ND, int d>
+__host__ __device__ __forceinline__ void accumulate_nd(int64_t& acc, float D) {
+  if constexpr (d < 4) {
+    const int32_t v = int32_t(f32_bits(add_rn(D, f32_of(0x4B400000u))) - 0x4B400000u);
+    acc += int64_t(v) * (int64_t(1) << (8 * (ND - 2 - d)));
+  } else if constexpr (d < ND - 1) {
+#ifdef __CUDA_ARCH__
+    const int32_t v = __float2int_rn(D);
+#else
+    const int32_t v = int32_t(D);
+#endif
+    acc += int64_t(v) * (int64_t(1) << (8 * (ND - 2 - d)));
+  } else {
+    const int32_t v = int32_t(f32_bits(add_rn(D, f32_of(0x4F400000u))) - 0x4F400000u);
+    acc += int64_t(v);
+  }
+}
+
+// The six-digit grouped form: (g3, g2) from D0..D3 as combine_hi forms them,
+// g0 = I4 + round(D5 / 2^8) (< 2^23), acc = 2^24 g3 + 2^8 g2 + g0.
+__host__ __device__ __forceinline__ int32_t combine_lo6(float D4, float D5) {
+  const uint32_t b5 = f32_bits(add_rn(D5, f32_of(0x4F400000u)));
+#ifdef __CUDA_ARCH__
+  const uint32_t i4 = uint32_t(__float2int_rn(D4));
+#else
+  const uint32_t i4 = uint32_t(int32_t(D4));
+#endif
+  return int32_t(i4 + b5 - 0x4F400000u);
+}
+__host__ __device__ __forceinline__ int64_t combine_g6(int32_t g3, int32_t g2, int32_t g0) {
+  return (int64_t(g3) << 24) + (int64_t(g2) << 8) + int64_t(g0);
+}
+
+template <int ND>
+__host__ __device__ __forceinline__ int64_t combine_nd(const float* D) {
+  int32_t g3, g2;
+  combine_hi(D[0], D[1], D[2], D[3], g3, g2);
+  if constexpr (ND == 7)
+    return combine_g(g3, g2, combine_lo(D[4], D[5], D[6]));
+  else
+    return combine_g6(g3, g2, combine_lo6(D[4], D[5]));
 }
 
 // acc * 2^pow2 as an f64 (|acc| < 2^62), rounded to nearest even once,

@@ -134,7 +134,7 @@ int run_single(ev_server* s, Request* r, std::vector<uint8_t>* classical) {
   o.mode = s->opts.mode;
   o.variant = s->opts.variant;
   // a fused arithmetic of the other amplitude type runs the tile pass instead
-  if (o.mode == EV_MODE_FUSED && (o.variant == EV_FUSED_OZAKI) != (o.dtype == EV_C128))
+  if (o.mode == EV_MODE_FUSED && (o.variant == EV_FUSED_OZAKI || o.variant == EV_FUSED_OZAKI6) != (o.dtype == EV_C128))
     o.mode = EV_MODE_TILED;
   const ev_circuit c = circuit_of(*r);
   classical->assign(r->ncl ? r->ncl : 1, 0);

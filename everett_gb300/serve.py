@@ -49,7 +49,7 @@ class Result:
 
 _MODES = {"exact": N.MODE_EXACT, "tiled": N.MODE_TILED, "fused": N.MODE_FUSED}
 _VARIANTS = {"tf32x3": N.FUSED_TF32X3, "bf16x3": N.FUSED_BF16X3, "fp32": N.FUSED_FP32,
-             "ozaki": N.FUSED_OZAKI}
+             "ozaki": N.FUSED_OZAKI, "ozaki6": N.FUSED_OZAKI6}
 
 
 class Server:

@@ -93,20 +93,24 @@ enum {
                         pass per run; same per-amplitude arithmetic        */
   EV_MODE_FUSED = 2  /* runs of ops fused on the host (f64) into dense
                         k-qubit unitaries, one HBM pass each; complex64
-                        with the variants below but EV_FUSED_OZAKI, which
-                        is the complex128 one                             */
+                        with the variants below but EV_FUSED_OZAKI and
+                        EV_FUSED_OZAKI6, the complex128 ones              */
 };
 /* Arithmetic of a fused k-qubit unitary (EV_MODE_FUSED). */
 enum {
   EV_FUSED_TF32X3 = 0, /* tensor cores, split TF32 products, f32 accumulate */
   EV_FUSED_BF16X3 = 1, /* tensor cores, split BF16 products, f32 accumulate */
   EV_FUSED_FP32 = 2,   /* CUDA cores, f32 complex multiply-add              */
-  EV_FUSED_OZAKI = 3   /* complex128: tensor cores, each f64 as seven 8-bit
+  EV_FUSED_OZAKI = 3,  /* complex128: tensor cores, each f64 as seven 8-bit
                           digits in FP16 (per-row / per-column scale), digit
                           products summed exactly in f32, recombined in
                           int64 (the Ozaki scheme); k = 5; a NaN or an
                           infinity in the state makes the run return
                           EV_ERR_INVALID_ARGUMENT                          */
+  EV_FUSED_OZAKI6 = 4  /* complex128: the same with six digits (47 bits per
+                          value below its row's or column's maximum): fewer
+                          MMAs and digit slices, ~7e-14 of a row's largest
+                          value per pass instead of ~3e-16                */
 };
 typedef struct ev_run_options {
   int32_t dtype;     /* EV_C128 or EV_C64                                  */
@@ -485,6 +489,9 @@ int ev_softfp_check(uint64_t seed, uint64_t count, uint64_t* mismatches);
  * kernel's own slicing and recombination routines.  A check of the build,
  * for tests; no reference counterpart. */
 int ev_ozaki_gemm_host(const double* x, uint64_t rows, const double* w, double* y);
+/* The same for the six-digit (digits = 6) or seven-digit (7) pass. */
+int ev_ozaki_gemm_host_digits(const double* x, uint64_t rows, const double* w, double* y,
+                              int32_t digits);
 /* max_j |self_j - other_j| over two states of equal size, either amplitude
  * type (the max amplitude error of a complex64 run against complex128). */
 int ev_max_abs_diff(const ev_state* self, const ev_state* other, double* out);

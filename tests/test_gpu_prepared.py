@@ -51,6 +51,7 @@ def plain(state, c, seed, **kw):
     ("complex64", "fused", {"variant": "tf32x3"}),
     ("complex64", "fused", {"variant": "fp32", "tile_bits": 4}),
     ("complex128", "fused", {"variant": "ozaki"}),
+    ("complex128", "fused", {"variant": "ozaki6"}),
 ])
 def test_prepared_equals_run(gpu, dtype, mode, kw):
     n = 14
