@@ -240,8 +240,11 @@ __device__ void batch_measure(V* tile, uint32_t size, int q, uint32_t cbit, doub
   __syncthreads();
 }
 
-template <typename V>
-__global__ void __launch_bounds__(512, 2) k_batch(BatchArgs a, int kmax) {
+// Compiled per block size: 256-thread CTAs, three of which fit an SM's
+// shared memory with the default tile, get 85 registers a thread; 512-thread
+// CTAs (two per SM) 64.
+template <typename V, int NT>
+__global__ void __launch_bounds__(NT, NT == 256 ? 3 : 2) k_batch(BatchArgs a, int kmax) {
   extern __shared__ __align__(16) unsigned char sm[];
   V* tile = reinterpret_cast<V*>(sm);
   uint64_t* offs = reinterpret_cast<uint64_t*>(sm + (sizeof(V) << kmax));
@@ -762,23 +765,27 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
   EV_CUDA(cudaEventRecord(A.e0, A.stream));
   k_batch_uniforms<<<unsigned((count + 127) / 128), 128, 0, A.stream>>>(args.circs, count, args.uni);
   int per_sm = 0;
-  if (dtype == EV_C128) {
-    EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_batch<double2>)));
-    EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<double2>, threads, smem));
-  } else {
-    EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_batch<float2>)));
-    EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<float2>, threads, smem));
-  }
+  const void* kfn = dtype == EV_C128
+                        ? (threads == 256 ? reinterpret_cast<const void*>(k_batch<double2, 256>)
+                                          : reinterpret_cast<const void*>(k_batch<double2, 512>))
+                        : (threads == 256 ? reinterpret_cast<const void*>(k_batch<float2, 256>)
+                                          : reinterpret_cast<const void*>(k_batch<float2, 512>));
+  EV_TRY(prepare_smem_kernel(kfn));
+  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, smem));
   if (per_sm < 1) return fail(EV_ERR_INVALID_ARGUMENT, "batch: configuration does not fit an SM");
   // every CTA of the persistent grid must be resident (items wait on each other)
   const unsigned grid = unsigned(sms * per_sm);
   if (debug_enabled())
     fprintf(stderr, "[ev] k_batch dtype %d tile %d threads %d smem %zu: %d CTAs/SM, %zu items\n",
             dtype, kmax, threads, smem, per_sm, q.size());
-  if (dtype == EV_C128)
-    k_batch<double2><<<grid, threads, smem, A.stream>>>(args, kmax);
+  if (dtype == EV_C128 && threads == 256)
+    k_batch<double2, 256><<<grid, threads, smem, A.stream>>>(args, kmax);
+  else if (dtype == EV_C128)
+    k_batch<double2, 512><<<grid, threads, smem, A.stream>>>(args, kmax);
+  else if (threads == 256)
+    k_batch<float2, 256><<<grid, threads, smem, A.stream>>>(args, kmax);
   else
-    k_batch<float2><<<grid, threads, smem, A.stream>>>(args, kmax);
+    k_batch<float2, 512><<<grid, threads, smem, A.stream>>>(args, kmax);
   EV_CUDA(cudaGetLastError());
   EV_CUDA(cudaEventRecord(A.e1, A.stream));
   // results: shots | expz, one copy down
