@@ -117,6 +117,46 @@ struct FF {
   __device__ __forceinline__ double value() const { return f2d_exact(hi) + f2d_exact(lo); }
 };
 
+// RN(hi + lo) as an f64 for a renormalised double-float pair (|lo| at most
+// half an ulp of hi), formed on the integer pipes.  With d = eh - el >= 24
+// the exact sum is the integer (Mh 2^d +- Ml) 2^(el - 150); for d > 39 Ml is
+// first shifted right by d - 39 with the bits it loses folded into bit 0
+// (they lie far below the rounding position, so only their presence
+// matters), which keeps the sum within 64 bits.  It is rounded to 53 bits
+// with ties to even.  Zeros, subnormals, infinities, NaNs and pairs that are
+// not renormalised take the FP64 add (the same value).
+__device__ __forceinline__ double ff_to_f64(float hi, float lo) {
+  const uint32_t uh = __float_as_uint(hi), ul = __float_as_uint(lo);
+  const int eh = int((uh >> 23) & 0xFFu);
+  int el = int((ul >> 23) & 0xFFu);
+  int d = eh - el;
+  if ((ul & 0x7FFFFFFFu) == 0u) return f2d_exact(hi);
+  if (eh == 0 || eh == 0xFF || el == 0 || el == 0xFF || d < 24) return f2d_exact(hi) + f2d_exact(lo);
+  const uint64_t mh = uint64_t((uh & 0x7FFFFFu) | 0x800000u);
+  uint64_t ml = uint64_t((ul & 0x7FFFFFu) | 0x800000u);
+  if (d > 39) {
+    const int s = d - 39;
+    ml = s >= 25 ? 1u : ((ml >> s) | uint64_t((ml & ((uint64_t(1) << s) - 1)) != 0));
+    el += s;
+    d = 39;
+  }
+  const uint64_t S = ((uh ^ ul) >> 31) ? (mh << d) - ml : (mh << d) + ml;  // > 0
+  // the leading bit is at 23 + d, or 22 + d after a borrow
+  const int p = (S >> (23 + d)) ? 23 + d : 22 + d;
+  const int sh = p - 52;  // bits below 2^sh are dropped (sh >= -7)
+  uint64_t m;
+  if (sh <= 0) {
+    m = S << (-sh);
+  } else {
+    const uint64_t kept = S >> sh, rem = S & ((uint64_t(1) << sh) - 1), half = uint64_t(1) << (sh - 1);
+    m = kept + ((rem > half || (rem == half && (kept & 1u))) ? 1u : 0u);
+  }
+  // value = m 2^(el - 150 + sh), m in [2^52, 2^53]: the leading 1 (and a
+  // round-up to 2^53) carries into the exponent field
+  const uint64_t ebits = uint64_t(el - 150 + sh + 1074) << 52;
+  return __longlong_as_double((long long)((uint64_t(uh >> 31) << 63) | (ebits + m)));
+}
+
 }  // namespace ev
 
 namespace ev {

@@ -21,6 +21,7 @@
 
 #include "ev_device.cuh"
 #include "ev_internal.h"
+#include "ev_softfp.cuh"
 
 namespace ev {
 
@@ -384,17 +385,27 @@ __global__ void k_pred_and(const uint8_t* __restrict__ classical, const uint64_t
 // sectors (entry 0 of the 2^n-double buffer is unused).  mass[n-1][r] =
 // |a_r|^2 + |a_{r+2^(n-1)}|^2 and mass[q][r] = mass[q+1][r] + mass[q+1][r+2^q].
 
-// complex128 leaves use the oracle's arithmetic (nsq + nsq, f64), so shots
-// match its tree exactly; complex64 leaves are the double-float sum of the
-// four exact float squares, rounded to f64 once (~1e-14 relative).
-__device__ __forceinline__ double leaf_mass(double2 u, double2 v) { return __dadd_rn(nsq(u), nsq(v)); }
+// complex128 leaves use the oracle's arithmetic (nsq + nsq, f64; the plain
+// product inside nsq formed on the integer pipes), so shots match its tree
+// exactly; complex64 leaves are the double-float sum of the four exact float
+// squares, rounded to f64 once (~1e-14 relative) on the integer pipes.
+// nsq(a) = fma(x, x, y*y) with the plain product y*y formed on the integer
+// pipes when y is in the integer product's range (the same bits).
+__device__ __forceinline__ double nsq_soft(double2 a) {
+  const softfp::Unpacked uy = softfp::unpack(a.y);
+  const double yy = uy.ok ? softfp::mul(uy, uy) : __dmul_rn(a.y, a.y);
+  return __fma_rn(a.x, a.x, yy);
+}
+__device__ __forceinline__ double leaf_mass(double2 u, double2 v) {
+  return __dadd_rn(nsq_soft(u), nsq_soft(v));
+}
 __device__ __forceinline__ double leaf_mass(float2 u, float2 v) {
   FF f;
   f.add_prod(u.x, u.x);
   f.add_prod(u.y, u.y);
   f.add_prod(v.x, v.x);
   f.add_prod(v.y, v.y);
-  return f.value();
+  return ff_to_f64(f.hi, f.lo);  // = f.value(), with the final add on the integer pipes
 }
 
 template <typename V>
@@ -682,6 +693,8 @@ static int build_mass(ev_state* s) {
   int q;  // highest level still to build
   if (n - LL >= 12) {
     const uint64_t S = uint64_t(1) << (n - LL);  // columns, two per thread
+    // (the complex128 instance holds ~150 registers, one block per SM at a
+    // time; a 3-block budget spills and measured slower: 6.31 vs 5.43 ms)
     if (s->dtype == EV_C128)
       k_mass_leaf_fused<double2, LL>
           <<<grid_for(s, S / 2, resident_blocks<k_mass_leaf_fused<double2, LL>>()), 256, 0,

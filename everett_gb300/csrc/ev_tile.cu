@@ -318,7 +318,56 @@ __global__ void k_softfp_check(uint64_t seed, uint64_t per_thread, unsigned long
   if (mine) atomicAdd(bad, mine);
 }
 
+// ff_to_f64 (ev_device.cuh) against the FP64 add of the pair's two exact
+// f64 values, on renormalised double-float pairs (TwoSum of random floats
+// whose exponents differ by 0..80, with ties and cancellations).
+__global__ void k_ff_check(uint64_t seed, uint64_t per_thread, unsigned long long* bad) {
+  const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  uint64_t st = seed ^ (gid * 0x9E3779B97F4A7C15ULL);
+  unsigned long long mine = 0;
+  for (uint64_t i = 0; i < per_thread; ++i) {
+    const uint64_t r0 = check_next(st), r1 = check_next(st), r2 = check_next(st);
+    const uint32_t ea = 1 + uint32_t(r0 % 253), gap = uint32_t((r0 >> 8) % 81);
+    const uint32_t eb = ea > gap ? ea - gap : 1;
+    uint32_t fa = uint32_t(r1) & 0x7FFFFFu, fb = uint32_t(r1 >> 32) & 0x7FFFFFu;
+    if ((r2 & 7) == 0) fb = (r2 & 8) ? 0u : 0x400000u;  // short significands: ties
+    const float a = __uint_as_float(uint32_t(r2 >> 63) << 31 | ea << 23 | fa);
+    const float b = __uint_as_float(uint32_t((r2 >> 62) & 1) << 31 | eb << 23 | fb);
+    FF f;
+    f.add(a);
+    f.add(b);
+    const double got = ff_to_f64(f.hi, f.lo), want = f2d_exact(f.hi) + f2d_exact(f.lo);
+    mine += __double_as_longlong(got) != __double_as_longlong(want);
+  }
+  if (mine) atomicAdd(bad, mine);
+}
+
 }  // namespace ev
+
+extern "C" int ev_ff_check(uint64_t seed, uint64_t count, uint64_t* mismatches) {
+  using namespace ev;
+  clear_error();
+  if (!mismatches) return fail(EV_ERR_INVALID_ARGUMENT, "ev_ff_check: null output");
+  int dev = 0, sms = 0;
+  EV_CUDA(cudaGetDevice(&dev));
+  EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint64_t threads = uint64_t(sms) * 4 * 256;
+  const uint64_t per = (count + threads - 1) / threads;
+  unsigned long long* d = nullptr;
+  EV_CUDA(cudaMalloc(reinterpret_cast<void**>(&d), sizeof(*d)));
+  int rc = EV_OK;
+  unsigned long long h = 0;
+  if (cudaMemset(d, 0, sizeof(*d)) != cudaSuccess) {
+    rc = fail(EV_ERR_CUDA, "ev_ff_check: memset failed");
+  } else {
+    k_ff_check<<<unsigned(sms * 4), 256>>>(seed, per, d);
+    if (cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = fail(EV_ERR_CUDA, "ev_ff_check: kernel failed");
+  }
+  cudaFree(d);
+  if (rc == EV_OK) *mismatches = h;
+  return rc;
+}
 
 extern "C" int ev_softfp_check(uint64_t seed, uint64_t count, uint64_t* mismatches) {
   using namespace ev;

@@ -484,6 +484,10 @@ int ev_probe_fp64(double* fma_per_s);
  * (families that reach every rounding case); *mismatches = pairs whose bits
  * differ.  A check of the build, for tests. */
 int ev_softfp_check(uint64_t seed, uint64_t count, uint64_t* mismatches);
+/* Checks the integer-pipe rounding of a double-float pair to f64 (the
+ * complex64 sampling tree's leaves) against the FP64 add on `count` pairs;
+ * *mismatches = pairs whose bits differ.  A check of the build, for tests. */
+int ev_ff_check(uint64_t seed, uint64_t count, uint64_t* mismatches);
 /* y = x W (rows x 64 times 64 x 64, row-major f64) in the digit-sliced
  * arithmetic of the EV_FUSED_OZAKI pass, restated on the host with the
  * kernel's own slicing and recombination routines.  A check of the build,

@@ -343,6 +343,18 @@ def test_integer_pipe_product_matches_fp64_pipe(gpu):
         assert bad.value == 0, (seed, bad.value)
 
 
+def test_double_float_rounding_matches_fp64_add(gpu):
+    """The complex64 sampling tree rounds each leaf's double-float pair to
+    f64 on the integer pipes; on 2^28 pairs per seed (exponent gaps 0..80,
+    ties, cancellations) it gives the FP64 add's bits."""
+    import ctypes as C
+    from everett_gb300 import _native as N
+    for seed in (1, 2):
+        bad = C.c_uint64(7)
+        N.check(N.lib().ev_ff_check(seed, 1 << 28, C.byref(bad)))
+        assert bad.value == 0, (seed, bad.value)
+
+
 @pytest.mark.parametrize("level", ["00", "11", "22", "21", "12"])
 def test_tiled_integer_pipe_levels_bit_exact(gpu, monkeypatch, level):
     """Every level of the complex128 tile passes' integer-pipe products
