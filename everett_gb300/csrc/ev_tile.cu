@@ -16,6 +16,7 @@
 // the tile's base index, so the whole tile either takes the gate or skips
 // it, and a control inside T becomes a local mask.
 #include <cstdlib>
+#include <cstring>
 
 #include "ev_bulk.cuh"
 #include "ev_tile.cuh"
@@ -24,6 +25,23 @@ namespace ev {
 
 constexpr int kTileThreads = 512;
 constexpr int kMaxPassOps = 48;  // op records per pass (staged in shared memory)
+
+// Block shape of the pass: by default two blocks of 512 threads per SM with
+// the records staged in shared memory; EV_TILE_THREADS=256 three blocks of
+// 256 threads per SM (80 registers a thread instead of 64), the records read
+// through L1 so that three tiles fit in shared memory; EV_TILE_THREADS=1x512
+// one block of 512 threads (128 registers, no spills).  All give the same
+// results.  Measured on the complex128 pass (28 qubits, depth 20, ms per
+// circuit): two blocks of 512 2311, three of 256 2424, one of 512 2603 (2497
+// with 2^13-amplitude tiles): the spills of the 64-register form cost less
+// than the warps the other shapes give up.
+static int tile_shape() {
+  const char* e = getenv("EV_TILE_THREADS");
+  if (e == nullptr) return 0;
+  if (strcmp(e, "256") == 0) return 1;
+  if (strcmp(e, "1x512") == 0) return 2;
+  return 0;
+}
 
 // How many amplitudes of each pair have their complex128 products formed on
 // the integer pipes (TileOp::soft), for real-matrix records and for the
@@ -70,10 +88,11 @@ constexpr uint32_t kTileWaitLimit = 1u << 24;  // try_wait polls before giving u
 // block: [tile 2^k amplitudes][row offsets 2^(k-L)][op records][comp qubits].
 // A load that never completes sets *err (the run's device flag, reported as
 // EV_ERR_TIMEOUT) and ends the block after a bounded drain.
-template <typename V, bool BULK>
-__global__ void __launch_bounds__(kTileThreads, 2)
+template <typename V, bool BULK, int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB)
     k_tile(V* __restrict__ s, uint64_t ntiles, const TilePlan* __restrict__ gplan,
            const TileOp* __restrict__ gops, int nops, const uint8_t* pred, int* err) {
+  constexpr bool kStageOps = MINB < 3;
   if (pred != nullptr && *pred == 0) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(8) uint64_t bar;
@@ -88,17 +107,20 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   // op records start on a 16-byte boundary (they are staged with 16-byte
   // stores); tile + offsets is not a multiple of 16 bytes for tiny tiles
   const size_t ops_at = (sizeof(V) * size + sizeof(uint64_t) * nrows + 15) & ~size_t(15);
-  TileOp* ops = reinterpret_cast<TileOp*>(smem_raw + ops_at);
-  uint8_t* comp = reinterpret_cast<uint8_t*>(ops + nops);
+  TileOp* sops = reinterpret_cast<TileOp*>(smem_raw + ops_at);
+  const TileOp* ops = kStageOps ? sops : gops;
+  uint8_t* comp = reinterpret_cast<uint8_t*>(sops + (kStageOps ? nops : 0));
   if (use_bulk && threadIdx.x == 0) {
     mbar_init(&bar, 1);
     mbar_init_fence();
   }
   {
-    const uint4* src = reinterpret_cast<const uint4*>(gops);
-    uint4* dst = reinterpret_cast<uint4*>(ops);
-    const int words = nops * int(sizeof(TileOp) / sizeof(uint4));
-    for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+    if (kStageOps) {
+      const uint4* src = reinterpret_cast<const uint4*>(gops);
+      uint4* dst = reinterpret_cast<uint4*>(sops);
+      const int words = nops * int(sizeof(TileOp) / sizeof(uint4));
+      for (int w = threadIdx.x; w < words; w += blockDim.x) dst[w] = src[w];
+    }
     if (threadIdx.x < 64) comp[threadIdx.x] = gplan->comp[threadIdx.x];
   }
   for (uint32_t h = threadIdx.x; h < nrows; h += blockDim.x) {
@@ -171,12 +193,12 @@ __global__ void __launch_bounds__(kTileThreads, 2)
   if (use_bulk && warp == 0) bulk_wait_all();
 }
 
-template <typename V, bool BULK>
+template <typename V, bool BULK, int NT, int MINB>
 static int launch_tile_as(ev_state* s, uint64_t ntiles, size_t smem, const TilePlan* dplan,
                           const TileOp* dops, int nops, const uint8_t* pred) {
-  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_tile<V, BULK>)));
+  EV_TRY(prepare_smem_kernel(reinterpret_cast<const void*>(k_tile<V, BULK, NT, MINB>)));
   int per_sm = 0;
-  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<V, BULK>, kTileThreads,
+  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tile<V, BULK, NT, MINB>, NT,
                                                         smem));
   if (per_sm < 1) per_sm = 1;
   uint64_t grid = uint64_t(s->num_sms) * per_sm;
@@ -184,7 +206,7 @@ static int launch_tile_as(ev_state* s, uint64_t ntiles, size_t smem, const TileP
   ProfScope prof(s, P_TILE, 2.0 * double(s->len()) * double(sizeof(V)));
   s->launches += 1;
   int* derr = reinterpret_cast<int*>(s->scratch.counter + 1);
-  k_tile<V, BULK><<<unsigned(grid), kTileThreads, smem, s->stream>>>(
+  k_tile<V, BULK, NT, MINB><<<unsigned(grid), NT, smem, s->stream>>>(
       static_cast<V*>(s->amps), ntiles, dplan, dops, nops, pred, derr);
   EV_CUDA(cudaGetLastError());
   return EV_OK;
@@ -195,10 +217,15 @@ static int launch_tile(ev_state* s, uint64_t ntiles, const TilePlan& plan, const
                        const TileOp* dops, int nops, const uint8_t* pred) {
   const size_t ops_at = (sizeof(V) * (size_t(1) << plan.k) +
                          sizeof(uint64_t) * (size_t(1) << (plan.k - plan.L)) + 15) & ~size_t(15);
+  const bool bulk = tile_bulk_enabled();
+  const int shape = tile_shape();
+  if (shape == 1 && !bulk)
+    return launch_tile_as<V, false, 256, 3>(s, ntiles, ops_at + 64, dplan, dops, nops, pred);
   const size_t smem = ops_at + sizeof(TileOp) * size_t(nops) + 64;
-  static const bool bulk = tile_bulk_enabled();
-  if (bulk) return launch_tile_as<V, true>(s, ntiles, smem, dplan, dops, nops, pred);
-  return launch_tile_as<V, false>(s, ntiles, smem, dplan, dops, nops, pred);
+  if (shape == 2 && !bulk)
+    return launch_tile_as<V, false, kTileThreads, 1>(s, ntiles, smem, dplan, dops, nops, pred);
+  if (bulk) return launch_tile_as<V, true, kTileThreads, 2>(s, ntiles, smem, dplan, dops, nops, pred);
+  return launch_tile_as<V, false, kTileThreads, 2>(s, ntiles, smem, dplan, dops, nops, pred);
 }
 
 int default_tile_bits(int dtype) { return dtype == EV_C128 ? 12 : 13; }

@@ -383,14 +383,21 @@ def test_tiled_integer_pipe_levels_bit_exact(gpu, monkeypatch, level):
     assert exact(CudaStateVectorBackend.run(rl, mode="tiled").state().amplitudes(), want), level
 
 
-@pytest.mark.parametrize("chain", ["0", "1", "2"])
-def test_tiled_chains_bit_exact(gpu, monkeypatch, chain):
+@pytest.mark.parametrize("chain,shape", [("0", ""), ("1", ""), ("2", ""), ("2", "256"),
+                                         ("2", "1x512"), ("0", "256")])
+def test_tiled_chains_bit_exact(gpu, monkeypatch, chain, shape):
     """The tile pass applies runs of 1-qubit records in registers: runs on one
     target with the same controls (pair chains) and uncontrolled runs over
     two targets (quad chains).  Every chaining level (none, pair chains,
-    pair and quad chains) gives the oracle's bits, with every 1-qubit kind,
-    controls inside and outside the tile, and tiles of 4 to 12 qubits."""
+    pair and quad chains) and every block shape of the pass (two blocks of
+    512 threads, three of 256 reading their records through L1, one of 512)
+    gives the oracle's bits, with every 1-qubit kind, controls inside and
+    outside the tile, and tiles of 4 to 12 qubits."""
     monkeypatch.setenv("EV_TILE_CHAIN", chain)
+    if shape:
+        monkeypatch.setenv("EV_TILE_THREADS", shape)
+    else:
+        monkeypatch.delenv("EV_TILE_THREADS", raising=False)
     rng = np.random.default_rng(31)
     n = 13
     c = Circuit(n)
