@@ -468,7 +468,8 @@ bool has_classical_ops(const ev_circuit* c) {
   return false;
 }
 
-void plan_circuit(const ev_circuit* c, int kmax, bool reorder, CircPlan* out) {
+void plan_circuit(const ev_circuit* c, int kmax, bool c64, CircPlan* out) {
+  const bool reorder = c64;  // complex64 may reorder commuting ops
   const int n = int(c->num_qubits);
   out->n = n;
   const int k = n <= kmax ? n : kmax;
@@ -518,6 +519,7 @@ void plan_circuit(const ev_circuit* c, int kmax, bool reorder, CircPlan* out) {
         continue;
       }
       encode_op(c, src, p.tset, local, &tmp);
+      if (c64) pack_f32_matrix(tmp.m, tmp.kind == T_1Q ? 8 : 32);
       BatchOp b;
       b.kind = tmp.kind;
       b.k1 = tmp.k1;

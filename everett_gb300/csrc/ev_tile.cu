@@ -267,6 +267,7 @@ int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, 
     ops.assign(p.ops.size(), TileOp{});
     for (size_t j = 0; j < p.ops.size(); ++j) {
       encode_op(c, c->ops[p.ops[j]], p.tset, local, &ops[j]);
+      if (s->dtype == EV_C64) pack_f32_matrix(ops[j].m, ops[j].kind == T_1Q ? 8 : 32);
       if (s->dtype == EV_C128 && ops[j].kind == T_1Q)
         ops[j].soft = uint8_t(ops[j].k1 == K1_REAL ? soft.real : soft.other);
     }

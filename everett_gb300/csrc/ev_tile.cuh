@@ -62,9 +62,30 @@ struct TilePlan {
   uint8_t comp[64];  // global qubits outside T, ascending
 };
 
+// Entry i of a record's matrix.  complex128 records hold f64 [re, im]
+// pairs; complex64 records hold f32 pairs, rounded once on the host
+// (pack_f32_matrix) because GB300 runs f64 -> f32 conversions at its FP64
+// rate: converting a 2x2 matrix per record and thread cost more than the
+// record's complex64 arithmetic on a 2^13-amplitude tile.
 template <typename V>
-__device__ __forceinline__ V ldm(const double* m, int i) {
-  return mkv<V>(m[2 * i], m[2 * i + 1]);
+__device__ __forceinline__ V ldm(const double* m, int i);
+template <>
+__device__ __forceinline__ double2 ldm<double2>(const double* m, int i) {
+  return make_double2(m[2 * i], m[2 * i + 1]);
+}
+template <>
+__device__ __forceinline__ float2 ldm<float2>(const double* m, int i) {
+  return reinterpret_cast<const float2*>(m)[i];
+}
+
+// Rewrites the first nd doubles of m as nd floats (round to nearest even,
+// the device's f64 -> f32 conversion) in its first nd * 4 bytes and zeroes
+// the rest of those nd doubles: the complex64 form of a record's matrix.
+inline void pack_f32_matrix(double* m, int nd) {
+  float f[32];
+  for (int j = 0; j < nd; ++j) f[j] = static_cast<float>(m[j]);
+  std::memset(m, 0, size_t(nd) * sizeof(double));
+  std::memcpy(m, f, size_t(nd) * sizeof(float));
 }
 
 __device__ __forceinline__ uint32_t ins0(uint32_t i, int p) {
