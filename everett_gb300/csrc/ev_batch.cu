@@ -51,13 +51,18 @@
 namespace ev {
 
 struct BatchOp {
-  uint8_t kind, k1, p0, p1, lo, hi, nins, soft;  // soft: as TileOp::soft
-  uint32_t lmask;
-  uint32_t mat;  // offset of the matrix in the pool (doubles)
+  uint8_t kind, k1, p0, p1, lo, hi, nins, soft;  // as TileOp (soft is 0 here)
+  uint8_t run, ctype;                            // chains, as TileOp
+  uint16_t lmask;  // local control mask (tiles of at most 16 qubits), or a classical bit
+  uint32_t mat;    // offset of the matrix in the pool (doubles)
   uint64_t emask;
   uint64_t ins;
 };
 static_assert(sizeof(BatchOp) == 32, "compact op record");
+__device__ __forceinline__ const double* rec_m(const BatchOp& op, const double* mats) {
+  return mats + op.mat;
+}
+__device__ __forceinline__ uint32_t rec_sok(const BatchOp&) { return 0; }
 
 struct BatchCirc {
   uint32_t n, k, npasses, pad;
@@ -318,21 +323,32 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 2) k_batch(BatchArgs a, in
       __syncthreads();
     }
     bool take = true;  // the IfClassic prefixes read so far hold
-    for (uint32_t o = 0; o < pr.nops; ++o) {
-      const BatchOp op = a.ops[pr.op0 + o];
+    for (uint32_t o = 0; o < pr.nops;) {
+      const BatchOp* rec = a.ops + pr.op0 + o;
+      const BatchOp op = *rec;
+      // chains (run > 1) are formed only in circuits without classical ops
+      const int run = op.run > 1 ? op.run : 1;
+      o += run;
       if (op.kind == B_IF) {
         take = take && s_cl[op.lmask] != 0;
         continue;
       }
-      const bool run = take;
+      const bool go = take;
       take = true;
-      if (!run) continue;
+      if (!go) continue;
       if (op.kind == B_MEAS) {
         batch_measure(tile, size, op.p0, op.lmask, red, s_cl, s_rng, s_meas);
         continue;
       }
       if ((base & op.emask) != op.emask) continue;
-      apply_tile_op(tile, k, op, a.mats + op.mat);
+      if (run > 1 && op.ctype == CH_QUAD)
+        tile_quad_chain(tile, size, rec, run, a.mats);
+      else if (run > 1 && op.ctype == CH_DIAG)
+        tile_diag_chain(tile, size, rec, run, a.mats);
+      else if (run > 1)
+        tile_chain(tile, size >> op.nins, rec, run, a.mats);
+      else
+        apply_tile_op(tile, k, op, a.mats + op.mat);
       __syncthreads();
     }
     if (classical && t < int(c.ncl)) a.cl[c.cl + t] = s_cl[t];
@@ -490,7 +506,8 @@ void plan_circuit(const ev_circuit* c, int kmax, bool c64, CircPlan* out) {
   // every circuit gets at least one pass: pass 0 is what writes |0...0>
   if (passes.empty()) passes.push_back({{}, (uint64_t(1) << k) - 1});
   std::unordered_map<size_t, std::vector<uint32_t>> seen;  // hash -> offsets
-  TileOp tmp;
+  std::vector<TileOp> recs;
+  const ChainSet chains = chain_set("EV_BATCH_CHAIN", ChainSet{false, false, true});
   for (const Pass& p : passes) {
     TilePlan plan{};
     plan.k = k;
@@ -508,17 +525,26 @@ void plan_circuit(const ev_circuit* c, int kmax, bool c64, CircPlan* out) {
       }
     out->plans.push_back(plan);
     out->passes.push_back({uint32_t(out->ops.size()), uint32_t(p.ops.size())});
-    for (uint64_t j : p.ops) {
-      const ev_op& src = c->ops[j];
+    // the pass's gate records, chained as the tile pass chains them (not in
+    // circuits with measurements or classical control, whose records run one
+    // by one in the classical register's order)
+    recs.assign(p.ops.size(), TileOp{});
+    for (size_t j = 0; j < p.ops.size(); ++j) {
+      const ev_op& src = c->ops[p.ops[j]];
+      if (src.kind != EV_OP_MEASURE && src.kind != EV_OP_IF) encode_op(c, src, p.tset, local, &recs[j]);
+    }
+    if (!out->classical) mark_chains(recs.data(), recs.size(), chains);
+    for (size_t jj = 0; jj < p.ops.size(); ++jj) {
+      const ev_op& src = c->ops[p.ops[jj]];
       if (src.kind == EV_OP_MEASURE || src.kind == EV_OP_IF) {
         BatchOp b{};
         b.kind = src.kind == EV_OP_MEASURE ? B_MEAS : B_IF;
         b.p0 = uint8_t(src.kind == EV_OP_MEASURE ? src.q0 : 0);
-        b.lmask = uint32_t(src.kind == EV_OP_MEASURE ? src.q1 : src.q0);
+        b.lmask = uint16_t(src.kind == EV_OP_MEASURE ? src.q1 : src.q0);
         out->ops.push_back(b);
         continue;
       }
-      encode_op(c, src, p.tset, local, &tmp);
+      TileOp& tmp = recs[jj];
       if (c64) pack_f32_matrix(tmp.m, tmp.kind == T_1Q ? 8 : 32);
       BatchOp b;
       b.kind = tmp.kind;
@@ -529,7 +555,9 @@ void plan_circuit(const ev_circuit* c, int kmax, bool c64, CircPlan* out) {
       b.hi = tmp.hi;
       b.nins = tmp.nins;
       b.soft = 0;
-      b.lmask = tmp.lmask;
+      b.run = tmp.run;
+      b.ctype = tmp.ctype;
+      b.lmask = uint16_t(tmp.lmask);
       b.emask = tmp.emask;
       b.ins = tmp.ins;
       const int nd = tmp.kind == T_1Q ? 8 : 32;

@@ -57,13 +57,6 @@ static SoftLevels tile_soft_levels() {
   return SoftLevels{e[0] - '0', e[1] - '0'};
 }
 
-// Chained application of records (TileOp::run): EV_TILE_CHAIN=0 applies
-// every record on its own, 1 forms pair chains only, 2 (default) pair and
-// quad chains; all give the same results.
-static int tile_chain_level() {
-  const char* e = getenv("EV_TILE_CHAIN");
-  return (e == nullptr || e[0] < '0' || e[0] > '2') ? 2 : e[0] - '0';
-}
 
 // How tiles move between HBM and shared memory.  By default every thread
 // loads and stores its share of the tile with 16-byte accesses.  With
@@ -164,10 +157,12 @@ __global__ void __launch_bounds__(NT, MINB)
       const TileOp& op = ops[o];
       const int run = op.run > 1 ? op.run : 1;
       if ((base & op.emask) == op.emask) {  // uniform across the block
-        if (run > 1 && op.hi != 0)
-          tile_quad_chain(tile, size, ops + o, run);
+        if (run > 1 && op.ctype == CH_QUAD)
+          tile_quad_chain(tile, size, ops + o, run, nullptr);
+        else if (run > 1 && op.ctype == CH_DIAG)
+          tile_diag_chain(tile, size, ops + o, run, nullptr);
         else if (run > 1)
-          tile_chain(tile, size >> op.nins, ops + o, run);
+          tile_chain(tile, size >> op.nins, ops + o, run, nullptr);
         else
           apply_tile_op(tile, k, op, op.m);
         __syncthreads();
@@ -247,7 +242,7 @@ int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, 
       plan_passes(c, first, last, n, k, L, uint64_t(kMaxPassOps), s->dtype == EV_C64);
   const uint64_t ntiles = uint64_t(1) << (n - k);
   const SoftLevels soft = tile_soft_levels();
-  const int chains = tile_chain_level();
+  const ChainSet chains = chain_set("EV_TILE_CHAIN", ChainSet{true, true, true});
   std::vector<TileOp> ops;
   for (const Pass& p : passes) {
     TilePlan plan{};
@@ -271,9 +266,7 @@ int plan_tiled(ev_state* s, const ev_circuit* c, uint64_t first, uint64_t last, 
       if (s->dtype == EV_C128 && ops[j].kind == T_1Q)
         ops[j].soft = uint8_t(ops[j].k1 == K1_REAL ? soft.real : soft.other);
     }
-    // complex128 only: a complex64 chain would convert its f64 matrices to
-    // f32 per pair, and those conversions run at the FP64 rate
-    if (chains && s->dtype == EV_C128) mark_chains(ops.data(), ops.size(), chains == 2);
+    mark_chains(ops.data(), ops.size(), chains);
     SegStep st;
     st.fused = 0;
     st.off0 = blob->add(&plan, sizeof(plan));

@@ -8,6 +8,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <type_traits>
 #include <vector>
@@ -43,7 +44,8 @@ struct __align__(16) TileOp {
                    // applied pair by pair in registers); 0 or 1: none
   uint8_t sok;     // complex128 T_1Q: the factors in m[8..15] are in the
                    // integer-pipe product's domain (SoftM1::ok)
-  uint8_t pad2[2];
+  uint8_t ctype;   // first record of a chain (run > 1): ChainKind
+  uint8_t pad2;
   uint64_t emask;  // controls outside the tile (global bit mask)
   uint64_t ins;    // T_1Q: sorted local positions of (local controls + target),
                    // 4 bits each, lowest position in the low nibble
@@ -53,6 +55,23 @@ struct __align__(16) TileOp {
 };
 
 static_assert(sizeof(TileOp) % 16 == 0, "op records are staged with 16-byte copies");
+
+// What a chain of records (TileOp::run > 1 on its first record) is:
+// CH_PAIR  1-qubit records on one target with the same controls, applied to
+//          pairs held in registers;
+// CH_QUAD  uncontrolled 1-qubit records on two targets, applied to quads;
+// CH_DIAG  diagonal records (diagonal and phase 1-qubit records with any
+//          local controls, CZ, diagonal 2-qubit records), applied to each
+//          amplitude in turn: a diagonal record multiplies every amplitude
+//          by the entry its index selects, independently of the others.
+enum ChainKind : uint8_t { CH_PAIR = 0, CH_QUAD = 1, CH_DIAG = 2 };
+
+// The matrix and integer-pipe flag of a record; records kept elsewhere (the
+// batched runner's, whose matrices sit in a shared pool) overload these.
+__host__ __device__ __forceinline__ const double* rec_m(const TileOp& op, const double*) {
+  return op.m;
+}
+__host__ __device__ __forceinline__ uint32_t rec_sok(const TileOp& op) { return op.sok; }
 
 struct TilePlan {
   int k, L;
@@ -236,7 +255,7 @@ __device__ __forceinline__ void pair_fp(const double* mm, V& a0, V& a1) {
     a1 = cadd(cmul(m2, a0), cmul(m3, a1));
     a0 = n0;
   } else if constexpr (K1 == K1_REAL) {
-    const R r0 = R(mm[0]), r1 = R(mm[2]), r2 = R(mm[4]), r3 = R(mm[6]);
+    const R r0 = ldm<V>(mm, 0).x, r1 = ldm<V>(mm, 1).x, r2 = ldm<V>(mm, 2).x, r3 = ldm<V>(mm, 3).x;
     const V n0 = cadd(rmul(r0, a0), rmul(r1, a1));
     a1 = cadd(rmul(r2, a0), rmul(r3, a1));
     a0 = n0;
@@ -258,10 +277,11 @@ __device__ __forceinline__ void pair_fp(const double* mm, V& a0, V& a1) {
 // straight-line block over both needs more registers than a 64-register
 // thread has, and its spills cost more than its extra overlap gains.
 template <int K1, typename V, typename Op>
-__device__ __forceinline__ void chain_rec(const Op& op, V& a0, V& a1, V& b0, V& b1) {
-  const double* mm = op.m;
+__device__ __forceinline__ void chain_rec(const Op& op, const double* mats, V& a0, V& a1, V& b0,
+                                          V& b1) {
+  const double* mm = rec_m(op, mats);
   if constexpr (std::is_same<V, double2>::value && K1 != K1_ANTI && K1 != K1_IDENT) {
-    if (op.soft && op.sok) {  // uniform across the block
+    if (op.soft && rec_sok(op)) {  // uniform across the block
       SoftM1 f;
       f.m0 = ldm<double2>(mm, 0);
       f.m1 = ldm<double2>(mm, 1);
@@ -284,14 +304,15 @@ __device__ __forceinline__ void chain_rec(const Op& op, V& a0, V& a1, V& b0, V& 
 }
 
 template <typename V, typename Op>
-__device__ __forceinline__ void chain_rec_any(const Op& op, V& a0, V& a1, V& b0, V& b1);
+__device__ __forceinline__ void chain_rec_any(const Op& op, const double* mats, V& a0, V& a1,
+                                              V& b0, V& b1);
 
 // A chain of `run` 1-qubit records that share their target and controls:
 // each thread loads two pairs, applies every record of the chain to them in
 // circuit order and stores them once.  Every amplitude sees the same
 // operations in the same order as record-by-record application.
 template <typename V, typename Op>
-__device__ void tile_chain(V* t, uint32_t count, const Op* ops, int run) {
+__device__ void tile_chain(V* t, uint32_t count, const Op* ops, int run, const double* mats) {
   const Op& op0 = ops[0];
   const uint32_t tbit = 1u << op0.p0, lmask = op0.lmask;
   const int nins = op0.nins;
@@ -310,7 +331,7 @@ __device__ void tile_chain(V* t, uint32_t count, const Op* ops, int run) {
     ja |= lmask;
     jb |= lmask;
     V a0 = t[ja], a1 = t[ja | tbit], b0 = t[jb], b1 = t[jb | tbit];
-    for (int r = 0; r < run; ++r) chain_rec_any(ops[r], a0, a1, b0, b1);
+    for (int r = 0; r < run; ++r) chain_rec_any(ops[r], mats, a0, a1, b0, b1);
     t[ja] = a0;
     t[ja | tbit] = a1;
     if (two) {
@@ -322,13 +343,14 @@ __device__ void tile_chain(V* t, uint32_t count, const Op* ops, int run) {
 
 // chain_rec for the record's kind.
 template <typename V, typename Op>
-__device__ __forceinline__ void chain_rec_any(const Op& op, V& a0, V& a1, V& b0, V& b1) {
+__device__ __forceinline__ void chain_rec_any(const Op& op, const double* mats, V& a0, V& a1,
+                                              V& b0, V& b1) {
   switch (op.k1) {
-    case K1_DENSE: chain_rec<K1_DENSE>(op, a0, a1, b0, b1); break;
-    case K1_REAL: chain_rec<K1_REAL>(op, a0, a1, b0, b1); break;
-    case K1_DIAG: chain_rec<K1_DIAG>(op, a0, a1, b0, b1); break;
-    case K1_PHASE: chain_rec<K1_PHASE>(op, a0, a1, b0, b1); break;
-    case K1_ANTI: chain_rec<K1_ANTI>(op, a0, a1, b0, b1); break;
+    case K1_DENSE: chain_rec<K1_DENSE>(op, mats, a0, a1, b0, b1); break;
+    case K1_REAL: chain_rec<K1_REAL>(op, mats, a0, a1, b0, b1); break;
+    case K1_DIAG: chain_rec<K1_DIAG>(op, mats, a0, a1, b0, b1); break;
+    case K1_PHASE: chain_rec<K1_PHASE>(op, mats, a0, a1, b0, b1); break;
+    case K1_ANTI: chain_rec<K1_ANTI>(op, mats, a0, a1, b0, b1); break;
     default: break;  // identity
   }
 }
@@ -340,7 +362,7 @@ __device__ __forceinline__ void chain_rec_any(const Op& op, V& a0, V& a1, V& b0,
 // The pairs of a record are disjoint and each amplitude sees its records in
 // circuit order, so the results equal record-by-record application.
 template <typename V, typename Op>
-__device__ void tile_quad_chain(V* t, uint32_t size, const Op* ops, int run) {
+__device__ void tile_quad_chain(V* t, uint32_t size, const Op* ops, int run, const double* mats) {
   const int lo = ops[0].lo, hi = ops[0].hi;
   const uint32_t lob = 1u << lo, hib = 1u << hi;
   const uint32_t count = size >> 2;
@@ -350,14 +372,84 @@ __device__ void tile_quad_chain(V* t, uint32_t size, const Op* ops, int run) {
     for (int r = 0; r < run; ++r) {
       const Op& op = ops[r];
       if (op.p0 == lo)
-        chain_rec_any(op, q0, q1, q2, q3);
+        chain_rec_any(op, mats, q0, q1, q2, q3);
       else
-        chain_rec_any(op, q0, q2, q1, q3);
+        chain_rec_any(op, mats, q0, q2, q1, q3);
     }
     t[base] = q0;
     t[base | lob] = q1;
     t[base | hib] = q2;
     t[base | lob | hib] = q3;
+  }
+}
+
+// A chain of `run` diagonal records (CH_DIAG): each thread holds a few
+// amplitudes (local indices l0 + j * blockDim.x) in registers, reads each
+// record once and applies it to all of them, in circuit order.  Records act
+// on each amplitude alone, so this equals record-by-record application.
+template <typename V, typename Op>
+__device__ void tile_diag_chain(V* t, uint32_t size, const Op* ops, int run, const double* mats) {
+  // one amplitude at a time for complex128: more live registers spill the
+  // 64-register tile pass
+  constexpr int CH = sizeof(V) == 16 ? 1 : 8;
+  const uint32_t nb = blockDim.x;
+  for (uint32_t l0 = threadIdx.x; l0 < size; l0 += CH * nb) {
+    V a[CH];
+#pragma unroll
+    for (int j = 0; j < CH; ++j)
+      if (l0 + j * nb < size) a[j] = t[l0 + j * nb];
+    for (int r = 0; r < run; ++r) {
+      const Op& op = ops[r];
+      const double* mm = rec_m(op, mats);
+      const uint32_t b0 = 1u << op.p0;
+      if (op.kind == T_1Q) {
+        const uint32_t lmask = op.lmask;
+        const int k1 = op.k1;
+        if (k1 == K1_IDENT) continue;
+        const V e0 = ldm<V>(mm, 0), e3 = ldm<V>(mm, 3);
+        bool soft0 = false, soft1 = false;
+        const softfp::Unpacked* u = reinterpret_cast<const softfp::Unpacked*>(mm + 8);
+        if constexpr (std::is_same<V, double2>::value) {
+          soft0 = op.soft && rec_sok(op);
+          soft1 = soft0 && op.soft == 2;
+        }
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          const uint32_t l = l0 + j * nb;
+          if ((l & lmask) != lmask) continue;  // a local control is 0
+          const bool one = (l & b0) != 0;
+          if (k1 == K1_PHASE && !one) continue;
+          if constexpr (std::is_same<V, double2>::value) {
+            if (one ? soft1 : soft0) {
+              a[j] = soft_diag(one ? e3 : e0, u[one ? 3 : 0], a[j]);
+              continue;
+            }
+          }
+          a[j] = cmul(one ? e3 : e0, a[j]);
+        }
+        continue;
+      }
+      const uint32_t b1 = 1u << op.p1;
+      if (op.kind == T_CZ) {
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          const uint32_t l = l0 + j * nb;
+          if ((l & b0) && (l & b1)) a[j] = cneg(a[j]);
+        }
+        continue;
+      }
+      // T_DIAG2: entry 5c with c = 2 * bit(p0) + bit(p1), as tile_2q maps them
+      const V d0 = ldm<V>(mm, 0), d1 = ldm<V>(mm, 5), d2 = ldm<V>(mm, 10), d3 = ldm<V>(mm, 15);
+#pragma unroll
+      for (int j = 0; j < CH; ++j) {
+        const uint32_t l = l0 + j * nb;
+        const V d = (l & b0) ? ((l & b1) ? d3 : d2) : ((l & b1) ? d1 : d0);
+        a[j] = cmul(d, a[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < CH; ++j)
+      if (l0 + j * nb < size) t[l0 + j * nb] = a[j];
   }
 }
 
@@ -510,14 +602,51 @@ inline void encode_op(const ev_circuit* c, const ev_op& op, uint64_t tset, const
   out->nins = uint8_t(ni);
 }
 
-// Marks the chains of a pass's records (TileOp::run).  A run of
-// consecutive uncontrolled 1-qubit records with the same outside controls
+// Which chains a pass forms (TileOp::run): pair chains, quad chains,
+// diagonal chains.  All give the same results.
+struct ChainSet {
+  bool pairs, quads, diag;
+};
+
+// A ChainSet from an environment variable: "0" none, otherwise letters p
+// (pair), q (quad), d (diagonal), or the levels 1 (p), 2 (pq), 3 (pqd).
+// EV_TILE_CHAIN sets the tile pass's (default pqd), EV_BATCH_CHAIN the
+// batched runner's.
+inline ChainSet chain_set(const char* var, ChainSet dflt) {
+  const char* e = getenv(var);
+  if (e == nullptr || e[0] == 0) return dflt;
+  if (e[1] == 0 && e[0] >= '0' && e[0] <= '3') {
+    const int l = e[0] - '0';
+    return ChainSet{l >= 1, l >= 2, l >= 3};
+  }
+  ChainSet c{false, false, false};
+  for (const char* x = e; *x; ++x) {
+    if (*x == 'p') c.pairs = true;
+    else if (*x == 'q') c.quads = true;
+    else if (*x == 'd') c.diag = true;
+    else return dflt;
+  }
+  return c;
+}
+
+inline bool is_diag_rec(const TileOp& o) {
+  if (o.kind == T_CZ || o.kind == T_DIAG2) return true;
+  return o.kind == T_1Q && (o.k1 == K1_DIAG || o.k1 == K1_PHASE || o.k1 == K1_IDENT);
+}
+
+// Marks the chains of a pass's records (TileOp::run, TileOp::ctype).  A run
+// of consecutive uncontrolled 1-qubit records with the same outside controls
 // whose targets are two local positions becomes a quad chain (lo/hi set on
 // its first record); a run on one target with the same controls becomes a
-// pair chain.
-inline void mark_chains(TileOp* ops, size_t nops, bool quads = true) {
+// pair chain; a longer run of diagonal records with the same outside
+// controls becomes a diagonal chain instead.  Only the kinds in cs form.
+inline void mark_chains(TileOp* ops, size_t nops, ChainSet cs) {
+  const bool quads = cs.quads, diag = cs.diag;
   for (size_t j = 0; j < nops;) {
     TileOp& h = ops[j];
+    size_t d = j;
+    if (diag)
+      while (d < nops && d - j < 255 && is_diag_rec(ops[d]) && ops[d].emask == h.emask) ++d;
     size_t e = j + 1;
     int t2 = -1;
     if (h.kind == T_1Q && h.lmask == 0 && quads) {
@@ -530,15 +659,24 @@ inline void mark_chains(TileOp* ops, size_t nops, bool quads = true) {
         }
         ++e;
       }
-    } else if (h.kind == T_1Q) {
+    } else if (h.kind == T_1Q && cs.pairs) {
       while (e < nops && e - j < 255 && ops[e].kind == T_1Q && ops[e].p0 == h.p0 &&
              ops[e].lmask == h.lmask && ops[e].emask == h.emask)
         ++e;
     }
+    if (d - j >= 2 && d > e) {
+      h.run = uint8_t(d - j);
+      h.ctype = CH_DIAG;
+      for (size_t r = j + 1; r < d; ++r) ops[r].run = 0;
+      j = d;
+      continue;
+    }
     h.run = uint8_t(e - j);
+    h.ctype = CH_PAIR;
     if (t2 >= 0) {
       h.lo = uint8_t(std::min<int>(h.p0, t2));
       h.hi = uint8_t(std::max<int>(h.p0, t2));
+      h.ctype = CH_QUAD;
     }
     for (size_t r = j + 1; r < e; ++r) ops[r].run = 0;
     j = e;

@@ -33,8 +33,15 @@ def oracle_expz(amps):
     return b[2] / O.norm_sqr(amps)
 
 
-@pytest.mark.parametrize("tile_bits", [6, 8, 12])
-def test_batch_c128_bit_exact(gpu, tile_bits):
+@pytest.mark.parametrize("tile_bits,chain", [(6, ""), (8, ""), (12, ""), (8, "0"), (12, "pqd")])
+def test_batch_c128_bit_exact(gpu, monkeypatch, tile_bits, chain):
+    """Batched complex128 runs give the oracle's bits at every tile size and
+    with every kind of chain (TFIM steps chain their Rzz records as diagonal
+    chains, their Rx records as quad chains)."""
+    if chain:
+        monkeypatch.setenv("EV_BATCH_CHAIN", chain)
+    else:
+        monkeypatch.delenv("EV_BATCH_CHAIN", raising=False)
     circs = tfim_mix(24, 2, 13, seed=tile_bits)
     circs.append(workloads.random_layers(11, 4, seed=9))
     circs.append(workloads.qft_on_basis(9, 300))

@@ -383,16 +383,18 @@ def test_tiled_integer_pipe_levels_bit_exact(gpu, monkeypatch, level):
     assert exact(CudaStateVectorBackend.run(rl, mode="tiled").state().amplitudes(), want), level
 
 
-@pytest.mark.parametrize("chain,shape", [("0", ""), ("1", ""), ("2", ""), ("2", "256"),
-                                         ("2", "1x512"), ("0", "256")])
+@pytest.mark.parametrize("chain,shape", [("0", ""), ("1", ""), ("2", ""), ("3", ""),
+                                         ("3", "256"), ("3", "1x512"), ("0", "256")])
 def test_tiled_chains_bit_exact(gpu, monkeypatch, chain, shape):
-    """The tile pass applies runs of 1-qubit records in registers: runs on one
-    target with the same controls (pair chains) and uncontrolled runs over
-    two targets (quad chains).  Every chaining level (none, pair chains,
-    pair and quad chains) and every block shape of the pass (two blocks of
-    512 threads, three of 256 reading their records through L1, one of 512)
-    gives the oracle's bits, with every 1-qubit kind, controls inside and
-    outside the tile, and tiles of 4 to 12 qubits."""
+    """The tile pass applies runs of records in registers: 1-qubit runs on
+    one target with the same controls (pair chains), uncontrolled 1-qubit
+    runs over two targets (quad chains) and runs of diagonal records (Rz,
+    phase and controlled phase, CZ, Rzz: diagonal chains).  Every chaining
+    level (none, pair, pair and quad, pair, quad and diagonal) and every
+    block shape of the pass (two blocks of 512 threads, three of 256 reading
+    their records through L1, one of 512) gives the oracle's bits, with every
+    1-qubit kind, controls inside and outside the tile, and tiles of 4 to 12
+    qubits."""
     monkeypatch.setenv("EV_TILE_CHAIN", chain)
     if shape:
         monkeypatch.setenv("EV_TILE_THREADS", shape)
@@ -411,6 +413,13 @@ def test_tiled_chains_bit_exact(gpu, monkeypatch, chain, shape):
                     c.controlled(ctrl, GATES_1Q[int(rng.integers(0, len(GATES_1Q)))], q)
         for i in range(layer % 2, n - 1, 2):
             c.cnot(i, i + 1)
+        # a run of diagonal records: Rz, phase, controlled phase, CZ, Rzz
+        for i in range(n - 1):
+            [lambda: c.gate1(Gate1.rz(0.3 + i), i),
+             lambda: c.controlled([(i + 5) % n], Gate1.phase(0.2 * i), i),
+             lambda: c.gate2(Gate2.cz(), i, i + 1),
+             lambda: c.gate2(Gate2.rzz(0.1 + 0.05 * i), i, i + 1),
+             lambda: c.gate1(Gate1.t(), i)][(i + layer) % 5]()
     want, _, _ = O.run_seeded(c, 0)
     for tb in (4, 6, 9, 12):
         got = CudaStateVectorBackend.run(c, mode="tiled", tile_bits=tb).state().amplitudes()
