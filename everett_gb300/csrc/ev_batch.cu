@@ -341,12 +341,8 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 2) k_batch(BatchArgs a, in
         continue;
       }
       if ((base & op.emask) != op.emask) continue;
-      if (run > 1 && op.ctype == CH_QUAD)
-        tile_quad_chain(tile, size, rec, run, a.mats);
-      else if (run > 1 && op.ctype == CH_DIAG)
+      if (run > 1)  // CH_DIAG, the one kind the batch plans form
         tile_diag_chain(tile, size, rec, run, a.mats);
-      else if (run > 1)
-        tile_chain(tile, size >> op.nins, rec, run, a.mats);
       else
         apply_tile_op(tile, k, op, a.mats + op.mat);
       __syncthreads();
@@ -507,7 +503,10 @@ void plan_circuit(const ev_circuit* c, int kmax, bool c64, CircPlan* out) {
   if (passes.empty()) passes.push_back({{}, (uint64_t(1) << k) - 1});
   std::unordered_map<size_t, std::vector<uint32_t>> seen;  // hash -> offsets
   std::vector<TileOp> recs;
-  const ChainSet chains = chain_set("EV_BATCH_CHAIN", ChainSet{false, false, true});
+  // diagonal chains only: pair and quad chains, which read their records from
+  // global memory here (the tile pass stages them in shared memory), measured
+  // slower on the TFIM batch, and their code costs k_batch registers
+  const ChainSet chains{false, false, chain_set("EV_BATCH_CHAIN", ChainSet{false, false, true}).diag};
   for (const Pass& p : passes) {
     TilePlan plan{};
     plan.k = k;

@@ -391,7 +391,7 @@ template <typename V, typename Op>
 __device__ void tile_diag_chain(V* t, uint32_t size, const Op* ops, int run, const double* mats) {
   // one amplitude at a time for complex128: more live registers spill the
   // 64-register tile pass
-  constexpr int CH = sizeof(V) == 16 ? 1 : 8;
+  constexpr int CH = sizeof(V) == 16 ? 1 : 4;
   const uint32_t nb = blockDim.x;
   for (uint32_t l0 = threadIdx.x; l0 < size; l0 += CH * nb) {
     V a[CH];
