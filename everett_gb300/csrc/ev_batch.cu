@@ -64,6 +64,26 @@ __device__ __forceinline__ const double* rec_m(const BatchOp& op, const double* 
 }
 __device__ __forceinline__ uint32_t rec_sok(const BatchOp&) { return 0; }
 
+// Records staged in shared memory at a time, at most (the window is sized at
+// launch from the shared memory the block has left).
+constexpr uint32_t kMaxWindow = 32;
+
+// A staged matrix slot, in doubles: a 4x4 complex matrix (complex64 records
+// hold f32 pairs, pack_f32_matrix).
+template <typename V>
+__host__ __device__ constexpr uint32_t mat_slot_doubles() {
+  return sizeof(V) == 16 ? 32 : 16;
+}
+
+// The 16-byte words of a record's matrix that its kernel reads.
+template <typename V>
+__device__ __forceinline__ uint32_t mat_words(uint8_t kind) {
+  constexpr uint32_t full = mat_slot_doubles<V>() / 2;
+  if (kind == T_1Q) return full / 4;  // 2x2
+  if (kind == T_DIAG2 || kind == T_DENSE2) return full;
+  return 0;  // permutations, CZ, measurements, IfClassic prefixes
+}
+
 struct BatchCirc {
   uint32_t n, k, npasses, pad;
   uint32_t plan0, pass0;
@@ -103,6 +123,7 @@ struct BatchArgs {
   const TilePlan* plans;
   const BatchOp* ops;
   const double* mats;
+  uint32_t window;  // records staged in shared memory at a time (BatchWindow)
   unsigned* head;
   unsigned* done;
   int* err;
@@ -254,6 +275,12 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 2) k_batch(BatchArgs a, in
   V* tile = reinterpret_cast<V*>(sm);
   uint64_t* offs = reinterpret_cast<uint64_t*>(sm + (sizeof(V) << kmax));
   double* red = reinterpret_cast<double*>(offs + (size_t(1) << (kmax > 4 ? kmax - 4 : 0)));
+  // staged records and their matrices: [window records][window slots]
+  const size_t stage_at = (reinterpret_cast<size_t>(red + 2 * blockDim.x) + 15) & ~size_t(15);
+  BatchOp* srec = reinterpret_cast<BatchOp*>(stage_at);
+  double* smat = reinterpret_cast<double*>(srec + a.window);
+  constexpr uint32_t kSlot = mat_slot_doubles<V>();
+  __shared__ uint32_t s_matoff[kMaxWindow];
   __shared__ TilePlan plan;
   __shared__ unsigned s_item;
   __shared__ int s_ok;
@@ -324,28 +351,62 @@ __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 2) k_batch(BatchArgs a, in
     }
     bool take = true;  // the IfClassic prefixes read so far hold
     for (uint32_t o = 0; o < pr.nops;) {
-      const BatchOp* rec = a.ops + pr.op0 + o;
-      const BatchOp op = *rec;
-      // chains (run > 1) are formed only in circuits without classical ops
-      const int run = op.run > 1 ? op.run : 1;
-      o += run;
-      if (op.kind == B_IF) {
-        take = take && s_cl[op.lmask] != 0;
-        continue;
+      // stage the next window of records and their matrices (records point
+      // at their slot, smat + j * kSlot); a chain never spans more records
+      // than a window holds
+      const uint32_t cnt = min(a.window, pr.nops - o);
+      __syncthreads();  // the previous window is no longer read
+      for (uint32_t w = t; w < 2 * cnt; w += nb) {
+        uint4 v = reinterpret_cast<const uint4*>(a.ops + pr.op0 + o)[w];
+        if ((w & 1) == 0) {  // the first half holds BatchOp::mat (bytes 12..15)
+          s_matoff[w >> 1] = v.w;
+          v.w = (w >> 1) * kSlot;
+        }
+        reinterpret_cast<uint4*>(srec)[w] = v;
       }
-      const bool go = take;
-      take = true;
-      if (!go) continue;
-      if (op.kind == B_MEAS) {
-        batch_measure(tile, size, op.p0, op.lmask, red, s_cl, s_rng, s_meas);
-        continue;
-      }
-      if ((base & op.emask) != op.emask) continue;
-      if (run > 1)  // CH_DIAG, the one kind the batch plans form
-        tile_diag_chain(tile, size, rec, run, a.mats);
-      else
-        apply_tile_op(tile, k, op, a.mats + op.mat);
       __syncthreads();
+      for (uint32_t w = t; w < cnt * (kSlot / 2); w += nb) {
+        const uint32_t j = w / (kSlot / 2), x = w % (kSlot / 2);
+        if (x < mat_words<V>(srec[j].kind))
+          reinterpret_cast<uint4*>(smat + j * kSlot)[x] =
+              reinterpret_cast<const uint4*>(a.mats + s_matoff[j])[x];
+      }
+      __syncthreads();
+      uint32_t j = 0;
+      while (j < cnt) {
+        const BatchOp* rec = srec + j;
+        const BatchOp op = *rec;
+        // chains (run > 1) are formed only in circuits without classical ops
+        const uint32_t run = op.run > 1 ? op.run : 1;
+        if (j + run > cnt) break;  // the next window starts at this chain
+        j += run;
+        if (op.kind == B_IF) {
+          take = take && s_cl[op.lmask] != 0;
+          continue;
+        }
+        const bool go = take;
+        take = true;
+        if (!go) continue;
+        if (op.kind == B_MEAS) {
+          batch_measure(tile, size, op.p0, op.lmask, red, s_cl, s_rng, s_meas);
+          continue;
+        }
+        if ((base & op.emask) != op.emask) continue;
+        if (run > 1 && op.ctype == CH_QUAD)
+          tile_quad_chain(tile, size, rec, int(run), smat);
+        else if (run > 1 && op.ctype == CH_DIAG)
+          tile_diag_chain(tile, size, rec, int(run), smat);
+        else if (run > 1)
+          tile_chain(tile, size >> op.nins, rec, int(run), smat);
+        else
+          apply_tile_op(tile, k, op, smat + op.mat);
+        __syncthreads();
+      }
+      if (j == 0) {  // cannot happen (runs are capped at the window): stop cleanly
+        if (t == 0) atomicExch(a.err, 1);
+        break;
+      }
+      o += j;
     }
     if (classical && t < int(c.ncl)) a.cl[c.cl + t] = s_cl[t];
     for (uint32_t l = t; l < size; l += nb) {
@@ -480,7 +541,7 @@ bool has_classical_ops(const ev_circuit* c) {
   return false;
 }
 
-void plan_circuit(const ev_circuit* c, int kmax, bool c64, CircPlan* out) {
+void plan_circuit(const ev_circuit* c, int kmax, bool c64, uint32_t window, CircPlan* out) {
   const bool reorder = c64;  // complex64 may reorder commuting ops
   const int n = int(c->num_qubits);
   out->n = n;
@@ -503,10 +564,10 @@ void plan_circuit(const ev_circuit* c, int kmax, bool c64, CircPlan* out) {
   if (passes.empty()) passes.push_back({{}, (uint64_t(1) << k) - 1});
   std::unordered_map<size_t, std::vector<uint32_t>> seen;  // hash -> offsets
   std::vector<TileOp> recs;
-  // diagonal chains only: pair and quad chains, which read their records from
-  // global memory here (the tile pass stages them in shared memory), measured
-  // slower on the TFIM batch, and their code costs k_batch registers
-  const ChainSet chains{false, false, chain_set("EV_BATCH_CHAIN", ChainSet{false, false, true}).diag};
+  // diagonal chains by default: with the records staged in shared memory,
+  // pair and quad chains measured no faster on the TFIM batch (4096
+  // circuits: none 687, diagonal 673, pair and quad 700, all 677 ms)
+  const ChainSet chains = chain_set("EV_BATCH_CHAIN", ChainSet{false, false, true});
   for (const Pass& p : passes) {
     TilePlan plan{};
     plan.k = k;
@@ -532,7 +593,7 @@ void plan_circuit(const ev_circuit* c, int kmax, bool c64, CircPlan* out) {
       const ev_op& src = c->ops[p.ops[j]];
       if (src.kind != EV_OP_MEASURE && src.kind != EV_OP_IF) encode_op(c, src, p.tset, local, &recs[j]);
     }
-    if (!out->classical) mark_chains(recs.data(), recs.size(), chains);
+    if (!out->classical) mark_chains(recs.data(), recs.size(), chains, window);
     for (size_t jj = 0; jj < p.ops.size(); ++jj) {
       const ev_op& src = c->ops[p.ops[jj]];
       if (src.kind == EV_OP_MEASURE || src.kind == EV_OP_IF) {
@@ -652,6 +713,33 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
   int sms = 0;
   EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   const size_t ab = dtype == EV_C128 ? 16 : 8;
+  // shared memory: tile | row offsets | reduction scratch | staged records
+  // and matrices.  The record window is as large as fits without costing a
+  // resident CTA (at least 4 records).
+  const void* kfn = dtype == EV_C128
+                        ? (threads == 256 ? reinterpret_cast<const void*>(k_batch<double2, 256>)
+                                          : reinterpret_cast<const void*>(k_batch<double2, 512>))
+                        : (threads == 256 ? reinterpret_cast<const void*>(k_batch<float2, 256>)
+                                          : reinterpret_cast<const void*>(k_batch<float2, 512>));
+  EV_TRY(prepare_smem_kernel(kfn));
+  const size_t smem_base =
+      ((ab << kmax) + (size_t(8) << (kmax > 4 ? kmax - 4 : 0)) + 2 * size_t(threads) * 8 + 15) &
+      ~size_t(15);
+  const size_t per_rec = sizeof(BatchOp) + 8 * size_t(dtype == EV_C128 ? mat_slot_doubles<double2>()
+                                                                      : mat_slot_doubles<float2>());
+  int per_sm = 0;
+  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, smem_base + 4 * per_rec));
+  if (per_sm < 1) return fail(EV_ERR_INVALID_ARGUMENT, "batch: configuration does not fit an SM");
+  uint32_t window = 4;
+  for (uint32_t w = kMaxWindow; w > 4; w -= 4) {
+    int fit = 0;
+    EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, kfn, threads, smem_base + w * per_rec));
+    if (fit >= per_sm) {
+      window = w;
+      break;
+    }
+  }
+  const size_t smem = smem_base + window * per_rec;
   for (uint64_t i = 0; i < count; ++i)
     if (int(items[i].circuit.num_qubits) > kmax && has_classical_ops(&items[i].circuit))
       return fail(EV_ERR_INVALID_ARGUMENT,
@@ -667,7 +755,7 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
     for (unsigned w = 0; w < hw; ++w)
       pool.emplace_back([&, w] {
         for (uint64_t i = w; i < count; i += hw)
-          plan_circuit(&items[i].circuit, kmax, dtype == EV_C64, &cp[i]);
+          plan_circuit(&items[i].circuit, kmax, dtype == EV_C64, window, &cp[i]);
       });
     for (auto& th : pool) th.join();
   }
@@ -789,24 +877,15 @@ static int batch_once(Arena& A, const ev_batch_circuit* items, uint64_t count, i
   args.head = reinterpret_cast<unsigned*>(dp + p_head);
   args.err = reinterpret_cast<int*>(dp + p_head + 16);
   args.cl = dp + p_cl;
-  const size_t smem = (ab << kmax) + (size_t(8) << (kmax > 4 ? kmax - 4 : 0)) + 2 * size_t(threads) * 8;
+  args.window = window;
   const auto t1 = clk::now();
   EV_CUDA(cudaEventRecord(A.e0, A.stream));
   k_batch_uniforms<<<unsigned((count + 127) / 128), 128, 0, A.stream>>>(args.circs, count, args.uni);
-  int per_sm = 0;
-  const void* kfn = dtype == EV_C128
-                        ? (threads == 256 ? reinterpret_cast<const void*>(k_batch<double2, 256>)
-                                          : reinterpret_cast<const void*>(k_batch<double2, 512>))
-                        : (threads == 256 ? reinterpret_cast<const void*>(k_batch<float2, 256>)
-                                          : reinterpret_cast<const void*>(k_batch<float2, 512>));
-  EV_TRY(prepare_smem_kernel(kfn));
-  EV_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, threads, smem));
-  if (per_sm < 1) return fail(EV_ERR_INVALID_ARGUMENT, "batch: configuration does not fit an SM");
   // every CTA of the persistent grid must be resident (items wait on each other)
   const unsigned grid = unsigned(sms * per_sm);
   if (debug_enabled())
-    fprintf(stderr, "[ev] k_batch dtype %d tile %d threads %d smem %zu: %d CTAs/SM, %zu items\n",
-            dtype, kmax, threads, smem, per_sm, q.size());
+    fprintf(stderr, "[ev] k_batch dtype %d tile %d threads %d smem %zu window %u: %d CTAs/SM, %zu items\n",
+            dtype, kmax, threads, smem, window, per_sm, q.size());
   if (dtype == EV_C128 && threads == 256)
     k_batch<double2, 256><<<grid, threads, smem, A.stream>>>(args, kmax);
   else if (dtype == EV_C128)

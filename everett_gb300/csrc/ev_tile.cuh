@@ -398,17 +398,21 @@ __device__ void tile_diag_chain(V* t, uint32_t size, const Op* ops, int run, con
 #pragma unroll
     for (int j = 0; j < CH; ++j)
       if (l0 + j * nb < size) a[j] = t[l0 + j * nb];
+    // not unrolled: with the compiler's unrolling this loop ran no iteration
+    // for a 2-record chain of the batched runner (its records in shared
+    // memory or in global memory alike; found by device printf, fixed by this
+    // pragma or by ptxas -O0)
+#pragma unroll 1
     for (int r = 0; r < run; ++r) {
       const Op& op = ops[r];
       const double* mm = rec_m(op, mats);
+      const int kind = op.kind;
       const uint32_t b0 = 1u << op.p0;
-      if (op.kind == T_1Q) {
-        const uint32_t lmask = op.lmask;
+      if (kind == T_1Q) {
         const int k1 = op.k1;
-        if (k1 == K1_IDENT) continue;
+        const uint32_t lmask = op.lmask;
         const V e0 = ldm<V>(mm, 0), e3 = ldm<V>(mm, 3);
         bool soft0 = false, soft1 = false;
-        const softfp::Unpacked* u = reinterpret_cast<const softfp::Unpacked*>(mm + 8);
         if constexpr (std::is_same<V, double2>::value) {
           soft0 = op.soft && rec_sok(op);
           soft1 = soft0 && op.soft == 2;
@@ -416,35 +420,37 @@ __device__ void tile_diag_chain(V* t, uint32_t size, const Op* ops, int run, con
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
           const uint32_t l = l0 + j * nb;
-          if ((l & lmask) != lmask) continue;  // a local control is 0
           const bool one = (l & b0) != 0;
-          if (k1 == K1_PHASE && !one) continue;
-          if constexpr (std::is_same<V, double2>::value) {
-            if (one ? soft1 : soft0) {
-              a[j] = soft_diag(one ? e3 : e0, u[one ? 3 : 0], a[j]);
-              continue;
+          // identity records, amplitudes with a local control at 0 and the
+          // 0 row of a phase record keep their value
+          if (k1 != K1_IDENT && (l & lmask) == lmask && (one || k1 != K1_PHASE)) {
+            bool done = false;
+            if constexpr (std::is_same<V, double2>::value) {
+              if (one ? soft1 : soft0) {
+                const softfp::Unpacked* u = reinterpret_cast<const softfp::Unpacked*>(mm + 8);
+                a[j] = soft_diag(one ? e3 : e0, u[one ? 3 : 0], a[j]);
+                done = true;
+              }
             }
+            if (!done) a[j] = cmul(one ? e3 : e0, a[j]);
           }
-          a[j] = cmul(one ? e3 : e0, a[j]);
         }
-        continue;
-      }
-      const uint32_t b1 = 1u << op.p1;
-      if (op.kind == T_CZ) {
+      } else if (kind == T_CZ) {
+        const uint32_t b1 = 1u << op.p1;
 #pragma unroll
         for (int j = 0; j < CH; ++j) {
           const uint32_t l = l0 + j * nb;
           if ((l & b0) && (l & b1)) a[j] = cneg(a[j]);
         }
-        continue;
-      }
-      // T_DIAG2: entry 5c with c = 2 * bit(p0) + bit(p1), as tile_2q maps them
-      const V d0 = ldm<V>(mm, 0), d1 = ldm<V>(mm, 5), d2 = ldm<V>(mm, 10), d3 = ldm<V>(mm, 15);
+      } else {  // T_DIAG2: entry 5c with c = 2 * bit(p0) + bit(p1), as tile_2q maps them
+        const uint32_t b1 = 1u << op.p1;
+        const V d0 = ldm<V>(mm, 0), d1 = ldm<V>(mm, 5), d2 = ldm<V>(mm, 10), d3 = ldm<V>(mm, 15);
 #pragma unroll
-      for (int j = 0; j < CH; ++j) {
-        const uint32_t l = l0 + j * nb;
-        const V d = (l & b0) ? ((l & b1) ? d3 : d2) : ((l & b1) ? d1 : d0);
-        a[j] = cmul(d, a[j]);
+        for (int j = 0; j < CH; ++j) {
+          const uint32_t l = l0 + j * nb;
+          const V d = (l & b0) ? ((l & b1) ? d3 : d2) : ((l & b1) ? d1 : d0);
+          a[j] = cmul(d, a[j]);
+        }
       }
     }
 #pragma unroll
@@ -639,18 +645,19 @@ inline bool is_diag_rec(const TileOp& o) {
 // whose targets are two local positions becomes a quad chain (lo/hi set on
 // its first record); a run on one target with the same controls becomes a
 // pair chain; a longer run of diagonal records with the same outside
-// controls becomes a diagonal chain instead.  Only the kinds in cs form.
-inline void mark_chains(TileOp* ops, size_t nops, ChainSet cs) {
+// controls becomes a diagonal chain instead.  Only the kinds in cs form, and
+// no chain is longer than maxrun records.
+inline void mark_chains(TileOp* ops, size_t nops, ChainSet cs, size_t maxrun = 255) {
   const bool quads = cs.quads, diag = cs.diag;
   for (size_t j = 0; j < nops;) {
     TileOp& h = ops[j];
     size_t d = j;
     if (diag)
-      while (d < nops && d - j < 255 && is_diag_rec(ops[d]) && ops[d].emask == h.emask) ++d;
+      while (d < nops && d - j < maxrun && is_diag_rec(ops[d]) && ops[d].emask == h.emask) ++d;
     size_t e = j + 1;
     int t2 = -1;
     if (h.kind == T_1Q && h.lmask == 0 && quads) {
-      while (e < nops && e - j < 255 && ops[e].kind == T_1Q && ops[e].lmask == 0 &&
+      while (e < nops && e - j < maxrun && ops[e].kind == T_1Q && ops[e].lmask == 0 &&
              ops[e].emask == h.emask) {
         const int p = ops[e].p0;
         if (p != h.p0 && p != t2) {
@@ -660,7 +667,7 @@ inline void mark_chains(TileOp* ops, size_t nops, ChainSet cs) {
         ++e;
       }
     } else if (h.kind == T_1Q && cs.pairs) {
-      while (e < nops && e - j < 255 && ops[e].kind == T_1Q && ops[e].p0 == h.p0 &&
+      while (e < nops && e - j < maxrun && ops[e].kind == T_1Q && ops[e].p0 == h.p0 &&
              ops[e].lmask == h.lmask && ops[e].emask == h.emask)
         ++e;
     }

@@ -33,10 +33,13 @@ def oracle_expz(amps):
     return b[2] / O.norm_sqr(amps)
 
 
-@pytest.mark.parametrize("tile_bits,chain", [(6, ""), (8, ""), (12, ""), (8, "0"), (12, "d")])
+@pytest.mark.parametrize("tile_bits,chain", [(6, ""), (8, ""), (12, ""), (8, "0"), (6, "pqd"),
+                                             (12, "pq")])
 def test_batch_c128_bit_exact(gpu, monkeypatch, tile_bits, chain):
-    """Batched complex128 runs give the oracle's bits at every tile size, with
-    and without diagonal chains (TFIM steps chain their Rzz records)."""
+    """Batched complex128 runs give the oracle's bits at every tile size and
+    with every kind of chain (TFIM steps chain their Rzz records as diagonal
+    chains, their Rx records as quad chains); records reach the kernel
+    through shared-memory windows, so long circuits span many windows."""
     if chain:
         monkeypatch.setenv("EV_BATCH_CHAIN", chain)
     else:
