@@ -389,9 +389,9 @@ def extras_c128_fused(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, p
                        ncu_figure("k_fused_oz_c128", "traffic_bytes_per_launch_full_size"))
     if roof:
         # digit-pair MMAs per launch: 2^n / 4096 steps x 2 halves x
-        # nd(nd+1)/2 pairs x 4 K-steps of 128 x 32 x 16 -- 7168 flops per
-        # amplitude with seven digits, 5376 with six
-        flops = 256.0 * nd * (nd + 1) * (1 << n)
+        # nd(nd+1)/2 pairs x 4 K-steps of 2 x 128 x 32 x 16 flops -- 7168
+        # flops per amplitude with seven digits, 5376 with six
+        flops = 128.0 * nd * (nd + 1) * (1 << n)
         tf = flops / (roof["avg_launch_ms"] / 1e3) / 1e12
         bf = bf16_peak()
         roof["tensor"] = {"achieved_tflops": round(tf, 1), "peak_tflops": bf[0],

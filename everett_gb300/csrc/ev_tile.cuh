@@ -60,10 +60,10 @@ static_assert(sizeof(TileOp) % 16 == 0, "op records are staged with 16-byte copi
 // CH_PAIR  1-qubit records on one target with the same controls, applied to
 //          pairs held in registers;
 // CH_QUAD  uncontrolled 1-qubit records on two targets, applied to quads;
-// CH_DIAG  diagonal records (diagonal and phase 1-qubit records with any
-//          local controls, CZ, diagonal 2-qubit records), applied to each
-//          amplitude in turn: a diagonal record multiplies every amplitude
-//          by the entry its index selects, independently of the others.
+// CH_DIAG  diagonal records (uncontrolled diagonal and phase 1-qubit
+//          records, CZ, diagonal 2-qubit records), applied to each amplitude
+//          in turn: a diagonal record multiplies every amplitude by the entry
+//          its index selects, independently of the others.
 enum ChainKind : uint8_t { CH_PAIR = 0, CH_QUAD = 1, CH_DIAG = 2 };
 
 // The matrix and integer-pipe flag of a record; records kept elsewhere (the
@@ -635,9 +635,15 @@ inline ChainSet chain_set(const char* var, ChainSet dflt) {
   return c;
 }
 
+// Records a diagonal chain takes: CZ, diagonal 2-qubit records, and
+// diagonal, phase and identity 1-qubit records without local controls.  A
+// locally controlled record touches a fraction of the tile on its own, which
+// a chain would test amplitude by amplitude (30-qubit QFT, whose controlled
+// phases would chain: 1.59 -> 1.93 s with them in).
 inline bool is_diag_rec(const TileOp& o) {
   if (o.kind == T_CZ || o.kind == T_DIAG2) return true;
-  return o.kind == T_1Q && (o.k1 == K1_DIAG || o.k1 == K1_PHASE || o.k1 == K1_IDENT);
+  return o.kind == T_1Q && o.lmask == 0 &&
+         (o.k1 == K1_DIAG || o.k1 == K1_PHASE || o.k1 == K1_IDENT);
 }
 
 // Marks the chains of a pass's records (TileOp::run, TileOp::ctype).  A run
