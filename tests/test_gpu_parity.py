@@ -389,7 +389,7 @@ def test_tiled_chains_bit_exact(gpu, monkeypatch, chain, shape):
     """The tile pass applies runs of records in registers: 1-qubit runs on
     one target with the same controls (pair chains), uncontrolled 1-qubit
     runs over two targets (quad chains) and runs of diagonal records (Rz,
-    phase, CZ, Rzz: diagonal chains, which controlled phases break).  Every chaining
+    phase, Rzz: diagonal chains, which CZ and controlled phases break).  Every chaining
     level (none, pair, pair and quad, pair, quad and diagonal) and every
     block shape of the pass (two blocks of 512 threads, three of 256 reading
     their records through L1, one of 512) gives the oracle's bits, with every
