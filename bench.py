@@ -757,10 +757,13 @@ def extras_kernels(n: int, peak: float, reps: int = 3):
     L = N.lib()
     rate = C.c_double()
     N.check(L.ev_probe_fp64(C.byref(rate)))
+    soft_add = C.c_double()
+    N.check(L.ev_probe_softadd(C.byref(soft_add)))
     g_dense = workloads.haar_1q(Rng.seed_from_u64(5))
     rng = np.random.default_rng(3)
     g2 = Gate2(rng.normal(size=16) + 1j * rng.normal(size=16))
-    out = {"fp64_fma_per_s_measured": float(f"{rate.value:.4g}")}
+    out = {"fp64_fma_per_s_measured": float(f"{rate.value:.4g}"),
+           "integer_pipe_add_per_s_measured": float(f"{soft_add.value:.4g}")}
     prng = np.random.default_rng(9)
     zdiag = ["+" + "".join("Z" if b else "I" for b in prng.integers(0, 2, n)) for _ in range(8)]
     # eight strings with one X part and one Y pattern (one pass), Z varying

@@ -129,6 +129,8 @@ _SIGS = {
     "ev_probe_fp64": [_DP],
     "ev_marginal_low": [_P, _U64, _DP],
     "ev_softfp_check": [_U64, _U64, C.POINTER(_U64)],
+    "ev_softfp_add_check": [_U64, _U64, C.POINTER(_U64)],
+    "ev_probe_softadd": [_DP],
     "ev_ff_check": [_U64, _U64, C.POINTER(_U64)],
     "ev_ozaki_gemm_host": [_DP, _U64, _DP, _DP],
     "ev_ozaki_gemm_host_digits": [_DP, _U64, _DP, _DP, _I32],

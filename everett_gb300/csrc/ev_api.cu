@@ -23,6 +23,7 @@
 
 #include "ev_device.cuh"
 #include "ev_internal.h"
+#include "ev_softfp.cuh"
 
 namespace ev {
 
@@ -886,7 +887,73 @@ __global__ void __launch_bounds__(256) k_probe_fp64(double* out, int iters, doub
   for (int c = 0; c < 8; ++c) t += a[c];
   if (t == -1.0) out[0] = t;
 }
+// Independent chains of integer-pipe adds (softfp::add), as k_probe_fp64
+// runs FMA chains: the rate against which moving an add off the FP64 pipe
+// is weighed.
+__global__ void __launch_bounds__(256) k_probe_softadd(double* out, int iters, double seed) {
+  double a[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) a[c] = seed + double(threadIdx.x + c);
+  const double add = 1.0000001e-7;
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) a[c] = softfp::add(a[c], add);
+  double t = 0.0;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) t += a[c];
+  if (t == -1.0) out[0] = t;
+}
 }  // namespace ev
+
+// Best of three timed launches of a probe kernel: operations per second
+// (blocks x 256 threads x iters x 8 chains per launch time).
+static int probe_rate(void (*kernel)(double*, int, double), int iters, const char* name,
+                      double* per_s) {
+  using namespace ev;
+  int dev = 0, sms = 0;
+  EV_CUDA(cudaGetDevice(&dev));
+  EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  cudaStream_t st = nullptr;
+  EV_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  double* out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = EV_OK;
+  const int blocks = sms * 8;
+  if (cudaMallocAsync(reinterpret_cast<void**>(&out), sizeof(double), st) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    rc = fail(EV_ERR_CUDA, "%s: setup failed", name);
+  } else {
+    kernel<<<blocks, 256, 0, st>>>(out, iters, 1.0);  // warm-up
+    double best = 0.0;
+    for (int rep = 0; rep < 3 && rc == EV_OK; ++rep) {
+      cudaEventRecord(e0, st);
+      kernel<<<blocks, 256, 0, st>>>(out, iters, 2.0 + rep);
+      cudaEventRecord(e1, st);
+      float ms = 0.f;
+      if (cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess || ms <= 0.f) {
+        rc = fail(EV_ERR_CUDA, "%s: timing failed", name);
+      } else {
+        const double r = double(blocks) * 256.0 * double(iters) * 8.0 / (double(ms) * 1e-3);
+        if (r > best) best = r;
+      }
+    }
+    if (rc == EV_OK) *per_s = best;
+  }
+  if (out) cudaFreeAsync(out, st);
+  cudaStreamSynchronize(st);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamDestroy(st);
+  cudaGetLastError();
+  return rc;
+}
+
+extern "C" int ev_probe_softadd(double* adds_per_s) {
+  ev::clear_error();
+  if (!adds_per_s) return ev::fail(EV_ERR_INVALID_ARGUMENT, "ev_probe_softadd: null output");
+  return probe_rate(ev::k_probe_softadd, 1 << 12, "ev_probe_softadd", adds_per_s);
+}
 
 extern "C" int ev_probe_fp64(double* fma_per_s) {
   clear_error();

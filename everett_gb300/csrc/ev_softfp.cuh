@@ -1,5 +1,5 @@
-// ev_softfp.cuh -- IEEE-754 binary64 multiplication, round to nearest even,
-// computed on the integer pipes.
+// ev_softfp.cuh -- IEEE-754 binary64 multiplication and addition, round to
+// nearest even, computed on the integer pipes.
 //
 // GB300's FP64 pipe retires about 0.53e12 fused multiply-adds per second,
 // far below its integer and FP32 pipes, and the complex128 gate passes are
@@ -18,7 +18,7 @@
 // equals it and the kept part is odd.
 //
 // The header compiles for the host too (g++), where the CPU tests compare it
-// with the host's own multiplication.
+// with the host's own multiplication and addition.
 #pragma once
 
 #include <stdint.h>
@@ -127,6 +127,67 @@ EV_SOFT_FN double mul(const Unpacked& a, const Unpacked& b) {
   // exponent, and a significand that rounded up to 2^53 carries into it.
   const uint32_t word = a.ex + b.ex + (top << 20);
   return from_bits(((uint64_t)word << 32) + m);
+}
+
+// Leading zeros of a nonzero 64-bit value.
+EV_SOFT_FN uint32_t clz64(uint64_t x) {
+#ifdef __CUDA_ARCH__
+  return (uint32_t)__clzll((long long)x);
+#else
+  return (uint32_t)__builtin_clzll(x);
+#endif
+}
+
+// True when x and y are both in the add's domain: normal, biased exponent in
+// [512, 1534] (the product's domain), where a sum can neither overflow nor
+// fall below the normal range.
+EV_SOFT_FN bool add_ok(double x, double y) {
+  const uint32_t ex = (uint32_t)(to_bits(x) >> 52) & 0x7FFu, ey = (uint32_t)(to_bits(y) >> 52) & 0x7FFu;
+  return ex - 512u <= 1022u && ey - 512u <= 1022u;
+}
+
+// RN(x + y) for add_ok(x, y); any value otherwise.  The larger magnitude
+// fixes the sign and exponent; the smaller significand is aligned to it with
+// a sticky bit (10 guard bits below the 53, so an alignment of 0 or 1 bit is
+// exact and a larger one leaves at most one left shift after a subtraction);
+// the sum is normalised with a leading-zero count and rounded to nearest
+// even.  An exact cancellation gives +0, as round to nearest does.  Written
+// from the IEEE-754 definition of addition; it costs ~60 integer
+// instructions, against one FP64 add.
+EV_SOFT_FN double add(double x, double y) {
+  const uint64_t kSign = 1ull << 63, kFrac = (1ull << 52) - 1, kHidden = 1ull << 52;
+  uint64_t ux = to_bits(x), uy = to_bits(y);
+  uint64_t ax = ux & ~kSign, ay = uy & ~kSign;
+  if (ax < ay) {
+    const uint64_t tu = ux, ta = ax;
+    ux = uy;
+    uy = tu;
+    ax = ay;
+    ay = ta;
+  }
+  const uint32_t ex = (uint32_t)(ax >> 52), ey = (uint32_t)(ay >> 52);
+  const uint32_t d = ex - ey;
+  const uint64_t X = ((ax & kFrac) | kHidden) << 10;  // leading 1 at bit 62
+  const uint64_t Y = ((ay & kFrac) | kHidden) << 10;
+  uint64_t yd;
+  if (d == 0)
+    yd = Y;
+  else if (d < 64)
+    yd = (Y >> d) | (uint64_t)((Y << (64 - d)) != 0);
+  else
+    yd = 1;  // below every kept and rounding bit: a sticky bit only
+  const uint64_t S = ((ux ^ uy) & kSign) ? X - yd : X + yd;
+  if (S == 0) return 0.0;
+  const uint32_t lz = clz64(S);  // 0: a carry into bit 63; 1: none; more: cancellation
+  const uint64_t sn = S << lz;   // leading 1 at bit 63
+  const uint64_t kept = sn >> 11;
+  const uint32_t low = (uint32_t)sn & 0x7FFu;
+  // round up above half an ulp, or at half with an odd kept part; a sticky
+  // bit from the alignment leaves low odd below bit 10, never at half
+  const uint64_t m = kept + (uint64_t)((low + (uint32_t)(kept & 1)) > 0x400u);  // [2^52, 2^53]
+  // the value's exponent is ex + 1 - lz; the significand's leading 1 (or a
+  // rounding carry to 2^53) adds the one back into the exponent field
+  return from_bits((ux & kSign) + ((uint64_t)(ex - lz) << 52) + m);
 }
 
 }  // namespace softfp

@@ -78,16 +78,31 @@ __host__ __device__ inline uint32_t soft_factors(int k1, const double* m, softfp
   }
 }
 
+// x + y, on the integer pipes (softfp::add) when soft is set and both
+// operands are in its domain, else on the FP64 pipe: the same bits.
+__device__ __forceinline__ double sadd(double x, double y, bool soft) {
+  return (soft && softfp::add_ok(x, y)) ? softfp::add(x, y) : __dadd_rn(x, y);
+}
+
 // new0 = m0*a0 + m1*a1, new1 = m2*a0 + m3*a1 for a record of kind K1 (REAL,
 // DENSE, DIAG or PHASE; PHASE reads and writes a1 only), with the products
-// of new0 (both == false) or of both outputs on the integer pipes.
+// of new0 (both == false) or of both outputs on the integer pipes; for REAL
+// records with both set, the first nadd of the four output parts' adds too.
 template <int K1>
-__device__ __forceinline__ void soft_pair(double2& a0, double2& a1, const SoftM1& f, bool both) {
+__device__ __forceinline__ void soft_pair(double2& a0, double2& a1, const SoftM1& f, bool both,
+                                          int nadd = 0) {
   if constexpr (K1 == K1_REAL || K1 == K1_DENSE) {
     const SoftAmp s0 = sunpack(a0), s1 = sunpack(a1);
     double2 n0, n1;
     if (sok(s0) & sok(s1)) {
       if constexpr (K1 == K1_REAL) {
+        if (both && nadd > 0) {  // uniform across the block
+          const double2 p0 = srmul(f.u0, s0), q0 = srmul(f.u1, s1);
+          const double2 p1 = srmul(f.u2, s0), q1 = srmul(f.u3, s1);
+          a0 = make_double2(sadd(p0.x, q0.x, nadd >= 1), sadd(p0.y, q0.y, nadd >= 2));
+          a1 = make_double2(sadd(p1.x, q1.x, nadd >= 3), sadd(p1.y, q1.y, nadd >= 4));
+          return;
+        }
         n0 = cadd(srmul(f.u0, s0), srmul(f.u1, s1));
         n1 = both ? cadd(srmul(f.u2, s0), srmul(f.u3, s1))
                   : cadd(rmul(f.m2.x, a0), rmul(f.m3.x, a1));

@@ -45,14 +45,16 @@ static int tile_shape() {
 
 // How many amplitudes of each pair have their complex128 products formed on
 // the integer pipes (TileOp::soft), for real-matrix records and for the
-// others.  EV_TILE_SOFT="rd" (two digits 0-2) overrides both.
+// others.  EV_TILE_SOFT="rd" overrides both: d in 0-2, r in 0-6, where 3-6
+// also form the first r - 2 of a real record's four adds per pair on the
+// integer pipes (softfp::add).  All give the same results.
 struct SoftLevels {
   int real, other;
 };
 constexpr SoftLevels kDefaultSoft{2, 2};
 static SoftLevels tile_soft_levels() {
   const char* e = getenv("EV_TILE_SOFT");
-  if (e == nullptr || e[0] < '0' || e[0] > '2' || e[1] < '0' || e[1] > '2' || e[2] != 0)
+  if (e == nullptr || e[0] < '0' || e[0] > '6' || e[1] < '0' || e[1] > '2' || e[2] != 0)
     return kDefaultSoft;
   return SoftLevels{e[0] - '0', e[1] - '0'};
 }
@@ -339,6 +341,39 @@ __global__ void k_softfp_check(uint64_t seed, uint64_t per_thread, unsigned long
   if (mine) atomicAdd(bad, mine);
 }
 
+// softfp::add against the FP64 add: first operands from the product check's
+// families, second operands from the same families or made from the first
+// (opposite sign with changed low bits: cancellation; exponent gaps of 50..66
+// with a random or an empty fraction: the alignment's edges and exact ties).
+__global__ void k_softadd_check(uint64_t seed, uint64_t per_thread, unsigned long long* bad) {
+  const uint64_t gid = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  uint64_t st = seed ^ (gid * 0xA0761D6478BD642FULL);
+  unsigned long long mine = 0;
+  for (uint64_t i = 0; i < per_thread; ++i) {
+    const int fam = int((gid + i) % 40);
+    const double a = check_operand(st, fam % 5);
+    const int fb = fam / 5;
+    double b;
+    if (fb < 5) {
+      b = check_operand(st, fb);
+    } else if (fb == 5) {
+      const uint64_t r = check_next(st);
+      const int k = int(r % 53);
+      const uint64_t flip = k ? (check_next(st) & ((1ull << k) - 1)) : 0;
+      b = __longlong_as_double((long long)((uint64_t(__double_as_longlong(a)) ^ flip) ^ (1ull << 63)));
+    } else {
+      const uint64_t r = check_next(st), ua = uint64_t(__double_as_longlong(a));
+      const uint64_t ea = (ua >> 52) & 0x7FF, gap = 50 + r % 17;
+      const uint64_t eb = ea < 512 + gap ? 512 : ea - gap;
+      const uint64_t frac = fb == 6 ? (check_next(st) & ((1ull << 52) - 1)) : 0;
+      b = __longlong_as_double((long long)(((r >> 40) & 1) << 63 | eb << 52 | frac));
+    }
+    const double got = softfp::add(a, b), want = __dadd_rn(a, b);
+    mine += (!softfp::add_ok(a, b)) || __double_as_longlong(got) != __double_as_longlong(want);
+  }
+  if (mine) atomicAdd(bad, mine);
+}
+
 // ff_to_f64 (ev_device.cuh) against the FP64 add of the pair's two exact
 // f64 values, on renormalised double-float pairs (TwoSum of random floats
 // whose exponents differ by 0..80, with ties and cancellations).
@@ -388,6 +423,36 @@ extern "C" int ev_ff_check(uint64_t seed, uint64_t count, uint64_t* mismatches) 
   cudaFree(d);
   if (rc == EV_OK) *mismatches = h;
   return rc;
+}
+
+static int run_soft_check(const char* name, void (*kernel)(uint64_t, uint64_t, unsigned long long*),
+                          uint64_t seed, uint64_t count, uint64_t* mismatches) {
+  using namespace ev;
+  if (!mismatches) return fail(EV_ERR_INVALID_ARGUMENT, "%s: null output", name);
+  int dev = 0, sms = 0;
+  EV_CUDA(cudaGetDevice(&dev));
+  EV_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const uint64_t threads = uint64_t(sms) * 4 * 256;
+  const uint64_t per = (count + threads - 1) / threads;
+  unsigned long long* d = nullptr;
+  EV_CUDA(cudaMalloc(reinterpret_cast<void**>(&d), sizeof(*d)));
+  int rc = EV_OK;
+  unsigned long long h = 0;
+  if (cudaMemset(d, 0, sizeof(*d)) != cudaSuccess) {
+    rc = fail(EV_ERR_CUDA, "%s: memset failed", name);
+  } else {
+    kernel<<<unsigned(sms * 4), 256>>>(seed, per, d);
+    if (cudaMemcpy(&h, d, sizeof(h), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = fail(EV_ERR_CUDA, "%s: kernel failed", name);
+  }
+  cudaFree(d);
+  if (rc == EV_OK) *mismatches = h;
+  return rc;
+}
+
+extern "C" int ev_softfp_add_check(uint64_t seed, uint64_t count, uint64_t* mismatches) {
+  ev::clear_error();
+  return run_soft_check("ev_softfp_add_check", ev::k_softadd_check, seed, count, mismatches);
 }
 
 extern "C" int ev_softfp_check(uint64_t seed, uint64_t count, uint64_t* mismatches) {

@@ -37,7 +37,8 @@ struct __align__(16) TileOp {
   uint8_t nins;    // T_1Q: number of sorted positions in ins[]
   uint8_t soft;    // complex128 T_1Q: products on the integer pipes
                    // (ev_softfp.cuh): 0 none, 1 first amplitude of each
-                   // pair, 2 both
+                   // pair, 2 both; real-matrix records 3..6: both, and the
+                   // adds of the first soft - 2 output parts too
   uint32_t lmask;  // local control mask
   uint8_t run;     // records from this one on that form a chain (T_1Q
                    // records on the same target with the same controls,
@@ -126,7 +127,8 @@ __device__ __forceinline__ void tile_1q_soft(double2* t, uint32_t count, const O
     tile_1q_fp64<K1>(t, count, op, mm);
     return;
   }
-  const bool both = op.soft == 2;
+  const bool both = op.soft >= 2;
+  const int nadd = op.soft > 2 ? op.soft - 2 : 0;
   const uint32_t tbit = 1u << op.p0, lmask = op.lmask;
   const int nins = op.nins;
   const uint64_t ins = op.ins;
@@ -137,11 +139,11 @@ __device__ __forceinline__ void tile_1q_soft(double2* t, uint32_t count, const O
     const uint32_t i0 = j | lmask, i1 = i0 | tbit;
     if constexpr (K1 == K1_PHASE) {
       double2 a0 = make_double2(0.0, 0.0), a1 = t[i1];
-      soft_pair<K1>(a0, a1, f, both);
+      soft_pair<K1>(a0, a1, f, both, nadd);
       t[i1] = a1;
     } else {
       double2 a0 = t[i0], a1 = t[i1];
-      soft_pair<K1>(a0, a1, f, both);
+      soft_pair<K1>(a0, a1, f, both, nadd);
       t[i0] = a0;
       t[i1] = a1;
     }
@@ -312,9 +314,10 @@ __device__ __forceinline__ void chain_rec(const Op& op, const double* mats, V& a
       f.u2 = u[2];
       f.u3 = u[3];
       f.ok = 1;
-      const bool both = op.soft == 2;
-      soft_pair<K1>(a0, a1, f, both);
-      soft_pair<K1>(b0, b1, f, both);
+      const bool both = op.soft >= 2;
+      const int nadd = op.soft > 2 ? op.soft - 2 : 0;
+      soft_pair<K1>(a0, a1, f, both, nadd);
+      soft_pair<K1>(b0, b1, f, both, nadd);
       return;
     }
   }
@@ -434,7 +437,7 @@ __device__ void tile_diag_chain(V* t, uint32_t size, const Op* ops, int run, con
         bool soft0 = false, soft1 = false;
         if constexpr (std::is_same<V, double2>::value) {
           soft0 = op.soft && rec_sok(op);
-          soft1 = soft0 && op.soft == 2;
+          soft1 = soft0 && op.soft >= 2;
         }
 #pragma unroll
         for (int j = 0; j < CH; ++j) {

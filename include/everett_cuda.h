@@ -484,6 +484,13 @@ int ev_probe_fp64(double* fma_per_s);
  * (families that reach every rounding case); *mismatches = pairs whose bits
  * differ.  A check of the build, for tests. */
 int ev_softfp_check(uint64_t seed, uint64_t count, uint64_t* mismatches);
+/* The same check for the integer-pipe double add (softfp::add) against the
+ * FP64 add, with second operands that cancel the first or sit at the
+ * alignment's exponent gaps.  A check of the build, for tests. */
+int ev_softfp_add_check(uint64_t seed, uint64_t count, uint64_t* mismatches);
+/* Measured rate of the integer-pipe double add (adds per second, from
+ * independent chains on every SM), beside ev_probe_fp64's FMA rate. */
+int ev_probe_softadd(double* adds_per_s);
 /* Checks the integer-pipe rounding of a double-float pair to f64 (the
  * complex64 sampling tree's leaves) against the FP64 add on `count` pairs;
  * *mismatches = pairs whose bits differ.  A check of the build, for tests. */

@@ -1,8 +1,11 @@
-// Compares ev::softfp::mul (everett_gb300/csrc/ev_softfp.cuh) with the
-// host's IEEE-754 multiplication, bit for bit, over operand families that
-// reach every rounding case: full random significands, short significands
-// (exact products and exact ties), significands next to 1 and 2 (carries into
-// the exponent), and the edges of the fast-path exponent range.
+// Compares ev::softfp::mul and ev::softfp::add (everett_gb300/csrc/
+// ev_softfp.cuh) with the host's IEEE-754 multiplication and addition, bit
+// for bit, over operand families that reach every rounding case: full random
+// significands, short significands (exact results and exact ties),
+// significands next to 1 and 2 (carries into the exponent), the edges of the
+// fast-path exponent range, and for sums second operands that cancel the
+// first (equal or nearly equal magnitudes of opposite sign) or sit at
+// exponent gaps around the 53-bit significand and the 64-bit alignment.
 //
 // Usage: test_softfp COUNT_PER_FAMILY SEED
 #include <cmath>
@@ -75,6 +78,53 @@ int main(int argc, char** argv) {
       }
     }
   }
+  // sums: the same families for both operands, then second operands made
+  // from the first (cancellation, exponent gaps at the alignment edges)
+  long long bad_add = 0, checked_add = 0;
+  for (int fa = 0; fa < 5; ++fa) {
+    for (int fb = 0; fb < 8; ++fb) {
+      for (long long i = 0; i < count / 40 + 1; ++i) {
+        const double a = family(fa);
+        double b;
+        if (fb < 5) {
+          b = family(fb);
+        } else if (fb == 5) {  // opposite sign, low bits changed: cancellation
+          const int k = int(next() % 53);  // fraction bits only
+          const uint64_t flip = k ? (next() & ((1ull << k) - 1)) : 0;
+          b = from_bits((to_bits(a) ^ flip) ^ (1ull << 63));
+        } else {  // a gap of 50..66 exponents below a, either sign
+          const uint64_t ua = to_bits(a);
+          const uint64_t ea = (ua >> 52) & 0x7FF;
+          const uint64_t gap = 50 + next() % 17;
+          const uint64_t eb = ea - gap < 512 ? 512 : ea - gap;
+          const uint64_t frac = fb == 6 ? next() : 0;  // fb 7: a power of two, exact ties
+          b = make(next() & 1, eb, frac);
+        }
+        if (!ev::softfp::add_ok(a, b)) {
+          std::printf("FAIL add domain: %a %a reported outside\n", a, b);
+          return 1;
+        }
+        volatile double want = a + b;
+        const double got = ev::softfp::add(a, b);
+        const double got2 = ev::softfp::add(b, a);
+        ++checked_add;
+        if (to_bits(got) != to_bits(want) || to_bits(got2) != to_bits(want)) {
+          if (++bad_add <= 10) std::printf("FAIL %a + %a: got %a / %a want %a\n", a, b, got, got2, (double)want);
+        }
+      }
+    }
+  }
+  // exact cancellation is +0; the domain excludes zeros, subnormals, inf, NaN
+  if (to_bits(ev::softfp::add(1.5, -1.5)) != to_bits(0.0)) {
+    std::printf("FAIL 1.5 + -1.5 is not +0\n");
+    return 1;
+  }
+  if (ev::softfp::add_ok(0.0, 1.0) || ev::softfp::add_ok(1.0, INFINITY) || ev::softfp::add_ok(NAN, 1.0)) {
+    std::printf("FAIL add domain accepted a zero, an infinity or a NaN\n");
+    return 1;
+  }
+  std::printf("%lld sums checked, %lld sum mismatches\n", checked_add, bad_add);
+  bad += bad_add;
   // operands outside the domain are reported
   const double outside[] = {0.0, -0.0, 5e-324, 2.2250738585072014e-308, INFINITY, -INFINITY, NAN,
                             make(0, 511, 0), make(0, 1535, 0)};

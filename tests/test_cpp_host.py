@@ -36,9 +36,11 @@ def test_cpp_rng_matches_oracle(program, seed):
 
 
 def test_integer_pipe_product_host(tmp_path):
-    """The integer-pipe double product (everett_gb300/csrc/ev_softfp.cuh),
-    compiled for the host, equals the host's IEEE multiplication on 2*10^7
-    operand pairs from families that reach every rounding case."""
+    """The integer-pipe double product and add (everett_gb300/csrc/
+    ev_softfp.cuh), compiled for the host, equal the host's IEEE
+    multiplication and addition on 2*10^7 operand pairs each from families
+    that reach every rounding case (sums: also cancellation and exponent gaps
+    at the alignment's edges)."""
     import shutil
     from pathlib import Path
     root = Path(__file__).resolve().parents[1]
@@ -54,3 +56,4 @@ def test_integer_pipe_product_host(tmp_path):
                            timeout=300)
         assert r.returncode == 0, r.stdout + r.stderr
         assert ", 0 mismatches" in r.stdout, r.stdout
+        assert ", 0 sum mismatches" in r.stdout, r.stdout

@@ -343,6 +343,22 @@ def test_integer_pipe_product_matches_fp64_pipe(gpu):
         assert bad.value == 0, (seed, bad.value)
 
 
+def test_integer_pipe_add_matches_fp64(gpu):
+    """The integer-pipe double add (softfp::add) gives the FP64 add's bits on
+    2^28 operand pairs per seed: the product check's families, cancellation
+    (opposite signs, changed low bits) and exponent gaps of 50..66 with random
+    or empty fractions (the alignment's edges, exact ties)."""
+    import ctypes as C
+    from everett_gb300 import _native as N
+    for seed in (1, 2):
+        bad = C.c_uint64(7)
+        N.check(N.lib().ev_softfp_add_check(seed, 1 << 28, C.byref(bad)))
+        assert bad.value == 0, (seed, bad.value)
+    rate = C.c_double()
+    N.check(N.lib().ev_probe_softadd(C.byref(rate)))
+    assert rate.value > 0
+
+
 def test_double_float_rounding_matches_fp64_add(gpu):
     """The complex64 sampling tree rounds each leaf's double-float pair to
     f64 on the integer pipes; on 2^28 pairs per seed (exponent gaps 0..80,
@@ -355,10 +371,11 @@ def test_double_float_rounding_matches_fp64_add(gpu):
         assert bad.value == 0, (seed, bad.value)
 
 
-@pytest.mark.parametrize("level", ["00", "11", "22", "21", "12"])
+@pytest.mark.parametrize("level", ["00", "11", "22", "21", "12", "32", "42", "62"])
 def test_tiled_integer_pipe_levels_bit_exact(gpu, monkeypatch, level):
     """Every level of the complex128 tile passes' integer-pipe products
-    (none, one amplitude per pair, both) gives the oracle's bits, including
+    (none, one amplitude per pair, both) and of real records' adds (one, two
+    or all four output parts of a pair) gives the oracle's bits, including
     pairs that leave the fast path: zeros of the initial state, gate entries
     and amplitudes below 2^-511."""
     monkeypatch.setenv("EV_TILE_SOFT", level)
