@@ -8,6 +8,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <type_traits>
@@ -272,6 +273,16 @@ __device__ __forceinline__ void pair_fp(const double* mm, V& a0, V& a1) {
   using R = typename Real<V>::T;
   if constexpr (K1 == K1_DENSE) {
     const V m0 = ldm<V>(mm, 0), m1 = ldm<V>(mm, 1), m2 = ldm<V>(mm, 2), m3 = ldm<V>(mm, 3);
+    if constexpr (std::is_same<V, float2>::value) {
+      // Rx-like complex64 records, as in tile_1q_fp64
+      if (m0.y == 0.f && m3.y == 0.f && m1.x == 0.f && m2.x == 0.f) {
+        const float2 n0 = make_float2(__fmaf_rn(m0.x, a0.x, -(m1.y * a1.y)),
+                                      __fmaf_rn(m0.x, a0.y, m1.y * a1.x));
+        a1 = make_float2(__fmaf_rn(m3.x, a1.x, -(m2.y * a0.y)), __fmaf_rn(m3.x, a1.y, m2.y * a0.x));
+        a0 = n0;
+        return;
+      }
+    }
     const V n0 = cadd(cmul(m0, a0), cmul(m1, a1));
     a1 = cadd(cmul(m2, a0), cmul(m3, a1));
     a0 = n0;
@@ -464,6 +475,14 @@ __device__ void tile_diag_chain(V* t, uint32_t size, const Op* ops, int run, con
           const uint32_t l = l0 + j * nb;
           if ((l & b0) && (l & b1)) a[j] = cneg(a[j]);
         }
+      } else if (op.k1 == 1) {  // parity-diagonal T_DIAG2: entry 0 or 5 by the bits' parity
+        const uint32_t p0 = op.p0, p1 = op.p1;
+        const V d0 = ldm<V>(mm, 0), d1 = ldm<V>(mm, 5);
+#pragma unroll
+        for (int j = 0; j < CH; ++j) {
+          const uint32_t l = l0 + j * nb;
+          a[j] = cmul((((l >> p0) ^ (l >> p1)) & 1u) ? d1 : d0, a[j]);
+        }
       } else {  // T_DIAG2: entry 5c with c = 2 * bit(p0) + bit(p1), as tile_2q maps them
         const uint32_t b1 = 1u << op.p1;
         const V d0 = ldm<V>(mm, 0), d1 = ldm<V>(mm, 5), d2 = ldm<V>(mm, 10), d3 = ldm<V>(mm, 15);
@@ -596,7 +615,19 @@ inline void encode_op(const ev_circuit* c, const ev_op& op, uint64_t tset, const
       case K2_CNOT: out->kind = T_CNOT; break;
       case K2_CZ: out->kind = T_CZ; break;
       case K2_SWAP: out->kind = T_SWAP; break;
-      case K2_DIAG: out->kind = T_DIAG2; break;
+      case K2_DIAG: {
+        out->kind = T_DIAG2;
+        // k1 = 1 marks a parity-diagonal record (entries 0 and 15 equal, 5
+        // and 10 equal: Rzz and its kin), whose entry is picked by the
+        // parity of the two bits alone
+        const double* m = op.m;
+        out->k1 = uint8_t(m[0] == m[30] && m[1] == m[31] && m[10] == m[20] && m[11] == m[21] &&
+                          std::signbit(m[0]) == std::signbit(m[30]) &&
+                          std::signbit(m[1]) == std::signbit(m[31]) &&
+                          std::signbit(m[10]) == std::signbit(m[20]) &&
+                          std::signbit(m[11]) == std::signbit(m[21]));
+        break;
+      }
       default: out->kind = T_DENSE2; break;
     }
     out->p0 = uint8_t(local[op.q0]);
