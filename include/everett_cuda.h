@@ -180,9 +180,10 @@ int ev_measure_qubit(ev_state* s, uint64_t k, double u, int32_t* outcome);
  * exits.  n <= 40 (EV_ERR_INVALID_ARGUMENT beyond).  The buffer must be
  * 16-byte aligned device (or managed) memory of the current device holding
  * 2^n amplitudes; anything else is EV_ERR_INVALID_ARGUMENT before any launch.
- * stream may be NULL (legacy default stream); the call returns after the
- * measurement has completed.  The first call in a CUDA context resolves the
- * array's device address there, so make it before any stream capture.  Calls
+ * stream may be NULL (legacy default stream).  The call synchronises that
+ * stream and returns after the measurement has completed, so it cannot be
+ * recorded into a CUDA graph (not during a stream capture either).  Its
+ * device address of the scratch array is resolved per CUDA context.  Calls
  * share the array: calls that overlap on the GPU race, ordered calls do not. */
 int ev_measure_qubit_noalloc(double* amps, uint64_t n, uint64_t k, double u,
                              void* stream, int32_t* outcome);
