@@ -267,7 +267,7 @@ __device__ void batch_measure(V* tile, uint32_t size, int q, uint32_t cbit, doub
 }
 
 // Compiled per block size: 256-thread CTAs, three of which fit an SM's
-// shared memory with the default tile, get 85 registers a thread; 512-thread
+// shared memory with the default tile, get 80 registers a thread; 512-thread
 // CTAs (two per SM) 64.
 template <typename V, int NT>
 __global__ void __launch_bounds__(NT, NT == 256 ? 3 : 2) k_batch(BatchArgs a, int kmax) {

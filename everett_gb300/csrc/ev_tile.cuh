@@ -41,9 +41,9 @@ struct __align__(16) TileOp {
                    // pair, 2 both; real-matrix records 3..6: both, and the
                    // adds of the first soft - 2 output parts too
   uint32_t lmask;  // local control mask
-  uint8_t run;     // records from this one on that form a chain (T_1Q
-                   // records on the same target with the same controls,
-                   // applied pair by pair in registers); 0 or 1: none
+  uint8_t run;     // records from this one on that form a chain (ctype:
+                   // pair, quad or diagonal, applied in registers); 0 or 1:
+                   // none
   uint8_t sok;     // complex128 T_1Q: the factors in m[8..15] are in the
                    // integer-pipe product's domain (SoftM1::ok)
   uint8_t ctype;   // first record of a chain (run > 1): ChainKind
