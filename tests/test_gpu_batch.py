@@ -106,6 +106,47 @@ def classical_mix(seed):
     return out
 
 
+def window_edge_circuits():
+    """Circuits whose measurements and IfClassic prefixes fall on the edges
+    of the batch kernel's 16-record windows: a prefix as the last record of
+    a window with the op it gates in the next one, a measurement as the
+    first record of a window, nested prefixes across an edge."""
+    out = []
+    for pad in (14, 15, 16, 30, 31):
+        c = Circuit.with_classical(6, 2)
+        c.h(0).cnot(0, 1)
+        c.measure(0, 0)
+        for j in range(pad):
+            c.rz(2 + j % 4, 0.1 * (j + 1))
+        c.x_if(0, 3)
+        c.if_classic(0, IfClassic(0, Apply1(Gate1.ry(0.7), 4)))
+        c.measure(3, 1)
+        c.z_if(1, 5)
+        out.append(c)
+    return out
+
+
+@pytest.mark.parametrize("dtype", ["complex128", "complex64"])
+def test_batch_classical_records_across_windows(gpu, dtype):
+    """Measurements and IfClassic prefixes give the oracle's classical bits
+    and amplitudes wherever they fall relative to the record windows."""
+    circs = window_edge_circuits()
+    run_seeds = [5 + 3 * i for i in range(len(circs))]
+    res, _ = batch.run_batch(circs, seeds=range(len(circs)), shots=50, dtype=dtype,
+                             tile_bits=10, threads=256, return_states=True,
+                             run_seeds=run_seeds)
+    for i, (c, r) in enumerate(zip(circs, res)):
+        want, bits, rc = O.run_seeded(c, run_seeds[i])
+        assert rc == 0
+        assert r.classical == bits, i
+        got = r.amplitudes
+        if dtype == "complex128":
+            assert np.max(np.abs(got - want)) < 1e-12, i
+        else:
+            fid = abs(np.vdot(want, got)) ** 2 / (np.vdot(got, got).real * np.vdot(want, want).real)
+            assert fid >= 1 - 1e-6, i
+
+
 @pytest.mark.parametrize("dtype", ["complex128", "complex64"])
 def test_batch_measurement_and_classical_control(gpu, dtype):
     circs = classical_mix(4)
