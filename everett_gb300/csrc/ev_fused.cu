@@ -1174,8 +1174,15 @@ __global__ void __launch_bounds__(kOzThreads, 1)
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int n = half * 32 + (part & 1) * 16 + c0 + 2 * j;
-        const double re = oz::scaled(acc[2 * j], rem + fexp[n] - oz::Fmt<ND>::kPow2Bias);
-        const double im = oz::scaled(acc[2 * j + 1], rem + fexp[n + 1] - oz::Fmt<ND>::kPow2Bias);
+        // three outputs in four converted on the FP64 pipe, which is idle
+        // while the integer pipes recombine, the fourth on the integer pipes:
+        // the same values either way.  30 qubits, ms per run (seven / six
+        // digits): all on the integer pipes 903 / 865, half on FP64 838 /
+        // 800, three quarters 825 / 771, all 832 / 766
+        const int p_re = rem + fexp[n] - oz::Fmt<ND>::kPow2Bias;
+        const int p_im = rem + fexp[n + 1] - oz::Fmt<ND>::kPow2Bias;
+        const double re = oz::scaled_fp64(acc[2 * j], p_re);
+        const double im = (j & 1) ? oz::scaled_fp64(acc[2 * j + 1], p_im) : oz::scaled(acc[2 * j + 1], p_im);
         __stcs(s + (rbase | d.ftab[n >> 1]), make_double2(re, im));
       }
     }

@@ -267,6 +267,21 @@ __host__ __device__ __forceinline__ double scaled(int64_t acc, int pow2) {
   return y;
 }
 
+#ifdef __CUDACC__
+// The same value as scaled(), formed on the FP64 pipe: the conversion of acc
+// rounds to nearest even as scaled() does, and a power-of-two scaling that
+// keeps the result normal is exact, an exponent-field add.  The complex128
+// fused pass sends part of its outputs here, where the FP64 pipe is idle
+// while the integer pipes recombine.
+__device__ __forceinline__ double scaled_fp64(int64_t acc, int pow2) {
+  const double x = __ll2double_rn(acc);
+  const uint64_t b = uint64_t(__double_as_longlong(x));
+  const int e = int((b >> 52) & 0x7FFu);
+  if (acc == 0 || e + pow2 <= 0 || e + pow2 >= 2047) return acc == 0 ? 0.0 : scalbn(x, pow2);
+  return __longlong_as_double((long long)(b + (uint64_t(int64_t(pow2)) << 52)));
+}
+#endif
+
 // Largest biased exponent among 64-bit values given by their high words.
 __host__ __device__ __forceinline__ int exp_of(uint32_t hi) { return int((hi >> 20) & 0x7FFu); }
 
