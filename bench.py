@@ -346,8 +346,7 @@ def extras_c64(L, N, ref_state, circuit, c128_ms, bytes_per_step, peak, peak_kin
         ms, prof = timed_runs(L, N, st, circuit, 3, **kw)
         roof = roofline_of(prof, "fused_unitary", 2.0 * (1 << n) * 8, peak, peak_kind,
                            f"k_fused_tc<5,{variant}> (fused 5-qubit unitary, tcgen05)",
-                           ncu_figure("k_fused_tc_bf16x3", "traffic_bytes_per_launch_full_size")
-                           if variant == "bf16x3" else None)
+                           ncu_figure(f"k_fused_tc_{variant}", "traffic_bytes_per_launch_full_size"))
         if roof:
             # 3 split products of a 64 x 64 real GEMM per row of 32 amplitudes:
             # 3 * 2 * 64 * 64 / 32 = 768 flops per amplitude (TF32 runs at half
